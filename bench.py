@@ -1,0 +1,328 @@
+"""Benchmark: batched CCM S-map/simplex predictions per second on GB300.
+
+Workload (one step): convergent cross mapping x -> y on a seeded coupled
+logistic map, T = 50000, E = 4, 20 log-spaced library sizes 100..40000, 200
+random-library replicates, simplex (k = E+1) and S-map (theta = 2, k = E+2)
+-- two fedm_run_command calls, 2 x 20 x 200 x 49997 ~= 4.0e8 forecasts.
+
+  value  forecasts / device time (inputs uploaded, first kernel to statistics)
+  e2e    forecasts / wall time of the C ABI calls from host buffers (host
+         preparation, splitter, uploads, kernels, downloads)
+
+Also reported: the plain FP64 GPU form and |delta rho| against it on a
+2-replicate sample, the roofline of the dominant kernel against the measured
+FP32 FFMA peak, and the CPU oracle on a bounded sample.  `--impl reference`
+times the CPU restatement of the reference path (all host threads) instead.
+"""
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT / "tests"))
+METRIC = "CCM S-map predictions/s: batched FP32+FP64-fix vs plain FP64 GPU @|Δρ|≤1e-6"
+HBM_GBS = 6794.1
+
+
+def load_pkg():
+    from fedm_loader import fedm, workloads
+
+    return fedm, workloads
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("gloo")
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def allreduce_max(world, v):
+    if world == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([v], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+class Clocks:
+    """Samples SM clocks and throttle reasons while the timed region runs."""
+
+    def __init__(self, device):
+        self.device = device
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), "--query-gpu=clocks.sm,clocks.max.sm,power.draw,"
+                 "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
+                 "--format=csv,noheader,nounits", "-lms", "200"], stdout=subprocess.PIPE, text=True)
+            self.th = threading.Thread(target=self._read, daemon=True)
+            self.th.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([v.strip() for v in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in self.rows:
+            try:
+                sm.append(float(r[0]))
+                mx = float(r[1])
+                for nm, v in zip(names, r[3:7]):
+                    if v.lower() == "active":
+                        reasons.add(nm)
+            except (ValueError, IndexError):
+                pass
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def flush_l2(device):
+    import torch
+
+    buf = torch.empty(512 << 20, dtype=torch.uint8, device=f"cuda:{device}")
+    buf.zero_()
+    torch.cuda.synchronize(device)
+    del buf
+
+
+def ccm_args(fedm, w, algorithm, reps, libraries=None):
+    return fedm.normalise(w["t"], w["x"], w["y"], E=w["E"], library=libraries or w["libraries"], numReps=reps,
+                          seed=w["seed"], algorithm=algorithm, theta=2.0 if algorithm == "smap" else 1.0)
+
+
+def algorithmic_units(w, reps):
+    """Pairs and bytes the distance/neighbour step must touch per step."""
+    E = w["E"]
+    npred = w["n_pred"]
+    pairs = 0
+    bytes_ = 0
+    for L in w["libraries"]:
+        pairs += npred * L
+        for k in (E + 1, E + 2):
+            bytes_ += 4 * E * (L + npred) + 4 * L + 12 * k * npred
+    return 2 * reps * pairs, reps * bytes_
+
+
+def run_ours(a):
+    fedm, workloads = load_pkg()
+    world, rank, local = dist_setup()
+    w = workloads.ccm_config(T=a.T, reps=a.reps, n_libs=a.n_libs, hi=a.lib_max)
+    w["n_pred"] = a.T - (w["E"] - 1)
+    ctx = fedm.Context(local, precision=fedm.PRECISION_MIXED)
+    fp32_peak = ctx.measure_peak(0)
+    calls = [ccm_args(fedm, w, alg, a.reps) for alg in ("simplex", "smap")]
+
+    def step():
+        tot = dict(device_ms=0.0, knn_kernel_ms=0.0, knn_launches=0, predictions=0, distance_pairs=0,
+                   h2d_bytes=0, d2h_bytes=0, fallback_points=0, kernel_launches=0, wall_ms=0.0)
+        rhos = []
+        for args in calls:
+            t0 = time.perf_counter()
+            r = ctx.run_command(args)
+            tot["wall_ms"] += (time.perf_counter() - t0) * 1e3
+            if r["rc"] != 0:
+                raise RuntimeError(f"run_command rc={r['rc']}: {r.get('error')}")
+            tm = ctx.timing()
+            for k in tot:
+                if k != "wall_ms":
+                    tot[k] += tm[k]
+            rhos.append(r["stats"]["rho"])
+        return tot, rhos
+
+    for _ in range(max(3, a.warmup)):
+        step()
+        flush_l2(local)
+    per_step = []
+    barrier(world)
+    with Clocks(local) as clk:
+        for _ in range(a.steps):
+            tot, rhos = step()
+            per_step.append(tot)
+            flush_l2(local)
+    barrier(world)
+    dev_s = sum(s["device_ms"] for s in per_step) / 1e3
+    wall_s = sum(s["wall_ms"] for s in per_step) / 1e3
+    preds = sum(s["predictions"] for s in per_step)
+    dev_s_max = allreduce_max(world, dev_s)
+    wall_s_max = allreduce_max(world, wall_s)
+    if rank != 0:
+        return
+    s0 = per_step[0]
+    value = preds * world / dev_s_max
+    e2e = preds * world / wall_s_max
+    pairs, alg_bytes = algorithmic_units(w, a.reps)
+    knn_ms_step = statistics.mean(s["knn_kernel_ms"] for s in per_step)
+    launches_step = statistics.mean(s["knn_launches"] for s in per_step)
+    flops_step = 3.0 * w["E"] * pairs
+    achieved = flops_step / launches_step / (knn_ms_step / launches_step * 1e-3) / 1e12
+    traffic = None
+    prof = ROOT / "profiles" / "knn_mixed_ccm_traffic.json"
+    if prof.exists():
+        pj = json.loads(prof.read_text())
+        traffic = pj.get("bytes_per_full_launch")
+
+    # plain FP64 GPU form and |delta rho| on a 2-replicate sample
+    sample_reps = 2
+    ctx64 = fedm.Context(local, precision=fedm.PRECISION_FP64)
+    t_fp64 = 0.0
+    p_fp64 = 0
+    drho = 0.0
+    for alg in ("simplex", "smap"):
+        args = ccm_args(fedm, w, alg, sample_reps)
+        r64 = ctx64.run_command(args)
+        tm = ctx64.timing()
+        t_fp64 += tm["device_ms"] / 1e3
+        p_fp64 += tm["predictions"]
+        rmx = ctx.run_command(args)
+        drho = max(drho, float(np.max(np.abs(np.asarray(r64["stats"]["rho"]) - np.asarray(rmx["stats"]["rho"])))))
+    ctx64.close()
+    fp64_value = p_fp64 / t_fp64
+
+    cpu = None
+    if world == 1 and not a.no_cpu:
+        cpu = cpu_baseline(fedm, w, a)
+
+    clocks = clk.summary()
+    out = {
+        "metric": METRIC, "value": value, "unit": "predictions/s", "n_gpus": world, "steps": a.steps,
+        "warmup": max(3, a.warmup), "ms_per_step": dev_s_max / a.steps * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "fp32+fp64", "data": "synthetic (seeded coupled logistic map)",
+        "config": {
+            "workload": f"ccm_xmap_T{a.T}_E4_L{a.n_libs}x100-{a.lib_max}_reps{a.reps}_simplex+smap",
+            "T": a.T, "E": w["E"], "libraries": w["libraries"], "replicates": a.reps,
+            "algorithms": ["simplex k=E+1", "smap theta=2 k=E+2"], "predictions_per_step": preds // a.steps,
+            "l2": "flushed between steps (512 MiB write)", "parallelism": f"replicas x{world}",
+        },
+        "e2e": {"value": e2e, "unit": "predictions/s", "h2d_bytes_per_step": int(s0["h2d_bytes"]),
+                "d2h_bytes_per_step": int(s0["d2h_bytes"]), "wall_ms_per_step": wall_s_max / a.steps * 1e3},
+        "gpu_launches": int(sum(s["kernel_launches"] for s in per_step)),
+        "roofline": {
+            "kernel": "knn_mixed_kernel (FP32 scan + FP64 re-rank + forecast)", "bound": "fp32_simt",
+            "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s", "frac": achieved / fp32_peak,
+            "peak_source": "measured FFMA peak of this GPU (fedm_measure_peak), not in MEASURED_PEAKS.json",
+            "algorithmic_flops_per_step": flops_step, "traffic": traffic,
+            "hbm": {"achieved_gbs": alg_bytes / (knn_ms_step * 1e-3) / 1e9, "peak_gbs": HBM_GBS,
+                    "frac": alg_bytes / (knn_ms_step * 1e-3) / 1e9 / HBM_GBS, "peak_source": "MEASURED_PEAKS.json"},
+        },
+        "fp64_plain": {"value": fp64_value, "unit": "predictions/s", "sample": f"{sample_reps} replicates, both algorithms",
+                       "mixed_over_fp64": value / fp64_value, "max_abs_drho_vs_fp64": drho},
+        "fallback_points_per_step": int(s0["fallback_points"]),
+        "clocks": clocks,
+        "cpu_baseline": cpu,
+    }
+    print(json.dumps(out), flush=True)
+
+
+def cpu_baseline(fedm, w, a, reps=1, n_libs=None):
+    """The oracle (CPU restatement of the reference path), all host threads."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import edm_oracle
+
+    cores = os.cpu_count() or 1
+    libs = w["libraries"] if n_libs is None else w["libraries"][:n_libs]
+    t0 = time.perf_counter()
+    preds = 0
+    for alg in ("simplex", "smap"):
+        args = edm_oracle.normalise(w["t"], w["x"], w["y"], E=w["E"], library=libs, numReps=reps, seed=w["seed"],
+                                    algorithm=alg, theta=2.0 if alg == "smap" else 1.0, numThreads=cores)
+        r = edm_oracle.run_command(args)
+        if r["rc"] != 0:
+            raise RuntimeError(f"oracle rc={r['rc']}")
+        preds += len(r["stats"]["rho"]) * w["n_pred"]
+    dt = time.perf_counter() - t0
+    return {"value": preds / dt, "unit": "predictions/s", "cores": cores, "kind": "port",
+            "sample": f"{reps} replicate(s) x {len(libs)} library sizes, simplex + smap ({preds} forecasts, {dt:.1f} s)"}
+
+
+def run_reference(a):
+    world, rank, local = dist_setup()
+    if rank != 0:
+        return
+    _, workloads = load_pkg()
+    w = workloads.ccm_config(T=a.T, reps=a.reps, n_libs=a.n_libs, hi=a.lib_max)
+    w["n_pred"] = a.T - (w["E"] - 1)
+    for _ in range(max(3, a.warmup)):
+        cpu_baseline(None, w, a, reps=1, n_libs=a.ref_libs)
+    vals = []
+    last = None
+    for _ in range(a.steps):
+        last = cpu_baseline(None, w, a, reps=1, n_libs=a.ref_libs)
+        vals.append(last["value"])
+    v = statistics.mean(vals)
+    out = {
+        "impl": "reference", "metric": METRIC, "value": v, "unit": "predictions/s", "n_gpus": world,
+        "steps": a.steps, "warmup": max(3, a.warmup), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "fp64", "data": "synthetic (seeded coupled logistic map)",
+        "config": {"workload": f"ccm_xmap_T{a.T}_E4_L{a.n_libs}x100-{a.lib_max}_reps{a.reps}_simplex+smap",
+                   "T": a.T, "E": w["E"], "libraries": w["libraries"], "replicates": a.reps,
+                   "sample_per_step": last["sample"]},
+        "cpu_baseline": {"value": v, "unit": "predictions/s", "cores": last["cores"], "kind": "port",
+                         "sample": last["sample"]},
+        "e2e": {"value": v, "unit": "predictions/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--T", type=int, default=50000)
+    ap.add_argument("--reps", type=int, default=200)
+    ap.add_argument("--n-libs", dest="n_libs", type=int, default=20)
+    ap.add_argument("--lib-max", dest="lib_max", type=int, default=40000)
+    ap.add_argument("--ref-libs", dest="ref_libs", type=int, default=None,
+                    help="library sizes in each CPU reference sample (default: all)")
+    ap.add_argument("--no-cpu", action="store_true")
+    a = ap.parse_args()
+    if a.impl == "reference":
+        run_reference(a)
+    else:
+        run_ours(a)
+
+
+if __name__ == "__main__":
+    main()

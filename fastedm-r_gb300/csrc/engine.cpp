@@ -1,0 +1,1034 @@
+// The run_command pipeline on one GB300.
+//
+// Host: clean the series, build the generator, configure every task with
+// the reference's splitter (src/edm.cpp:90-212), build one manifold per E for
+// all rows, turn each task's masks into row lists.  Device: one batched
+// launch sequence per (E, coprediction) group over the point space of all
+// its tasks, chunked to bound scratch memory; rho/MAE per (task, theta) on the
+// device; only the statistics and the saved forecasts come back.
+#include "engine.h"
+
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <climits>
+#include <cmath>
+#include <cstring>
+#include <numeric>
+#include <thread>
+#include <unordered_map>
+
+namespace fedm {
+
+// Device helpers (kernels_util.cu).
+void fill_f64(double* p, long long n, double v, cudaStream_t s);
+void fill_i32(int* p, long long n, int v, cudaStream_t s);
+void to_f32(const double* src, float* dst, long long n, cudaStream_t s);
+
+namespace {
+
+void ck(cudaError_t e, const char* what)
+{
+  if (e != cudaSuccess)
+    throw Error{ RC_UNKNOWN_ERROR, std::string(what) + ": " + cudaGetErrorString(e) };
+}
+
+double now_ms()
+{
+  using namespace std::chrono;
+  return duration<double, std::milli>(steady_clock::now().time_since_epoch()).count();
+}
+
+} // namespace
+
+// ------------------------------------------------------------------ Context
+Context::Context(int dev) : device(dev)
+{
+  ck(cudaSetDevice(dev), "cudaSetDevice");
+  ck(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), "cudaStreamCreate");
+  ck(cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, dev), "cudaDeviceGetAttribute");
+}
+
+Context::~Context()
+{
+  cudaSetDevice(device);
+  for (auto& kv : bufs_)
+    if (kv.second.p)
+      cudaFree(kv.second.p);
+  if (stream)
+    cudaStreamDestroy(stream);
+}
+
+void* Context::buf(const std::string& name, size_t bytes)
+{
+  DevBuf& b = bufs_[name];
+  if (bytes == 0)
+    bytes = 16;
+  if (b.cap < bytes) {
+    if (b.p) {
+      ck(cudaStreamSynchronize(stream), "sync before realloc");
+      ck(cudaFree(b.p), "cudaFree");
+      b.p = nullptr;
+      b.cap = 0;
+    }
+    size_t want = bytes + bytes / 8;
+    ck(cudaMalloc(&b.p, want), ("cudaMalloc " + name).c_str());
+    b.cap = want;
+  }
+  return b.p;
+}
+
+void Context::upload(void* dst, const void* src, size_t bytes)
+{
+  if (bytes) {
+    ck(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, stream), "H2D");
+    timing.h2d_bytes += (long long)bytes;
+  }
+}
+
+void Context::download(void* dst, const void* src, size_t bytes)
+{
+  if (bytes) {
+    ck(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, stream), "D2H");
+    timing.d2h_bytes += (long long)bytes;
+  }
+}
+
+void Context::check(const char* what)
+{
+  ck(cudaGetLastError(), what);
+}
+
+namespace {
+
+// ------------------------------------------------------------ preparation
+struct Prepared
+{
+  Generator gen;
+  Options opts;
+  bool explore = true;
+  std::vector<int> Es, libraries;
+};
+
+void prepare(const fedm_args& a, Prepared& P)
+{
+  // src/r.cpp:119-246
+  Options& o = P.opts;
+  o.missing_distance = a.missing_distance;
+  o.low_memory = a.low_memory;
+  o.past_only = a.predict_with_past;
+  if (a.n_thetas > 0 && a.thetas)
+    o.thetas.assign(a.thetas, a.thetas + a.n_thetas);
+  else
+    o.thetas = { 1.0 };
+  if (a.nE <= 0 || !a.Es)
+    throw Error{ RC_UNKNOWN_ERROR, "no E values" };
+  if (a.n <= 0 || !a.t || !a.x)
+    throw Error{ RC_UNKNOWN_ERROR, "empty series" };
+  P.Es.assign(a.Es, a.Es + a.nE);
+  for (int E : P.Es)
+    if (E <= 0)
+      throw Error{ RC_UNKNOWN_ERROR, "E must be positive" };
+  if (a.libs)
+    P.libraries.assign(a.libs, a.libs + a.n_libs);
+  if (a.algorithm != 0 && a.algorithm != 1)
+    throw Error{ RC_INVALID_ALGORITHM, "unknown algorithm" };
+  o.algorithm = a.algorithm;
+  o.distance = 1;
+  Generator& g = P.gen;
+  g.n = a.n;
+  g.t = clean_vector(a.t, a.n);
+  g.x = clean_vector(a.x, a.n);
+  for (int i = 0; i < a.n; i++)
+    if (g.t[i] == MISSING_D)
+      g.x[i] = MISSING_D;
+  if (a.y) {
+    g.xmap = clean_vector(a.y, a.n);
+    P.explore = false;
+  }
+  o.idw = a.panel_weight;
+  if (a.panel) {
+    g.panel.assign(a.panel, a.panel + a.n);
+    o.panel_mode = true;
+    if (a.panel_weights) {
+      std::vector<int> uniq(g.panel);
+      uniq.erase(std::unique(uniq.begin(), uniq.end()), uniq.end());
+      const int m = a.n_panel_weights;
+      for (int i = 0; i < (int)uniq.size(); i++)
+        for (int j = 0; j < (int)uniq.size(); j++)
+          if (i < m && j < m)
+            o.id_weights[{ uniq[i], uniq[j] }] = (float)a.panel_weights[i + (size_t)j * m];
+      o.has_id_weights = !o.id_weights.empty();
+      o.idw = 0;
+    }
+  }
+  if (a.co_x)
+    g.co_x = clean_vector(a.co_x, a.n);
+  for (int e = 0; e < a.num_extras; e++)
+    g.extras.push_back(clean_vector(a.extras + (size_t)e * a.n, a.n));
+  g.tau = a.tau;
+  g.p = a.p;
+  g.num_extras_lagged = 0;
+  g.dt = a.dt;
+  g.reldt = a.reldt;
+  g.allow_missing = a.allow_missing;
+  g.init(a.dt_weight);
+  o.has_missing = a.allow_missing;
+  if (a.allow_missing && o.missing_distance == 0) {
+    // src/stats.cpp:103-108 on the cleaned x
+    o.missing_distance = 2 / std::sqrt(3.14159265358979323846) * sd_observed(g.x);
+  }
+}
+
+int host_threads(const fedm_args& a)
+{
+  int hw = (int)std::thread::hardware_concurrency();
+  int t = std::max(a.num_threads, hw > 0 ? hw : 1);
+  return std::min(t, 64);
+}
+
+// Device copies of the per-row tables, shared by every group of a run.
+struct DevRows
+{
+  double* lib_target;
+  double* co_target;
+  double* lib_target_time;
+  double* point_time;
+  int* panel;
+  int* panel_dense;
+  float* id_w;
+  int n_pid;
+  int n_rows;
+};
+
+DevRows upload_rows(Context& ctx, const Generator& g, const RowTables& rt, const Options& o)
+{
+  DevRows d{};
+  const size_t n = (size_t)g.n;
+  d.n_rows = g.n;
+  d.lib_target = (double*)ctx.buf("lib_target", n * 8);
+  d.co_target = (double*)ctx.buf("co_target", n * 8);
+  d.lib_target_time = (double*)ctx.buf("lib_target_time", n * 8);
+  d.point_time = (double*)ctx.buf("point_time", n * 8);
+  ctx.upload(d.lib_target, rt.lib_target.data(), n * 8);
+  ctx.upload(d.co_target, rt.co_target.data(), n * 8);
+  ctx.upload(d.lib_target_time, rt.lib_target_time.data(), n * 8);
+  ctx.upload(d.point_time, rt.point_time.data(), n * 8);
+  if (g.panel_mode) {
+    d.panel = (int*)ctx.buf("panel", n * 4);
+    ctx.upload(d.panel, g.panel.data(), n * 4);
+    if (o.has_id_weights) {
+      std::vector<int> ids(g.panel);
+      std::sort(ids.begin(), ids.end());
+      ids.erase(std::unique(ids.begin(), ids.end()), ids.end());
+      std::unordered_map<int, int> dense;
+      for (int i = 0; i < (int)ids.size(); i++)
+        dense[ids[i]] = i;
+      std::vector<int> pd(n);
+      for (size_t i = 0; i < n; i++)
+        pd[i] = dense[g.panel[i]];
+      const int m = (int)ids.size();
+      std::vector<float> w((size_t)m * m, NAN);
+      for (int a = 0; a < m; a++)
+        for (int b = 0; b < m; b++) {
+          auto it = o.id_weights.find({ ids[a], ids[b] });
+          if (it != o.id_weights.end())
+            w[(size_t)a * m + b] = it->second;
+        }
+      d.panel_dense = (int*)ctx.buf("panel_dense", n * 4);
+      d.id_w = (float*)ctx.buf("id_w", w.size() * 4);
+      ctx.upload(d.panel_dense, pd.data(), n * 4);
+      ctx.upload(d.id_w, w.data(), w.size() * 4);
+      d.n_pid = m;
+    }
+  }
+  return d;
+}
+
+// Outcome of one task.
+struct TaskOut
+{
+  int rc = 0;
+  int kmin = MISSING_I, kmax = MISSING_I;
+  std::vector<double> rho, mae;
+  std::vector<double> pred_last;  // saved forecasts (last theta), one per prediction row of the task
+  std::vector<double> coeffs;     // [n_pred x (Ea+1)]
+  // detail (single-task seam only)
+  std::vector<double> pred_all;   // [n_thetas x n_pred]
+  std::vector<int> kused;         // [n_pred]
+  std::vector<int> nn_offsets, nn_idx;
+  std::vector<double> nn_dist;
+};
+
+struct GroupJob
+{
+  int Ea = 0;
+  const double* dF = nullptr;   // library manifold on the device
+  const double* dFp = nullptr;  // prediction manifold on the device
+  const float* dF32 = nullptr;
+  const std::vector<double>* hF = nullptr;   // host copies (mixed-path margin)
+  const std::vector<double>* hFp = nullptr;
+  bool copredict = false;
+  std::vector<int> task_ids;    // indices into the run's task list
+  std::vector<const std::vector<int>*> lib_lists, pred_lists;
+  bool detail = false;          // keep per-point outputs and neighbour lists
+  bool knn_for_all = false;     // route all-neighbour tasks through the list path
+};
+
+constexpr int KCAP_MAX = 16384;
+constexpr int MIX_KMAX = 14;        // neighbours the mixed kernel serves (slots C = 16)
+constexpr int MIX_POINTS = 512;     // prediction points per mixed work item
+constexpr long long FB_CAP = 1 << 24;
+
+// Whether the mixed kernel's preconditions hold for a group (see
+// kernels_mixed.cu): L2, no missing values in any used row, no panel
+// penalty or restriction, no past-only rule, Ea <= 8.  Also returns the
+// per-column centre and the largest centred row norm.
+bool mixed_eligible(const Context& ctx, const Options& o, const GroupJob& job, std::vector<double>& center,
+                    double& R)
+{
+  if (ctx.precision != FEDM_PRECISION_MIXED || o.distance != 1 || o.has_missing || o.low_memory || o.past_only ||
+      !o.force_compute || job.Ea > 8 || job.Ea < 1 || !job.hF || !job.hFp)
+    return false;
+  if (o.panel_mode && (o.idw != 0 || o.has_id_weights))
+    return false;
+  const int Ea = job.Ea;
+  std::vector<double> lo(Ea, INFINITY), hi(Ea, -INFINITY);
+  auto scan = [&](const std::vector<double>& F, const std::vector<int>& rows) {
+    for (int r : rows)
+      for (int j = 0; j < Ea; j++) {
+        const double v = F[(size_t)r * Ea + j];
+        if (v == MISSING_D || !std::isfinite(v))
+          return false;
+        lo[j] = std::min(lo[j], v);
+        hi[j] = std::max(hi[j], v);
+      }
+    return true;
+  };
+  std::vector<const std::vector<int>*> seen_l, seen_p;
+  for (size_t i = 0; i < job.lib_lists.size(); i++) {
+    if (std::find(seen_l.begin(), seen_l.end(), job.lib_lists[i]) == seen_l.end()) {
+      seen_l.push_back(job.lib_lists[i]);
+      if (!scan(*job.hF, *job.lib_lists[i]))
+        return false;
+    }
+    if (std::find(seen_p.begin(), seen_p.end(), job.pred_lists[i]) == seen_p.end()) {
+      seen_p.push_back(job.pred_lists[i]);
+      if (!scan(*job.hFp, *job.pred_lists[i]))
+        return false;
+    }
+  }
+  center.assign(Ea, 0.0);
+  for (int j = 0; j < Ea; j++)
+    if (lo[j] <= hi[j])
+      center[j] = 0.5 * (lo[j] + hi[j]);
+  double r2 = 0;
+  for (int j = 0; j < Ea; j++) {
+    const double a = std::max(std::fabs(lo[j] - center[j]), std::fabs(hi[j] - center[j]));
+    r2 += a * a;
+  }
+  R = std::sqrt(r2) * 1.01;
+  return std::isfinite(R) && R < 1e15;
+}
+
+void run_group(Context& ctx, const Options& o, const std::vector<Task>& tasks, const DevRows& rows,
+               GroupJob& job, std::vector<TaskOut>& outs)
+{
+  const int nT = (int)job.task_ids.size();
+  if (nT == 0)
+    return;
+  const int Ea = job.Ea, n = Ea + 1;
+  const int nth = (int)o.thetas.size();
+  cudaStream_t s = ctx.stream;
+
+  std::vector<double> center;
+  double R = 0;
+  const bool mixed_group = mixed_eligible(ctx, o, job, center, R);
+
+  // task table and row pools
+  std::vector<DevTask> dt(nT);
+  std::unordered_map<const std::vector<int>*, int> lib_off, pred_off;
+  std::vector<int> lib_pool, pred_pool;
+  long long P = 0, max_nlib_all = 1;
+  int kcap = 1, kmix = 0;
+  bool any_finite = false, any_all = false, any_coeffs = false, any_mixed = false;
+  for (int j = 0; j < nT; j++) {
+    const Task& t = tasks[job.task_ids[j]];
+    const std::vector<int>* L = job.lib_lists[j];
+    const std::vector<int>* Pl = job.pred_lists[j];
+    auto it = lib_off.find(L);
+    if (it == lib_off.end()) {
+      it = lib_off.emplace(L, (int)lib_pool.size()).first;
+      lib_pool.insert(lib_pool.end(), L->begin(), L->end());
+    }
+    auto it2 = pred_off.find(Pl);
+    if (it2 == pred_off.end()) {
+      it2 = pred_off.emplace(Pl, (int)pred_pool.size()).first;
+      pred_pool.insert(pred_pool.end(), Pl->begin(), Pl->end());
+    }
+    DevTask& d = dt[j];
+    d.point_base = P;
+    d.lib_off = it->second;
+    d.n_lib = (int)L->size();
+    d.pred_off = it2->second;
+    d.n_pred = (int)Pl->size();
+    d.k = t.k;
+    d.task = j;
+    d.save_coeffs = t.save_coeffs || job.detail;
+    d.all_mode = (t.k < 0 || t.k >= d.n_lib) ? 1 : 0;
+    if (d.all_mode && job.knn_for_all && d.n_lib <= KCAP_MAX) {
+      d.all_mode = 0;
+      d.k = std::max(d.n_lib, 0);
+    }
+    if (!d.all_mode && d.k > KCAP_MAX)
+      throw Error{ RC_NOT_IMPLEMENTED, "k above the supported maximum of 16384 neighbours" };
+    d.mixed = (mixed_group && !d.all_mode && d.k >= 1 && d.k <= MIX_KMAX) ? 1 : 0;
+    if (d.all_mode) {
+      any_all = true;
+      max_nlib_all = std::max<long long>(max_nlib_all, d.n_lib);
+    } else if (d.mixed) {
+      any_mixed = true;
+      kmix = std::max(kmix, d.k);
+      kcap = std::max(kcap, d.k);  // fallback points use the exact list path
+    } else {
+      any_finite = true;
+      kcap = std::max(kcap, d.k);
+    }
+    any_coeffs |= (bool)d.save_coeffs && o.algorithm == 1;
+    P += d.n_pred;
+  }
+  if (Ea + 32 * (n + 1) + n * (n + 1) / 2 + n > 24000 && any_all && o.algorithm == 1)
+    throw Error{ RC_NOT_IMPLEMENTED, "embedding too wide for the all-neighbour S-map" };
+
+  DevTask* d_tasks = (DevTask*)ctx.buf("tasks", dt.size() * sizeof(DevTask));
+  int* d_lib = (int*)ctx.buf("lib_pool", std::max<size_t>(lib_pool.size(), 1) * 4);
+  int* d_pred = (int*)ctx.buf("pred_pool", std::max<size_t>(pred_pool.size(), 1) * 4);
+  double* d_thetas = (double*)ctx.buf("thetas", nth * 8);
+  ctx.upload(d_tasks, dt.data(), dt.size() * sizeof(DevTask));
+  ctx.upload(d_lib, lib_pool.data(), lib_pool.size() * 4);
+  ctx.upload(d_pred, pred_pool.data(), pred_pool.size() * 4);
+  ctx.upload(d_thetas, o.thetas.data(), nth * 8);
+
+  GroupParams g{};
+  g.F = job.dF;
+  g.Fp = job.dFp;
+  g.lib_target = rows.lib_target;
+  g.pred_target = job.copredict ? rows.co_target : rows.lib_target;
+  g.lib_target_time = rows.lib_target_time;
+  g.point_time = rows.point_time;
+  g.panel = rows.panel;
+  g.panel_dense = rows.panel_dense;
+  g.id_w = rows.id_w;
+  g.n_pid = rows.n_pid;
+  g.lib_rows = d_lib;
+  g.pred_rows = d_pred;
+  g.tasks = d_tasks;
+  g.n_tasks = nT;
+  g.Ea = Ea;
+  g.n_thetas = nth;
+  g.thetas = d_thetas;
+  g.algorithm = o.algorithm;
+  g.l1 = o.distance == 0;
+  // the lazy (lowMemory) distance always tests for missing values and has
+  // no past-only rule (src/distances.cpp:69-149)
+  g.has_missing = o.has_missing || o.low_memory;
+  g.missing_distance = o.missing_distance;
+  g.panel_mode = o.panel_mode;
+  g.idw = o.idw;
+  g.skip_other_panels = o.panel_mode && o.idw < 0;
+  g.has_id_weights = o.has_id_weights;
+  g.past_only = o.past_only && !o.low_memory;
+  g.force_compute = o.force_compute;
+  g.total_points = P;
+  g.pred = (double*)ctx.buf("pred", (size_t)std::max<long long>(P, 1) * nth * 8);
+  fill_f64(g.pred, P * nth, MISSING_D, s);
+  if (any_coeffs) {
+    g.coeffs = (double*)ctx.buf("coeffs", (size_t)std::max<long long>(P, 1) * n * 8);
+    fill_f64(g.coeffs, P * n, MISSING_D, s);
+  }
+  if (job.detail) {
+    g.kused = (int*)ctx.buf("kused", (size_t)std::max<long long>(P, 1) * 4);
+    fill_i32(g.kused, P, MISSING_I, s);
+  }
+  g.task_rc = (int*)ctx.buf("task_rc", nT * 4);
+  g.task_kmin = (int*)ctx.buf("task_kmin", nT * 4);
+  g.task_kmax = (int*)ctx.buf("task_kmax", nT * 4);
+  g.err_flag = (int*)ctx.buf("err_flag", 4);
+  fill_i32(g.task_rc, nT, 0, s);
+  fill_i32(g.task_kmin, nT, INT_MAX, s);
+  fill_i32(g.task_kmax, nT, INT_MIN, s);
+  fill_i32(g.err_flag, 1, 0, s);
+
+  cudaEvent_t gs, ge;
+  ck(cudaEventCreate(&gs), "event");
+  ck(cudaEventCreate(&ge), "event");
+  ck(cudaEventRecord(gs, s), "event");
+  ctx.timing.kernel_launches += 6;  // fills
+
+  // chunking: neighbour lists, statuses and the all-mode Gram buffer
+  const long long budget = 2LL << 30;
+  long long per_point = (long long)kcap * 12 + 8;
+  if (any_all && o.algorithm == 1)
+    per_point += (long long)nth * (n * n + n) * 8;
+  long long chunk = std::max<long long>(1, std::min<long long>(std::max<long long>(P, 1), budget / per_point));
+  ChunkBuffers c{};
+  c.kcap = kcap;
+  c.nn_idx = (int*)ctx.buf("nn_idx", (size_t)chunk * kcap * 4);
+  c.nn_dist = (double*)ctx.buf("nn_dist", (size_t)chunk * kcap * 8);
+  c.nn_count = (int*)ctx.buf("nn_count", (size_t)chunk * 4);
+  c.status = (int*)ctx.buf("status", (size_t)chunk * 4);
+  if (any_all && o.algorithm == 1)
+    c.gram = (double*)ctx.buf("gram", (size_t)chunk * nth * (n * n + n) * 8);
+  long long scratch = 1;
+  if (any_all)
+    scratch = std::max(scratch, all_mode_scratch_doubles(ctx.num_sms, max_nlib_all));
+  if ((any_finite || any_mixed) && o.algorithm == 1)
+    scratch = std::max(scratch, smap_nn_scratch_doubles(ctx.num_sms, n, kcap));
+  if (any_all && o.algorithm == 1 && n > 8)
+    scratch = std::max(scratch, (long long)ctx.num_sms * 4 * 128 * (3LL * n * n + 3LL * n));
+  c.scratch = (double*)ctx.buf("scratch", (size_t)scratch * 8);
+  c.scratch_doubles = scratch;
+
+  // detail mode: per-point neighbour lists gathered from every path
+  std::vector<std::vector<int>> pt_idx;
+  std::vector<std::vector<double>> pt_dist;
+  if (job.detail) {
+    pt_idx.resize(P);
+    pt_dist.resize(P);
+  }
+  std::vector<int> h_cnt, h_idx, h_status;
+  std::vector<double> h_dist;
+  std::vector<long long> h_plist;
+  auto gather_detail = [&](long long cl) {
+    h_cnt.resize(cl);
+    h_status.resize(cl);
+    h_idx.resize((size_t)cl * kcap);
+    h_dist.resize((size_t)cl * kcap);
+    ctx.download(h_cnt.data(), c.nn_count, cl * 4);
+    ctx.download(h_status.data(), c.status, cl * 4);
+    ctx.download(h_idx.data(), c.nn_idx, (size_t)cl * kcap * 4);
+    ctx.download(h_dist.data(), c.nn_dist, (size_t)cl * kcap * 8);
+    ck(cudaStreamSynchronize(s), "sync");
+    for (long long q = 0; q < cl; q++) {
+      const long long p = c.plist ? h_plist[q] : c.p_begin + q;
+      if (h_status[q] != PT_OK)
+        continue;
+      pt_idx[p].assign(h_idx.begin() + q * kcap, h_idx.begin() + q * kcap + h_cnt[q]);
+      pt_dist[p].assign(h_dist.begin() + q * kcap, h_dist.begin() + q * kcap + h_cnt[q]);
+    }
+  };
+
+  cudaEvent_t e0, e1;
+  ck(cudaEventCreate(&e0), "event");
+  ck(cudaEventCreate(&e1), "event");
+  float knn_ms = 0;
+  auto timed = [&](auto&& launch) {
+    ck(cudaEventRecord(e0, s), "event");
+    launch();
+    ck(cudaEventRecord(e1, s), "event");
+    ctx.check("neighbour kernel");
+    ck(cudaEventSynchronize(e1), "sync");
+    float ms = 0;
+    cudaEventElapsedTime(&ms, e0, e1);
+    knn_ms += ms;
+    ctx.timing.knn_launches++;
+  };
+  auto exact_pass = [&](bool with_list_path, bool with_all) {
+    ctx.timing.kernel_launches += 1;  // status fill
+    if (with_list_path) {
+      timed([&] { launch_knn_exact(g, c, ctx.num_sms, s); });
+      if (o.algorithm == 0)
+        launch_simplex_nn(g, c, s);
+      else
+        launch_smap_nn(g, c, ctx.num_sms, s);
+      ctx.check("forecast");
+      ctx.timing.kernel_launches += 1;
+    }
+    if (with_all) {
+      launch_all_mode(g, c, ctx.num_sms, max_nlib_all, s);
+      ctx.check("all_mode");
+      ctx.timing.kernel_launches += o.algorithm == 1 ? 2 : 1;
+    }
+  };
+
+  // 1. mixed-precision kernel for the tasks it serves
+  if (any_mixed) {
+    const int S = Ea <= 4 ? 4 : 8;
+    const long long nrows = (long long)rows.n_rows;
+    double* d_center = (double*)ctx.buf("center", Ea * 8);
+    ctx.upload(d_center, center.data(), Ea * 8);
+    float* F32 = (float*)ctx.buf("F32", (size_t)nrows * S * 4);
+    center_to_f32(job.dF, nrows, Ea, d_center, F32, S, s);
+    float* Fp32 = F32;
+    if (job.dFp != job.dF) {
+      Fp32 = (float*)ctx.buf("Fp32", (size_t)nrows * S * 4);
+      center_to_f32(job.dFp, nrows, Ea, d_center, Fp32, S, s);
+    }
+    std::vector<int> order;
+    for (int j = 0; j < nT; j++)
+      if (dt[j].mixed)
+        order.push_back(j);
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return dt[a].n_lib > dt[b].n_lib; });
+    std::vector<int2> items;
+    for (int j : order)
+      for (int b = 0; b < dt[j].n_pred; b += MIX_POINTS)
+        items.push_back(make_int2(j, b));
+    MixedRun m{};
+    m.F32 = F32;
+    m.Fp32 = Fp32;
+    m.items = (const int2*)ctx.buf("items", std::max<size_t>(items.size(), 1) * sizeof(int2));
+    ctx.upload((void*)m.items, items.data(), items.size() * sizeof(int2));
+    m.n_items = (int)items.size();
+    m.counter = (int*)ctx.buf("mix_counter", 8);
+    m.fb_count = m.counter + 1;
+    fill_i32(m.counter, 2, 0, s);
+    m.fb_cap = (int)std::min<long long>(std::max<long long>(P, 1), FB_CAP);
+    m.fb_list = (long long*)ctx.buf("fb_list", (size_t)m.fb_cap * 8);
+    m.gamma = (Ea + 2) * std::ldexp(1.0, -23);
+    m.err_abs = std::ldexp(R, -21) + 1e-21;
+    const int C = kmix <= 6 ? 8 : 16;
+    if (job.detail) {
+      m.kslots = C;
+      m.nn_idx = (int*)ctx.buf("mix_nn_idx", (size_t)std::max<long long>(P, 1) * C * 4);
+      m.nn_dist = (double*)ctx.buf("mix_nn_dist", (size_t)std::max<long long>(P, 1) * C * 8);
+    }
+    timed([&] { launch_knn_mixed(g, m, C, ctx.num_sms, s); });
+    ctx.timing.kernel_launches += (job.dFp != job.dF ? 2 : 1) + 1;  // centring, counter fill
+    int nfb = 0;
+    ctx.download(&nfb, m.fb_count, 4);
+    ck(cudaStreamSynchronize(s), "sync");
+    ctx.timing.fallback_points += nfb;
+    if (job.detail) {
+      std::vector<int> ku(P), mi((size_t)P * C);
+      std::vector<double> md((size_t)P * C);
+      ctx.download(ku.data(), g.kused, P * 4);
+      ctx.download(mi.data(), m.nn_idx, (size_t)P * C * 4);
+      ctx.download(md.data(), m.nn_dist, (size_t)P * C * 8);
+      ck(cudaStreamSynchronize(s), "sync");
+      for (int j = 0; j < nT; j++)
+        if (dt[j].mixed)
+          for (long long p = dt[j].point_base; p < dt[j].point_base + dt[j].n_pred; p++)
+            if (ku[p] != MISSING_I) {
+              pt_idx[p].assign(mi.begin() + p * C, mi.begin() + p * C + ku[p]);
+              pt_dist[p].assign(md.begin() + p * C, md.begin() + p * C + ku[p]);
+            }
+    }
+    if (nfb > m.fb_cap) {
+      // too many uncertified points: run every mixed task exactly
+      for (auto& d : dt)
+        d.mixed = 0;
+      ctx.upload(d_tasks, dt.data(), dt.size() * sizeof(DevTask));
+      fill_f64(g.pred, P * nth, MISSING_D, s);
+      if (g.coeffs)
+        fill_f64(g.coeffs, P * n, MISSING_D, s);
+      if (g.kused)
+        fill_i32(g.kused, P, MISSING_I, s);
+      fill_i32(g.task_rc, nT, 0, s);
+      fill_i32(g.task_kmin, nT, INT_MAX, s);
+      fill_i32(g.task_kmax, nT, INT_MIN, s);
+      for (auto& v : pt_idx)
+        v.clear();
+      for (auto& v : pt_dist)
+        v.clear();
+      any_finite = true;
+    } else if (nfb > 0) {
+      h_plist.resize(nfb);
+      ctx.download(h_plist.data(), m.fb_list, (size_t)nfb * 8);
+      ck(cudaStreamSynchronize(s), "sync");
+      for (long long b = 0; b < nfb; b += chunk) {
+        c.p_begin = 0;
+        c.p_end = std::min<long long>(nfb - b, chunk);
+        c.plist = m.fb_list + b;
+        fill_i32(c.status, c.p_end, PT_SKIP, s);
+        exact_pass(true, false);
+        if (job.detail) {
+          std::vector<long long> keep(h_plist.begin() + b, h_plist.begin() + b + c.p_end);
+          std::swap(keep, h_plist);
+          gather_detail(c.p_end);
+          std::swap(keep, h_plist);
+        }
+      }
+      c.plist = nullptr;
+    }
+  }
+
+  // 2. exact kernels over the point space for the other tasks
+  if (any_finite || any_all) {
+    for (long long b = 0; b < P; b += chunk) {
+      if (ctx.keep_going && !ctx.keep_going())
+        throw Error{ RC_BREAK_HIT, "cancelled" };
+      c.p_begin = b;
+      c.p_end = std::min(P, b + chunk);
+      c.plist = nullptr;
+      const long long cl = c.p_end - c.p_begin;
+      fill_i32(c.status, cl, PT_SKIP, s);
+      exact_pass(any_finite, any_all);
+      if (job.detail && any_finite)
+        gather_detail(cl);
+    }
+  }
+  ctx.timing.knn_kernel_ms += knn_ms;
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+
+  // statistics
+  double* d_rho = (double*)ctx.buf("rho", (size_t)nT * nth * 8);
+  double* d_mae = (double*)ctx.buf("mae", (size_t)nT * nth * 8);
+  launch_stats(g, nullptr, nT, d_rho, d_mae, s);
+  ctx.check("stats");
+  ctx.timing.kernel_launches += 1;
+  ck(cudaEventRecord(ge, s), "event");
+  ck(cudaEventSynchronize(ge), "sync");
+  {
+    float ms = 0;
+    cudaEventElapsedTime(&ms, gs, ge);
+    ctx.timing.device_ms += ms;
+  }
+  cudaEventDestroy(gs);
+  cudaEventDestroy(ge);
+  std::vector<int> rc(nT), kmin(nT), kmax(nT);
+  std::vector<double> rho((size_t)nT * nth), mae((size_t)nT * nth);
+  int err = 0;
+  ctx.download(rc.data(), g.task_rc, nT * 4);
+  ctx.download(kmin.data(), g.task_kmin, nT * 4);
+  ctx.download(kmax.data(), g.task_kmax, nT * 4);
+  ctx.download(rho.data(), d_rho, rho.size() * 8);
+  ctx.download(mae.data(), d_mae, mae.size() * 8);
+  ctx.download(&err, g.err_flag, 4);
+  ck(cudaStreamSynchronize(s), "sync");
+  if (err)
+    throw Error{ RC_UNKNOWN_ERROR, "panel weight missing for a compared pair of panels" };
+  for (int j = 0; j < nT; j++) {
+    TaskOut& to = outs[job.task_ids[j]];
+    const Task& t = tasks[job.task_ids[j]];
+    to.rc = rc[j];
+    to.kmin = kmin[j] == INT_MAX ? MISSING_I : kmin[j];
+    to.kmax = kmax[j] == INT_MIN ? MISSING_I : kmax[j];
+    to.rho.assign(rho.begin() + (size_t)j * nth, rho.begin() + (size_t)(j + 1) * nth);
+    to.mae.assign(mae.begin() + (size_t)j * nth, mae.begin() + (size_t)(j + 1) * nth);
+    const long long base = dt[j].point_base;
+    const int np = dt[j].n_pred;
+    if (t.save_prediction || job.detail) {
+      to.pred_last.resize(np);
+      ctx.download(to.pred_last.data(), g.pred + (size_t)(nth - 1) * P + base, (size_t)np * 8);
+    }
+    if (job.detail) {
+      to.pred_all.resize((size_t)nth * np);
+      for (int th = 0; th < nth; th++)
+        ctx.download(to.pred_all.data() + (size_t)th * np, g.pred + (size_t)th * P + base, (size_t)np * 8);
+      to.kused.resize(np);
+      ctx.download(to.kused.data(), g.kused + base, (size_t)np * 4);
+      to.nn_offsets.assign(np + 1, 0);
+      for (int i = 0; i < np; i++) {
+        const auto& li = pt_idx[base + i];
+        const auto& ld = pt_dist[base + i];
+        to.nn_idx.insert(to.nn_idx.end(), li.begin(), li.end());
+        to.nn_dist.insert(to.nn_dist.end(), ld.begin(), ld.end());
+        to.nn_offsets[i + 1] = (int)to.nn_idx.size();
+      }
+    }
+    if ((t.save_coeffs || job.detail) && o.algorithm == 1 && g.coeffs) {
+      to.coeffs.resize((size_t)np * n);
+      ctx.download(to.coeffs.data(), g.coeffs + (size_t)base * n, (size_t)np * n * 8);
+    } else if (t.save_coeffs || job.detail) {
+      to.coeffs.assign((size_t)np * n, MISSING_D);
+    }
+  }
+  ck(cudaStreamSynchronize(s), "sync");
+}
+
+double na(double v)
+{
+  return v != MISSING_D ? v : NAN;
+}
+
+// src/r.cpp:73-105 (column-major read of the buffer, NA where filtered)
+std::vector<double> to_R_matrix(const std::vector<double>& v, int r, int c, const std::vector<uint8_t>& filter)
+{
+  std::vector<double> m((size_t)r * c, NAN);
+  size_t k = 0;
+  for (int j = 0; j < c; j++)
+    for (int i = 0; i < r; i++) {
+      if (!filter.empty() && !filter[i])
+        continue;
+      m[(size_t)j * r + i] = k < v.size() ? na(v[k]) : NAN;
+      k++;
+    }
+  return m;
+}
+
+std::vector<int> rows_of(const std::vector<uint8_t>& mask)
+{
+  std::vector<int> r;
+  for (int i = 0; i < (int)mask.size(); i++)
+    if (mask[i])
+      r.push_back(i);
+  return r;
+}
+
+// Library manifold rows: the mask's rows whose target is observed
+// (src/manifold.h:186-189).
+std::vector<int> lib_rows_of(const std::vector<uint8_t>& mask, const RowTables& rt)
+{
+  std::vector<int> r;
+  for (int i = 0; i < (int)mask.size(); i++)
+    if (mask[i] && rt.lib_target[i] != MISSING_D)
+      r.push_back(i);
+  return r;
+}
+
+struct Manifolds
+{
+  std::map<std::pair<int, bool>, std::vector<double>> host;
+  std::map<std::pair<int, bool>, double*> dev;
+};
+
+double* device_manifold(Context& ctx, Manifolds& M, const Generator& g, const RowTables& rt, int E, bool co,
+                        int threads)
+{
+  auto key = std::make_pair(E, co);
+  auto it = M.dev.find(key);
+  if (it != M.dev.end())
+    return it->second;
+  auto& h = M.host[key];
+  h = build_manifold(g, rt, E, co, threads);
+  double* d = (double*)ctx.buf("F_" + std::to_string(E) + (co ? "_co" : ""), std::max<size_t>(h.size(), 1) * 8);
+  ctx.upload(d, h.data(), h.size() * 8);
+  M.dev[key] = d;
+  return d;
+}
+
+} // namespace
+
+// ------------------------------------------------------------ run_command
+CommandResult run_command(Context& ctx, const fedm_args& a)
+{
+  CommandResult R;
+  const double t0 = now_ms();
+  ctx.timing = fedm_timing{};
+  ck(cudaSetDevice(ctx.device), "cudaSetDevice");
+  Prepared P;
+  prepare(a, P);
+  const Generator& gen = P.gen;
+  const Options& o = P.opts;
+  const int threads = host_threads(a);
+  const int maxE = P.Es.back();
+  std::vector<uint8_t> usable = gen.usable(maxE, false, threads);
+  const int numUsable = (int)std::count(usable.begin(), usable.end(), (uint8_t)1);
+  if (numUsable == 0) {
+    R.rc = RC_UNKNOWN_ERROR;  // src/r.cpp:259-266
+    return R;
+  }
+  std::vector<int> libraries = P.libraries;
+  if (!P.explore && libraries.empty())
+    libraries = { numUsable };
+  const bool copredict_mode = !gen.co_x.empty();
+  std::vector<uint8_t> cousable;
+  if (copredict_mode)
+    cousable = gen.usable(maxE, true, threads);
+  TaskPlan plan = configure_tasks(gen, o, P.Es, libraries, a.k, a.num_reps, a.crossfold, P.explore, a.full,
+                                  a.shuffle, a.save_predictions, a.save_copredictions, a.save_smap_coeffs,
+                                  copredict_mode, usable, cousable, a.seed);
+  RowTables rt = build_row_tables(gen);
+  DevRows drows = upload_rows(ctx, gen, rt, o);
+
+  // row lists per mask (shared by every task that uses the mask)
+  std::vector<std::vector<int>> lib_lists(plan.masks.size()), pred_lists(plan.masks.size());
+  std::vector<uint8_t> lib_done(plan.masks.size(), 0), pred_done(plan.masks.size(), 0);
+  for (const Task& t : plan.tasks) {
+    if (!lib_done[t.lib_mask]) {
+      lib_lists[t.lib_mask] = lib_rows_of(plan.masks[t.lib_mask], rt);
+      lib_done[t.lib_mask] = 1;
+    }
+    if (!pred_done[t.pred_mask]) {
+      pred_lists[t.pred_mask] = rows_of(plan.masks[t.pred_mask]);
+      pred_done[t.pred_mask] = 1;
+    }
+  }
+
+  std::vector<TaskOut> outs(plan.tasks.size());
+  Manifolds M;
+  // groups: (E, copredict) in first-appearance order
+  std::vector<std::pair<int, bool>> order;
+  for (const Task& t : plan.tasks) {
+    auto key = std::make_pair(t.E, t.copredict);
+    if (std::find(order.begin(), order.end(), key) == order.end())
+      order.push_back(key);
+  }
+  for (auto key : order) {
+    GroupJob job;
+    job.Ea = gen.E_actual(key.first);
+    job.copredict = key.second;
+    job.dF = device_manifold(ctx, M, gen, rt, key.first, false, threads);
+    job.dFp = key.second ? device_manifold(ctx, M, gen, rt, key.first, true, threads) : job.dF;
+    job.hF = &M.host[std::make_pair(key.first, false)];
+    job.hFp = key.second ? &M.host[std::make_pair(key.first, true)] : job.hF;
+    for (int i = 0; i < (int)plan.tasks.size(); i++) {
+      const Task& t = plan.tasks[i];
+      if (t.E == key.first && t.copredict == key.second) {
+        job.task_ids.push_back(i);
+        job.lib_lists.push_back(&lib_lists[t.lib_mask]);
+        job.pred_lists.push_back(&pred_lists[t.pred_mask]);
+      }
+    }
+    run_group(ctx, o, plan.tasks, drows, job, outs);
+  }
+
+  // src/r.cpp:348-457 marshalling, in task order
+  int rc = 0, kMin = 0, kMax = 0;
+  long long npred = 0, pairs = 0;
+  for (size_t f = 0; f < plan.tasks.size(); f++) {
+    const Task& t = plan.tasks[f];
+    const TaskOut& to = outs[f];
+    if (f == 0 || to.kmin < kMin)
+      kMin = to.kmin;
+    if (f == 0 || to.kmax > kMax)
+      kMax = to.kmax;
+    const int Ea = gen.E_actual(t.E);
+    for (size_t th = 0; th < o.thetas.size(); th++) {
+      if (!t.copredict) {
+        R.sE.push_back(Ea);
+        R.sL.push_back(t.library);
+        R.sT.push_back(na(o.thetas[th]));
+        R.sR.push_back(na(to.rho[th]));
+        R.sM.push_back(na(to.mae[th]));
+      } else {
+        R.cE.push_back(Ea);
+        R.cL.push_back(t.library);
+        R.cT.push_back(na(o.thetas[th]));
+        R.cR.push_back(na(to.rho[th]));
+        R.cM.push_back(na(to.mae[th]));
+      }
+    }
+    if (to.rc > rc)
+      rc = to.rc;
+    const std::vector<uint8_t>& pm = plan.masks[t.pred_mask];
+    const int nrow = (int)pm.size();
+    if (t.save_prediction) {
+      // only the first of the numThetas columns the reference reads is
+      // defined (src/r.cpp:394-399 reads past a one-theta buffer)
+      auto m = to_R_matrix(to.pred_last, nrow, 1, pm);
+      if (!t.copredict) {
+        R.preds = m;
+        R.pred_rows = nrow;
+        R.pred_cols = 1;
+      } else {
+        R.copreds = m;
+        R.copred_rows = nrow;
+        R.copred_cols = 1;
+      }
+    }
+    if (t.save_coeffs && !t.copredict) {
+      R.coeffs = to_R_matrix(to.coeffs, nrow, Ea + 1, pm);
+      R.coeff_rows = nrow;
+      R.coeff_cols = Ea + 1;
+    }
+    npred += (long long)pred_lists[t.pred_mask].size() * (long long)o.thetas.size();
+    pairs += (long long)pred_lists[t.pred_mask].size() * (long long)lib_lists[t.lib_mask].size();
+  }
+  R.rc = rc;
+  R.kmin = kMin;
+  R.kmax = kMax;
+  if (a.allow_missing) {
+    R.has_missing_distance = true;
+    R.missing_distance = o.missing_distance;
+  }
+  if (a.dt || a.reldt) {
+    R.has_dt_weight = true;
+    R.dt_weight = gen.dt_weight;
+  }
+  ctx.timing.host_ms = now_ms() - t0;
+  ctx.timing.predictions = npred;
+  ctx.timing.distance_pairs = pairs;
+  return R;
+}
+
+// ------------------------------------------------------ single-task seam
+int run_task(Context& ctx, const fedm_args& a, fedm_task_io& io)
+{
+  const double t0 = now_ms();
+  ctx.timing = fedm_timing{};
+  ck(cudaSetDevice(ctx.device), "cudaSetDevice");
+  Prepared P;
+  prepare(a, P);
+  Options o = P.opts;
+  o.distance = io.distance == 0 ? 0 : 1;
+  o.force_compute = io.force_compute != 0;
+  const Generator& gen = P.gen;
+  const int threads = host_threads(a);
+  RowTables rt = build_row_tables(gen);
+  std::vector<uint8_t> lm(io.library_rows, io.library_rows + a.n), pm(io.prediction_rows, io.prediction_rows + a.n);
+  for (auto& v : lm)
+    v = v ? 1 : 0;
+  for (auto& v : pm)
+    v = v ? 1 : 0;
+  std::vector<int> L = lib_rows_of(lm, rt), Pl = rows_of(pm);
+  const int Ea = gen.E_actual(io.E);
+  const int nth = (int)o.thetas.size();
+  const bool sizes_only = io.predictions == nullptr;
+  Task t;
+  t.E = io.E;
+  t.k = io.k;
+  t.copredict = io.copredict != 0;
+  t.save_coeffs = true;
+  std::vector<Task> tasks{ t };
+  std::vector<TaskOut> outs(1);
+  if (!sizes_only || true) {
+    DevRows drows = upload_rows(ctx, gen, rt, o);
+    Manifolds M;
+    GroupJob job;
+    job.Ea = Ea;
+    job.copredict = t.copredict;
+    job.dF = device_manifold(ctx, M, gen, rt, io.E, false, threads);
+    job.dFp = t.copredict ? device_manifold(ctx, M, gen, rt, io.E, true, threads) : job.dF;
+    job.hF = &M.host[std::make_pair(io.E, false)];
+    job.hFp = t.copredict ? &M.host[std::make_pair(io.E, true)] : job.hF;
+    job.task_ids = { 0 };
+    job.lib_lists = { &L };
+    job.pred_lists = { &Pl };
+    job.detail = true;
+    job.knn_for_all = true;
+    run_group(ctx, o, tasks, drows, job, outs);
+  }
+  const TaskOut& to = outs[0];
+  io.n_pred = (int)Pl.size();
+  io.n_lib = (int)L.size();
+  io.e_actual = Ea;
+  io.total_nn = to.nn_offsets.empty() ? 0 : to.nn_offsets.back();
+  ctx.timing.host_ms = now_ms() - t0;
+  if (sizes_only)
+    return RC_SUCCESS;
+  const int np = io.n_pred;
+  std::copy(to.pred_all.begin(), to.pred_all.end(), io.predictions);
+  if (io.coeffs)
+    std::copy(to.coeffs.begin(), to.coeffs.end(), io.coeffs);
+  // per-point return codes (src/edm.cpp:598-610 and 730-813)
+  for (int i = 0; i < np; i++) {
+    const bool made = to.kused[i] != MISSING_I;
+    for (int th = 0; th < nth; th++) {
+      int code = 0;
+      if (!made)
+        code = th == 0 ? (o.force_compute ? 0 : 503) : 8000;
+      if (io.rc)
+        io.rc[(size_t)th * np + i] = code;
+    }
+    if (io.kused)
+      io.kused[i] = to.kused[i];
+  }
+  if (io.nn_offsets)
+    std::copy(to.nn_offsets.begin(), to.nn_offsets.end(), io.nn_offsets);
+  if (io.nn_idx)
+    std::copy(to.nn_idx.begin(), to.nn_idx.end(), io.nn_idx);
+  if (io.nn_dist)
+    std::copy(to.nn_dist.begin(), to.nn_dist.end(), io.nn_dist);
+  if (io.stats_rho)
+    for (int th = 0; th < nth; th++)
+      io.stats_rho[th] = to.rho[th];
+  if (io.stats_mae)
+    for (int th = 0; th < nth; th++)
+      io.stats_mae[th] = to.mae[th];
+  return to.rc;
+}
+
+} // namespace fedm

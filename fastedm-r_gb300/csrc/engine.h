@@ -1,0 +1,59 @@
+// C++ engine behind the C ABI: one context per GPU, the run_command
+// pipeline and the single-task seam.
+#pragma once
+
+#include <map>
+#include <string>
+#include <vector>
+
+#include "host.h"
+#include "kernels.h"
+
+namespace fedm {
+
+struct DevBuf
+{
+  void* p = nullptr;
+  size_t cap = 0;
+};
+
+class Context
+{
+public:
+  int device = 0;
+  int num_sms = 1;
+  cudaStream_t stream = nullptr;
+  int precision = FEDM_PRECISION_MIXED;
+  int (*keep_going)(void) = nullptr;
+  std::string last_error;
+  fedm_timing timing{};
+
+  explicit Context(int dev);
+  ~Context();
+  // Grow-only named device buffers (the context's memory pool).
+  void* buf(const std::string& name, size_t bytes);
+  void upload(void* dst, const void* src, size_t bytes);
+  void download(void* dst, const void* src, size_t bytes);
+  void check(const char* what);
+
+private:
+  std::map<std::string, DevBuf> bufs_;
+};
+
+// Everything run_command returns, in host memory.
+struct CommandResult
+{
+  int rc = 0;
+  std::vector<int> sE, sL, cE, cL;
+  std::vector<double> sT, sR, sM, cT, cR, cM;
+  int kmin = MISSING_I, kmax = MISSING_I;
+  std::vector<double> preds, copreds, coeffs;  // R matrices (column-major)
+  int pred_rows = 0, pred_cols = 0, copred_rows = 0, copred_cols = 0, coeff_rows = 0, coeff_cols = 0;
+  double missing_distance = 0, dt_weight = 0;
+  bool has_missing_distance = false, has_dt_weight = false;
+};
+
+CommandResult run_command(Context& ctx, const fedm_args& a);
+int run_task(Context& ctx, const fedm_args& a, fedm_task_io& io);
+
+} // namespace fedm

@@ -1,0 +1,135 @@
+// Device-side data layout and kernel launchers.
+//
+// HBM layout of one run (all FP64 unless noted):
+//   F_E      [n_rows x Ea]   lagged manifold of every row for one E
+//   coF_E    [n_rows x Ea]   the coprediction manifold (co_x lags)
+//   F32_E    [n_rows x Ea]   float copy for the mixed-precision scan
+//   row tables [n_rows]      library target, coprediction target, target
+//                            time, point time, panel id
+//   lib_rows / pred_rows     int32 row lists, one slice per task
+//   pred     [n_thetas x P]  forecasts, theta-major over the point space
+//   coeffs   [P x (Ea+1)]    S-map coefficients of the last theta
+// A "point" is one (task, prediction row); P counts them over all tasks.
+#pragma once
+
+#include <cstdint>
+
+#include <cuda_runtime.h>
+
+namespace fedm {
+
+struct DevTask
+{
+  long long point_base;  // first global point id of this task
+  int lib_off, n_lib;    // slice of lib_rows
+  int pred_off, n_pred;  // slice of pred_rows
+  int k;                 // neighbours requested (>0) or -1 (all valid)
+  int task;              // index of the task's rc / k / stats slots
+  int save_coeffs;
+  int all_mode;          // k < 0 or k >= n_lib: every valid neighbour, library order
+  int mixed;             // handled by the mixed-precision kernel
+};
+
+struct GroupParams
+{
+  // inputs
+  const double* F;
+  const double* Fp;
+  const float* F32;
+  const double* lib_target;
+  const double* pred_target;
+  const double* lib_target_time;
+  const double* point_time;
+  const int* panel;
+  const int* panel_dense;  // dense panel index per row (id weights matrix)
+  const float* id_w;       // [n_pid x n_pid] id weights, NaN = no entry
+  int n_pid;
+  const int* lib_rows;
+  const int* pred_rows;
+  const DevTask* tasks;
+  int n_tasks;
+  int Ea;
+  int n_thetas;
+  const double* thetas;
+  int algorithm;  // 0 simplex, 1 smap
+  int l1;
+  int has_missing;
+  double missing_distance;
+  int panel_mode;
+  double idw;
+  int skip_other_panels;
+  int has_id_weights;
+  int past_only;
+  int force_compute;
+  long long total_points;  // size of the point space of the whole run
+  // outputs
+  double* pred;            // [n_thetas x total_points]
+  double* coeffs;          // [total_points x (Ea+1)] or null
+  int* kused;              // [total_points] or null
+  int* task_rc;            // per task: max return code
+  int* task_kmin;
+  int* task_kmax;
+  int* err_flag;           // set on a device-detected fault (missing id weight)
+};
+
+// Point statuses written by the neighbour kernels.
+enum : int
+{
+  PT_OK = 0,
+  PT_EARLY_SUCCESS = 1,  // k == 0 or no valid neighbour: rc SUCCESS, no forecast
+  PT_INSUFFICIENT = 2,   // the same without forceCompute: rc 503
+  PT_SKIP = 3            // point belongs to the other (all / finite k) path
+};
+
+struct ChunkBuffers
+{
+  long long p_begin, p_end;  // point range of this chunk
+  int kcap;                  // neighbour slots per point
+  int* nn_idx;               // [chunk x kcap]
+  double* nn_dist;           // [chunk x kcap]
+  int* nn_count;             // [chunk] k used
+  int* status;               // [chunk]
+  double* scratch;           // per-warp / per-thread scratch
+  long long scratch_doubles; // its size
+  double* gram;              // [chunk x n_thetas x (n*n + n)] for the all-mode S-map
+  const long long* plist;    // optional: chunk point q is plist[q] (p_begin = 0, p_end = count)
+};
+
+// Exact FP64 kernels (reference operation order, no FMA contraction).
+void launch_knn_exact(const GroupParams& g, const ChunkBuffers& c, int num_sms, cudaStream_t s);
+void launch_simplex_nn(const GroupParams& g, const ChunkBuffers& c, cudaStream_t s);
+void launch_smap_nn(const GroupParams& g, const ChunkBuffers& c, int num_sms, cudaStream_t s);
+void launch_all_mode(const GroupParams& g, const ChunkBuffers& c, int num_sms, long long max_nlib, cudaStream_t s);
+void launch_stats(const GroupParams& g, const DevTask* tasks_host_unused, int n_tasks, double* rho, double* mae,
+                  cudaStream_t s);
+long long all_mode_scratch_doubles(int num_sms, long long max_nlib);
+long long smap_nn_scratch_doubles(int num_sms, int n, int kcap);
+
+// Mixed-precision neighbour scan for the common case (L2, no missing values,
+// no panels, no past-only rule, finite k): FP32 candidate distances on a
+// centred float copy of the manifold with a proven error margin, an FP64
+// re-rank of every candidate inside the margin (reference operation order,
+// so neighbour distances are the FP64 bits), then the forecast.  Points it
+// cannot certify are appended to `fb_list` for the exact kernels.
+struct MixedRun
+{
+  const float* F32;    // centred float library manifold, row stride 4 or 8
+  const float* Fp32;   // centred float prediction manifold (same centre)
+  const int2* items;   // (task, first prediction index) blocks of 512 points
+  int n_items;
+  int* counter;        // work-queue head
+  double err_abs;      // bound on | ||fl32 diff|| - ||exact diff|| | from input rounding
+  double gamma;        // relative bound of the FP32 accumulation
+  long long* fb_list;  // points to recompute exactly
+  int* fb_count;
+  int fb_cap;
+  int* nn_idx;         // optional [total_points x kslots] final neighbour lists
+  double* nn_dist;
+  int kslots;
+};
+
+void launch_knn_mixed(const GroupParams& g, const MixedRun& m, int C, int num_sms, cudaStream_t s);
+void center_to_f32(const double* F, long long n, int Ea, const double* center, float* F32, int stride,
+                   cudaStream_t s);
+
+} // namespace fedm

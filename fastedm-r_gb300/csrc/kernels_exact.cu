@@ -1,0 +1,727 @@
+// Exact FP64 kernels: distances, k-nearest-neighbour selection, simplex and
+// S-map forecasts, rho/MAE.  Arithmetic follows the reference's operation
+// order (EDM-Developers/fastEDM-r src/distances.cpp:151-229,
+// src/edm.cpp:652-814, src/stats.cpp:64-94).  This translation unit is built
+// with --fmad=false so every a*b+c stays a rounded multiply and a rounded
+// add, as in the reference's FP64 loops; sqrt and division are IEEE
+// round-to-nearest, so distances are bit-identical to the CPU.
+#include <cfloat>
+#include <climits>
+#include <cstdio>
+
+#include "kernels.h"
+#include "exp_rn.cuh"
+#include "smap_solve.cuh"
+
+namespace fedm {
+
+namespace {
+
+constexpr double MISS = 1.0e+100;
+constexpr unsigned FULL = 0xffffffffu;
+
+__device__ __forceinline__ int find_task(const GroupParams& g, long long p)
+{
+  int lo = 0, hi = g.n_tasks - 1;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (g.tasks[mid].point_base <= p)
+      lo = mid;
+    else
+      hi = mid - 1;
+  }
+  return lo;
+}
+
+// One reference distance (src/distances.cpp:160-226).  Returns false for
+// skipped or invalid pairs (zero or missing distance).
+__device__ __forceinline__ bool exact_distance(const GroupParams& g, int lrow, int prow, const double* y, int ppanel,
+                                               double ptime, double& out)
+{
+  if (g.skip_other_panels && g.panel[lrow] != ppanel)
+    return false;
+  if (g.past_only && g.lib_target_time[lrow] > ptime)
+    return false;
+  double d = 0.0;
+  if (g.panel_mode && g.idw > 0) {
+    d += g.idw * (double)(g.panel[lrow] != ppanel);
+  } else if (g.panel_mode && g.has_id_weights) {
+    float w = g.id_w[(size_t)g.panel_dense[lrow] * g.n_pid + g.panel_dense[prow]];
+    if (isnan(w)) {
+      atomicExch(g.err_flag, 1);  // the reference's map::at throws here
+      w = 0.f;
+    }
+    d += (double)w;
+  }
+  const double* x = g.F + (size_t)lrow * g.Ea;
+  const int Ea = g.Ea;
+  for (int j = 0; j < Ea; j++) {
+    double a = x[j], b = y[j], dij;
+    if (g.has_missing && (a == MISS || b == MISS)) {
+      if (g.missing_distance == 0) {
+        d = MISS;
+        break;
+      }
+      dij = g.missing_distance;
+    } else {
+      dij = a - b;
+    }
+    if (g.l1)
+      d += fabs(dij) / Ea;
+    else
+      d += dij * dij;
+  }
+  if (d != 0 && d != MISS) {
+    out = g.l1 ? d : sqrt(d);
+    return true;
+  }
+  return false;
+}
+
+__device__ __forceinline__ long long point_of(const ChunkBuffers& c, long long q)
+{
+  return c.plist ? c.plist[q] : c.p_begin + q;
+}
+
+__device__ __forceinline__ void note_rc(const GroupParams& g, int task, int code)
+{
+  if (code)
+    atomicMax(&g.task_rc[task], code);
+}
+
+// Return codes of a point that made no forecast (src/edm.cpp:598-610): the
+// reference writes rc(0, i) only, so with several thetas the untouched
+// entries keep UNKNOWN_ERROR and dominate the task's max.
+__device__ __forceinline__ void early_rc(const GroupParams& g, int task, int status, int t)
+{
+  if (t == 0)
+    note_rc(g, task, status == PT_EARLY_SUCCESS ? 0 : 503);
+  else
+    note_rc(g, task, 8000);
+}
+
+__device__ __forceinline__ void note_k(const GroupParams& g, int task, long long p, int k)
+{
+  atomicMin(&g.task_kmin[task], k);
+  atomicMax(&g.task_kmax[task], k);
+  if (g.kused)
+    g.kused[p] = k;
+}
+
+// ------------------------------------------------------ neighbour selection
+// One warp per prediction point.  The k best (distance, library index)
+// pairs are kept sorted in shared memory; a library chunk of 32 is scored in
+// parallel and its candidates are inserted in index order, which realises
+// the reference's (distance asc, index asc) order (src/edm.cpp:652-681).
+__global__ void knn_exact_kernel(GroupParams g, ChunkBuffers c, int warps_per_block, int per_warp_bytes)
+{
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  unsigned char* base = smem + (size_t)wib * per_warp_bytes;
+  double* sy = (double*)base;
+  double* sD = sy + g.Ea;
+  int* sI = (int*)(sD + c.kcap);
+  const long long nwarps = (long long)gridDim.x * warps_per_block;
+  const long long chunk = c.p_end - c.p_begin;
+  for (long long q = (long long)blockIdx.x * warps_per_block + wib; q < chunk; q += nwarps) {
+    const long long p = point_of(c, q);
+    const int ti = find_task(g, p);
+    const DevTask T = g.tasks[ti];
+    if (T.all_mode || (T.mixed && !c.plist))
+      continue;
+    const int prow = g.pred_rows[T.pred_off + (int)(p - T.point_base)];
+    for (int j = lane; j < g.Ea; j += 32)
+      sy[j] = g.Fp[(size_t)prow * g.Ea + j];
+    const int ppanel = g.panel ? g.panel[prow] : 0;
+    const double ptime = g.point_time[prow];
+    __syncwarp();
+    const int k = T.k;
+    int count = 0, numValid = 0;
+    for (int b0 = 0; b0 < T.n_lib; b0 += 32) {
+      const int i = b0 + lane;
+      double d = 0;
+      bool valid = false;
+      if (i < T.n_lib)
+        valid = exact_distance(g, g.lib_rows[T.lib_off + i], prow, sy, ppanel, ptime, d);
+      numValid += __popc(__ballot_sync(FULL, valid));
+      const double thr = (k <= 0 || count < k) ? DBL_MAX : sD[k - 1];
+      unsigned cm = __ballot_sync(FULL, valid && k > 0 && (count < k ? true : d < thr));
+      while (cm) {
+        const int src = __ffs(cm) - 1;
+        cm &= cm - 1;
+        const double dd = __shfl_sync(FULL, d, src);
+        if (count == k && !(dd < sD[k - 1]))
+          continue;
+        int cnt = 0;
+        for (int e = lane; e < count; e += 32)
+          cnt += sD[e] <= dd;
+        const int pos = __reduce_add_sync(FULL, cnt);
+        const int last = count < k - 1 ? count : k - 1;
+        for (int top = last; top > pos; top -= 32) {
+          const int e = top - 1 - lane;
+          const bool act = e >= pos;
+          double vD = 0;
+          int vI = 0;
+          if (act) {
+            vD = sD[e];
+            vI = sI[e];
+          }
+          __syncwarp();
+          if (act) {
+            sD[e + 1] = vD;
+            sI[e + 1] = vI;
+          }
+          __syncwarp();
+        }
+        if (lane == 0) {
+          sD[pos] = dd;
+          sI[pos] = b0 + src;
+        }
+        count = count + 1 < k ? count + 1 : k;
+        __syncwarp();
+      }
+    }
+    int status = PT_OK, keff = k;
+    if (k > numValid) {
+      if (g.force_compute)
+        keff = numValid;
+      else
+        status = PT_INSUFFICIENT;
+    }
+    if (status == PT_OK && (keff == 0 || numValid == 0))
+      status = g.force_compute ? PT_EARLY_SUCCESS : PT_INSUFFICIENT;
+    int* oi = c.nn_idx + q * c.kcap;
+    double* od = c.nn_dist + q * c.kcap;
+    if (status == PT_OK) {
+      if (keff == numValid) {
+        // all valid neighbours, in library order (src/edm.cpp:615-616)
+        for (int e = lane; e < count; e += 32) {
+          int r = 0;
+          const int me = sI[e];
+          for (int f = 0; f < count; f++)
+            r += sI[f] < me;
+          oi[r] = me;
+          od[r] = sD[e];
+        }
+      } else {
+        for (int e = lane; e < keff; e += 32) {
+          oi[e] = sI[e];
+          od[e] = sD[e];
+        }
+      }
+    }
+    if (lane == 0) {
+      c.status[q] = status;
+      c.nn_count[q] = keff;
+      if (status == PT_OK)
+        note_k(g, T.task, p, keff);
+      else if (g.kused)
+        g.kused[p] = INT_MIN;
+    }
+    __syncwarp();
+  }
+}
+
+// ------------------------------------------------------------- simplex
+// src/edm.cpp:707-735, one thread per (point, theta).
+__global__ void simplex_nn_kernel(GroupParams g, ChunkBuffers c)
+{
+  const long long chunk = c.p_end - c.p_begin;
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= chunk * g.n_thetas)
+    return;
+  const int t = (int)(idx / chunk);
+  const long long q = idx - (long long)t * chunk;
+  const long long p = point_of(c, q);
+  const DevTask T = g.tasks[find_task(g, p)];
+  if (T.all_mode || (T.mixed && !c.plist))
+    return;
+  const int st = c.status[q];
+  if (st != PT_OK) {
+    early_rc(g, T.task, st, t);
+    return;
+  }
+  const int ke = c.nn_count[q];
+  const double* dists = c.nn_dist + q * c.kcap;
+  const int* inds = c.nn_idx + q * c.kcap;
+  double minDist = dists[0];
+  for (int j = 1; j < ke; j++)
+    minDist = dists[j] < minDist ? dists[j] : minDist;
+  const double theta = g.thetas[t];
+  double sumw = 0.0;
+  for (int j = 0; j < ke; j++)
+    sumw = sumw + exp_rn(-theta * (dists[j] / minDist));
+  double r = 0.0;
+  for (int j = 0; j < ke; j++) {
+    const double w = exp_rn(-theta * (dists[j] / minDist));
+    r = r + g.lib_target[g.lib_rows[T.lib_off + inds[j]]] * (w / sumw);
+  }
+  g.pred[(size_t)t * g.total_points + p] = r;
+}
+
+// ---------------------------------------------------------------- S-map
+// Forecast from coefficients (src/edm.cpp:784-812).
+__device__ __forceinline__ void smap_finish(const GroupParams& g, const DevTask& T, long long p, int prow, int t,
+                                            const double* ics, int n)
+{
+  const double* y = g.Fp + (size_t)prow * g.Ea;
+  double r = ics[0];
+  for (int j = 0; j < g.Ea; j++) {
+    const double yj = y[j];
+    if (yj != MISS)
+      r += yj * ics[j + 1];
+  }
+  if (g.coeffs && T.save_coeffs && t == g.n_thetas - 1) {
+    for (int j = 0; j < n; j++)
+      g.coeffs[(size_t)p * n + j] = fabs(ics[j]) < 1.0e-11 ? MISS : ics[j];
+  }
+  g.pred[(size_t)t * g.total_points + p] = r;
+}
+
+constexpr int SMALL_N = 8;
+
+// src/edm.cpp:737-814 for a finite neighbour list, one thread per
+// (point, theta).  X^T X and X^T y are summed over the neighbours in order.
+__global__ void smap_nn_kernel(GroupParams g, ChunkBuffers c, long long slab)
+{
+  const long long chunk = c.p_end - c.p_begin;
+  const long long nthreads = (long long)gridDim.x * blockDim.x;
+  const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int n = g.Ea + 1;
+  double lW[SMALL_N * SMALL_N], lU[SMALL_N * SMALL_N], lV[SMALL_N * SMALL_N], lsv[SMALL_N], ltmp[SMALL_N],
+    lb[SMALL_N], lx[SMALL_N];
+  double *W = lW, *U = lU, *V = lV, *sv = lsv, *tmp = ltmp, *bv = lb, *xs = lx;
+  if (n > SMALL_N) {
+    double* s = c.scratch + tid * slab;
+    W = s;
+    U = W + n * n;
+    V = U + n * n;
+    sv = V + n * n;
+    tmp = sv + n;
+    bv = tmp + n;
+    xs = bv + n;
+  }
+  for (long long idx = tid; idx < chunk * g.n_thetas; idx += nthreads) {
+    const int t = (int)(idx / chunk);
+    const long long q = idx - (long long)t * chunk;
+    const long long p = point_of(c, q);
+    const DevTask T = g.tasks[find_task(g, p)];
+    if (T.all_mode || (T.mixed && !c.plist))
+      continue;
+    const int st = c.status[q];
+    if (st != PT_OK) {
+      early_rc(g, T.task, st, t);
+      continue;
+    }
+    const int ke = c.nn_count[q];
+    const double* dists = c.nn_dist + q * c.kcap;
+    const int* inds = c.nn_idx + q * c.kcap;
+    double mean = 0;
+    for (int j = 0; j < ke; j++)
+      mean += dists[j];
+    mean /= (double)ke;
+    const double theta = g.thetas[t];
+    for (int a = 0; a < n; a++) {
+      for (int b = a; b < n; b++) {
+        double s = 0;
+        for (int i = 0; i < ke; i++) {
+          const double w = exp_rn(-theta * (dists[i] / mean));
+          const int row = g.lib_rows[T.lib_off + inds[i]];
+          const double xa = a == 0 ? w : w * g.F[(size_t)row * g.Ea + a - 1];
+          const double xb = b == 0 ? w : w * g.F[(size_t)row * g.Ea + b - 1];
+          s += xa * xb;
+        }
+        W[a * n + b] = s;
+        W[b * n + a] = s;
+      }
+      double s = 0;
+      for (int i = 0; i < ke; i++) {
+        const double w = exp_rn(-theta * (dists[i] / mean));
+        const int row = g.lib_rows[T.lib_off + inds[i]];
+        const double xa = a == 0 ? w : w * g.F[(size_t)row * g.Ea + a - 1];
+        s += xa * (w * g.lib_target[row]);
+      }
+      bv[a] = s;
+    }
+    svd_solve(W, U, V, sv, tmp, bv, xs, n);
+    const int prow = g.pred_rows[T.pred_off + (int)(p - T.point_base)];
+    smap_finish(g, T, p, prow, t, xs, n);
+  }
+}
+
+// ------------------------------------------------------ all-neighbour mode
+// k = -1 (or k >= library size): every valid neighbour in library order
+// (src/edm.cpp:613-617).  One warp per point; the point's distances are kept
+// in the warp's scratch row and the weighted sums are warp reductions.
+__device__ __forceinline__ double warp_sum_d(double v)
+{
+  for (int o = 16; o > 0; o >>= 1)
+    v += __shfl_xor_sync(FULL, v, o);
+  return v;
+}
+__device__ __forceinline__ double warp_min_d(double v)
+{
+  for (int o = 16; o > 0; o >>= 1)
+    v = fmin(v, __shfl_xor_sync(FULL, v, o));
+  return v;
+}
+
+__global__ void all_mode_kernel(GroupParams g, ChunkBuffers c, long long max_nlib, int per_warp_bytes)
+{
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, wpb = blockDim.x >> 5;
+  const long long gw = (long long)blockIdx.x * wpb + wib;
+  const long long nwarps = (long long)gridDim.x * wpb;
+  double* scr = c.scratch + gw * max_nlib;
+  const int n = g.Ea + 1;
+  const int nent = n * (n + 1) / 2 + n;
+  unsigned char* base = smem + (size_t)wib * per_warp_bytes;
+  double* sy = (double*)base;           // [Ea]
+  double* sX = sy + g.Ea;               // [32 x (n+1)]
+  double* sG = sX + 32 * (n + 1);       // [nent]
+  for (long long p = c.p_begin + gw; p < c.p_end; p += nwarps) {
+    const long long q = p - c.p_begin;
+    const DevTask T = g.tasks[find_task(g, p)];
+    if (!T.all_mode)
+      continue;
+    const int prow = g.pred_rows[T.pred_off + (int)(p - T.point_base)];
+    for (int j = lane; j < g.Ea; j += 32)
+      sy[j] = g.Fp[(size_t)prow * g.Ea + j];
+    const int ppanel = g.panel ? g.panel[prow] : 0;
+    const double ptime = g.point_time[prow];
+    __syncwarp();
+    double lmin = DBL_MAX, lsum = 0;
+    int lcnt = 0;
+    for (int i = lane; i < T.n_lib; i += 32) {
+      double d;
+      if (exact_distance(g, g.lib_rows[T.lib_off + i], prow, sy, ppanel, ptime, d)) {
+        scr[i] = d;
+        lmin = fmin(lmin, d);
+        lsum += d;
+        lcnt++;
+      } else {
+        scr[i] = -1.0;
+      }
+    }
+    const int cnt = __reduce_add_sync(FULL, lcnt);
+    const double dmin = warp_min_d(lmin);
+    const double mean = warp_sum_d(lsum) / (double)cnt;
+    int status = PT_OK;
+    if (!g.force_compute && T.k > 0 && T.k > cnt)
+      status = PT_INSUFFICIENT;
+    else if (cnt == 0)
+      status = g.force_compute ? PT_EARLY_SUCCESS : PT_INSUFFICIENT;
+    if (status != PT_OK) {
+      if (lane < g.n_thetas)
+        for (int t = lane; t < g.n_thetas; t += 32)
+          early_rc(g, T.task, status, t);
+      if (lane == 0 && g.kused)
+        g.kused[p] = INT_MIN;
+      __syncwarp();
+      continue;
+    }
+    if (lane == 0)
+      note_k(g, T.task, p, cnt);
+    for (int t = 0; t < g.n_thetas; t++) {
+      const double theta = g.thetas[t];
+      if (g.algorithm == 0) {
+        double ls = 0;
+        for (int i = lane; i < T.n_lib; i += 32)
+          if (scr[i] >= 0)
+            ls = ls + exp_rn(-theta * (scr[i] / dmin));
+        const double sumw = warp_sum_d(ls);
+        double lr = 0;
+        for (int i = lane; i < T.n_lib; i += 32)
+          if (scr[i] >= 0) {
+            const double w = exp_rn(-theta * (scr[i] / dmin));
+            lr = lr + g.lib_target[g.lib_rows[T.lib_off + i]] * (w / sumw);
+          }
+        const double r = warp_sum_d(lr);
+        if (lane == 0)
+          g.pred[(size_t)t * g.total_points + p] = r;
+      } else {
+        for (int e = lane; e < nent; e += 32)
+          sG[e] = 0;
+        __syncwarp();
+        for (int b0 = 0; b0 < T.n_lib; b0 += 32) {
+          const int i = b0 + lane;
+          double* xr = sX + lane * (n + 1);
+          if (i < T.n_lib && scr[i] >= 0) {
+            const double w = exp_rn(-theta * (scr[i] / mean));
+            const int row = g.lib_rows[T.lib_off + i];
+            xr[0] = w;
+            for (int j = 1; j < n; j++)
+              xr[j] = w * g.F[(size_t)row * g.Ea + j - 1];
+            xr[n] = w * g.lib_target[row];
+          } else {
+            for (int j = 0; j <= n; j++)
+              xr[j] = 0;
+          }
+          __syncwarp();
+          for (int e = lane; e < nent; e += 32) {
+            int a, b;
+            if (e < n * (n + 1) / 2) {
+              // e -> (a, b) with a <= b, row-major upper triangle
+              a = 0;
+              int rem = e;
+              while (rem >= n - a) {
+                rem -= n - a;
+                a++;
+              }
+              b = a + rem;
+            } else {
+              a = e - n * (n + 1) / 2;
+              b = n;  // the y column
+            }
+            double acc = sG[e];
+            for (int r = 0; r < 32; r++)
+              acc += sX[r * (n + 1) + a] * sX[r * (n + 1) + b];
+            sG[e] = acc;
+          }
+          __syncwarp();
+        }
+        double* G = c.gram + (q * g.n_thetas + t) * (long long)(n * n + n);
+        for (int e = lane; e < nent; e += 32) {
+          if (e < n * (n + 1) / 2) {
+            int a = 0, rem = e;
+            while (rem >= n - a) {
+              rem -= n - a;
+              a++;
+            }
+            const int b = a + rem;
+            G[a * n + b] = sG[e];
+            G[b * n + a] = sG[e];
+          } else {
+            G[n * n + (e - n * (n + 1) / 2)] = sG[e];
+          }
+        }
+        __syncwarp();
+      }
+    }
+    if (lane == 0)
+      c.status[q] = PT_OK;
+  }
+}
+
+// Solves the all-mode S-map systems written by all_mode_kernel.
+__global__ void smap_all_solve_kernel(GroupParams g, ChunkBuffers c, long long slab)
+{
+  const long long chunk = c.p_end - c.p_begin;
+  const long long nthreads = (long long)gridDim.x * blockDim.x;
+  const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int n = g.Ea + 1;
+  double lW[SMALL_N * SMALL_N], lU[SMALL_N * SMALL_N], lV[SMALL_N * SMALL_N], lsv[SMALL_N], ltmp[SMALL_N],
+    lx[SMALL_N];
+  double *W = lW, *U = lU, *V = lV, *sv = lsv, *tmp = ltmp, *xs = lx;
+  if (n > SMALL_N) {
+    double* s = c.scratch + tid * slab;
+    W = s;
+    U = W + n * n;
+    V = U + n * n;
+    sv = V + n * n;
+    tmp = sv + n;
+    xs = tmp + n;
+  }
+  for (long long idx = tid; idx < chunk * g.n_thetas; idx += nthreads) {
+    const int t = (int)(idx / chunk);
+    const long long q = idx - (long long)t * chunk;
+    const long long p = c.p_begin + q;
+    const DevTask T = g.tasks[find_task(g, p)];
+    if (!T.all_mode || c.status[q] != PT_OK)
+      continue;
+    const double* G = c.gram + (q * g.n_thetas + t) * (long long)(n * n + n);
+    for (int i = 0; i < n * n; i++)
+      W[i] = G[i];
+    svd_solve(W, U, V, sv, tmp, G + n * n, xs, n);
+    const int prow = g.pred_rows[T.pred_off + (int)(p - T.point_base)];
+    smap_finish(g, T, p, prow, t, xs, n);
+  }
+}
+
+// ----------------------------------------------------------------- stats
+// rho and MAE per (task, theta) over forecasts whose target is observed
+// (src/edm.cpp:441-467, src/stats.cpp:64-94).  Two passes like the
+// reference's centred correlation.
+__global__ void stats_kernel(GroupParams g, double* rho, double* mae)
+{
+  __shared__ double red[5][256];
+  const int ti = blockIdx.x / g.n_thetas, t = blockIdx.x % g.n_thetas;
+  const DevTask T = g.tasks[ti];
+  const double* pr = g.pred + (size_t)t * g.total_points + T.point_base;
+  double c = 0, s1 = 0, s2 = 0, sa = 0;
+  for (int i = threadIdx.x; i < T.n_pred; i += blockDim.x) {
+    const double y1 = g.pred_target[g.pred_rows[T.pred_off + i]], y2 = pr[i];
+    if (y1 != MISS && y2 != MISS) {
+      c += 1;
+      s1 += y1;
+      s2 += y2;
+      sa += fabs(y1 - y2);
+    }
+  }
+  red[0][threadIdx.x] = c;
+  red[1][threadIdx.x] = s1;
+  red[2][threadIdx.x] = s2;
+  red[3][threadIdx.x] = sa;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o)
+      for (int v = 0; v < 4; v++)
+        red[v][threadIdx.x] += red[v][threadIdx.x + o];
+    __syncthreads();
+  }
+  const double cnt = red[0][0], m1 = red[1][0] / cnt, m2 = red[2][0] / cnt, sabs = red[3][0];
+  __syncthreads();
+  double s11 = 0, s22 = 0, s12 = 0;
+  for (int i = threadIdx.x; i < T.n_pred; i += blockDim.x) {
+    const double y1 = g.pred_target[g.pred_rows[T.pred_off + i]], y2 = pr[i];
+    if (y1 != MISS && y2 != MISS) {
+      const double a = y1 - m1, b = y2 - m2;
+      s11 += a * a;
+      s22 += b * b;
+      s12 += a * b;
+    }
+  }
+  red[0][threadIdx.x] = s11;
+  red[1][threadIdx.x] = s22;
+  red[2][threadIdx.x] = s12;
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o)
+      for (int v = 0; v < 3; v++)
+        red[v][threadIdx.x] += red[v][threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    double r = MISS, m = MISS;
+    if (cnt > 0) {
+      const double sd1 = sqrt(red[0][0]), sd2 = sqrt(red[1][0]);
+      r = (sd1 < 1e-9 || sd2 < 1e-9) ? MISS : red[2][0] / (sd1 * sd2);
+      const double v = sabs / cnt;
+      m = v < 1e-8 ? 0 : v;
+    }
+    rho[T.task * g.n_thetas + t] = r;
+    mae[T.task * g.n_thetas + t] = m;
+  }
+}
+
+int knn_warps_per_block(int Ea, int kcap, int& per_warp)
+{
+  per_warp = ((Ea * 8 + kcap * 12) + 15) / 16 * 16;
+  int w = 8;
+  while (w > 1 && (long long)w * per_warp > 200 * 1024)
+    w >>= 1;
+  return w;
+}
+
+int all_warps_per_block(int Ea, int& per_warp)
+{
+  const int n = Ea + 1;
+  per_warp = ((Ea + 32 * (n + 1) + n * (n + 1) / 2 + n) * 8 + 15) / 16 * 16;
+  int w = 4;
+  while (w > 1 && (long long)w * per_warp > 200 * 1024)
+    w >>= 1;
+  return w;
+}
+
+} // namespace
+
+void launch_knn_exact(const GroupParams& g, const ChunkBuffers& c, int num_sms, cudaStream_t s)
+{
+  int per_warp;
+  const int w = knn_warps_per_block(g.Ea, c.kcap, per_warp);
+  const size_t smem = (size_t)w * per_warp;
+  if (smem > 48 * 1024)
+    cudaFuncSetAttribute(knn_exact_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  const long long chunk = c.p_end - c.p_begin;
+  long long blocks = (chunk + w - 1) / w;
+  const long long cap = (long long)num_sms * 64;
+  if (blocks > cap)
+    blocks = cap;
+  if (blocks < 1)
+    blocks = 1;
+  knn_exact_kernel<<<(int)blocks, 32 * w, smem, s>>>(g, c, w, per_warp);
+}
+
+void launch_simplex_nn(const GroupParams& g, const ChunkBuffers& c, cudaStream_t s)
+{
+  const long long total = (c.p_end - c.p_begin) * g.n_thetas;
+  if (total <= 0)
+    return;
+  simplex_nn_kernel<<<(int)((total + 255) / 256), 256, 0, s>>>(g, c);
+}
+
+long long smap_nn_scratch_doubles(int num_sms, int n, int kcap)
+{
+  (void)kcap;
+  if (n <= SMALL_N)
+    return 0;
+  const long long slab = 3LL * n * n + 4LL * n;
+  return (long long)num_sms * 4 * 128 * slab;
+}
+
+void launch_smap_nn(const GroupParams& g, const ChunkBuffers& c, int num_sms, cudaStream_t s)
+{
+  const int n = g.Ea + 1;
+  const long long slab = 3LL * n * n + 4LL * n;
+  const long long total = (c.p_end - c.p_begin) * g.n_thetas;
+  if (total <= 0)
+    return;
+  long long blocks = (total + 127) / 128;
+  if (n > SMALL_N) {
+    const long long cap = c.scratch_doubles / (128 * slab);
+    if (blocks > cap)
+      blocks = cap;
+  } else if (blocks > (long long)num_sms * 64) {
+    blocks = (long long)num_sms * 64;
+  }
+  if (blocks < 1)
+    blocks = 1;
+  smap_nn_kernel<<<(int)blocks, 128, 0, s>>>(g, c, slab);
+}
+
+long long all_mode_scratch_doubles(int num_sms, long long max_nlib)
+{
+  return (long long)num_sms * 8 * 4 * (max_nlib > 0 ? max_nlib : 1);
+}
+
+void launch_all_mode(const GroupParams& g, const ChunkBuffers& c, int num_sms, long long max_nlib, cudaStream_t s)
+{
+  int per_warp;
+  const int w = all_warps_per_block(g.Ea, per_warp);
+  const size_t smem = (size_t)w * per_warp;
+  if (smem > 48 * 1024)
+    cudaFuncSetAttribute(all_mode_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  const long long warps_avail = c.scratch_doubles / (max_nlib > 0 ? max_nlib : 1);
+  long long blocks = warps_avail / w;
+  const long long chunk = c.p_end - c.p_begin;
+  if (blocks > (chunk + w - 1) / w)
+    blocks = (chunk + w - 1) / w;
+  if (blocks < 1)
+    blocks = 1;
+  all_mode_kernel<<<(int)blocks, 32 * w, smem, s>>>(g, c, max_nlib, per_warp);
+  if (g.algorithm == 1) {
+    const int n = g.Ea + 1;
+    const long long slab = 3LL * n * n + 3LL * n;
+    const long long total = chunk * g.n_thetas;
+    long long b2 = (total + 127) / 128;
+    if (n > SMALL_N) {
+      const long long cap = c.scratch_doubles / (128 * slab);
+      if (b2 > cap)
+        b2 = cap;
+    } else if (b2 > (long long)num_sms * 64) {
+      b2 = (long long)num_sms * 64;
+    }
+    if (b2 < 1)
+      b2 = 1;
+    smap_all_solve_kernel<<<(int)b2, 128, 0, s>>>(g, c, slab);
+  }
+}
+
+void launch_stats(const GroupParams& g, const DevTask*, int n_tasks, double* rho, double* mae, cudaStream_t s)
+{
+  if (n_tasks <= 0)
+    return;
+  stats_kernel<<<n_tasks * g.n_thetas, 256, 0, s>>>(g, rho, mae);
+}
+
+} // namespace fedm

@@ -1,0 +1,230 @@
+// FP64 solvers for the S-map normal equations, written with explicit
+// round-to-nearest multiply and add intrinsics so that every translation unit
+// (with or without FMA contraction) computes the same bits.
+//
+// svd_solve restates Eigen 3.3's JacobiSVD of a square matrix (two-sided
+// Jacobi sweeps over (p, q) pairs with a 2x2 real SVD, singular values made
+// positive and sorted, rank threshold diagSize * epsilon) followed by
+// SVDBase::solve, which is what the reference calls
+// (EDM-Developers/fastEDM-r src/edm.cpp:780-782).  Eigen is MPL2; only its
+// published algorithm is followed.
+#pragma once
+
+#include <cfloat>
+
+namespace fedm {
+
+__device__ __forceinline__ double mul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double add(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double sub(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ double dvd(double a, double b) { return __ddiv_rn(a, b); }
+
+struct Rot
+{
+  double c, s;
+};
+
+// rows p, q <- J [row p; row q], J = [c s; -s c]
+__device__ __forceinline__ void rot_rows(double* A, int n, int p, int q, Rot j)
+{
+  for (int i = 0; i < n; i++) {
+    const double x = A[p * n + i], y = A[q * n + i];
+    A[p * n + i] = add(mul(j.c, x), mul(j.s, y));
+    A[q * n + i] = add(mul(-j.s, x), mul(j.c, y));
+  }
+}
+
+// cols p, q <- [col p, col q] J^T  (Eigen's applyOnTheRight)
+__device__ __forceinline__ void rot_cols(double* A, int n, int p, int q, Rot j)
+{
+  const double c = j.c, s = -j.s;
+  for (int i = 0; i < n; i++) {
+    const double x = A[i * n + p], y = A[i * n + q];
+    A[i * n + p] = add(mul(c, x), mul(s, y));
+    A[i * n + q] = add(mul(-s, x), mul(c, y));
+  }
+}
+
+__device__ inline void jacobi_2x2(const double* W, int n, int p, int q, Rot& jl, Rot& jr)
+{
+  const double tiny = DBL_MIN;
+  const double m00 = W[p * n + p], m01 = W[p * n + q], m10 = W[q * n + p], m11 = W[q * n + q];
+  Rot r1;
+  const double t = add(m00, m11), d = sub(m10, m01);
+  if (fabs(d) < tiny) {
+    r1.s = 0;
+    r1.c = 1;
+  } else {
+    const double u = dvd(t, d);
+    const double tmp = __dsqrt_rn(add(1.0, mul(u, u)));
+    r1.s = dvd(1.0, tmp);
+    r1.c = dvd(u, tmp);
+  }
+  const double n00 = add(mul(r1.c, m00), mul(r1.s, m10));
+  const double n01 = add(mul(r1.c, m01), mul(r1.s, m11));
+  const double n11 = add(mul(-r1.s, m01), mul(r1.c, m11));
+  const double deno = mul(2.0, fabs(n01));
+  if (deno < tiny) {
+    jr.c = 1;
+    jr.s = 0;
+  } else {
+    const double tau = dvd(sub(n00, n11), deno);
+    const double w = __dsqrt_rn(add(mul(tau, tau), 1.0));
+    const double tt = tau > 0 ? dvd(1.0, add(tau, w)) : dvd(1.0, sub(tau, w));
+    const double sign_t = tt > 0 ? 1.0 : -1.0;
+    const double nn = dvd(1.0, __dsqrt_rn(add(mul(tt, tt), 1.0)));
+    jr.s = mul(mul(mul(-sign_t, dvd(n01, fabs(n01))), fabs(tt)), nn);
+    jr.c = nn;
+  }
+  const double jtc = jr.c, jts = -jr.s;
+  jl.c = sub(mul(r1.c, jtc), mul(r1.s, jts));
+  jl.s = add(mul(r1.c, jts), mul(r1.s, jtc));
+}
+
+// Solves A x = b in the pseudo-inverse sense.  W holds A (n x n, destroyed);
+// U, V: n*n scratch; sv, tmp: n scratch.
+__device__ inline void svd_solve(double* W, double* U, double* V, double* sv, double* tmp, const double* b, double* x,
+                                 int n)
+{
+  const double tiny = DBL_MIN, eps = DBL_EPSILON, precision = 2 * DBL_EPSILON;
+  double scale = 0;
+  for (int i = 0; i < n * n; i++)
+    scale = fmax(scale, fabs(W[i]));
+  if (!isfinite(scale)) {
+    for (int i = 0; i < n; i++)
+      x[i] = 0;
+    return;
+  }
+  if (scale == 0)
+    scale = 1;
+  for (int i = 0; i < n * n; i++) {
+    W[i] = dvd(W[i], scale);
+    U[i] = 0;
+    V[i] = 0;
+  }
+  for (int i = 0; i < n; i++)
+    U[i * n + i] = V[i * n + i] = 1;
+  double maxDiag = 0;
+  for (int i = 0; i < n; i++)
+    maxDiag = fmax(maxDiag, fabs(W[i * n + i]));
+  bool finished = false;
+  int sweeps = 0;
+  while (!finished && sweeps < 100) {
+    finished = true;
+    sweeps++;
+    for (int p = 1; p < n; p++) {
+      for (int q = 0; q < p; q++) {
+        const double threshold = fmax(tiny, mul(precision, maxDiag));
+        if (fabs(W[p * n + q]) > threshold || fabs(W[q * n + p]) > threshold) {
+          finished = false;
+          Rot jl, jr;
+          jacobi_2x2(W, n, p, q, jl, jr);
+          rot_rows(W, n, p, q, jl);
+          rot_cols(U, n, p, q, Rot{ jl.c, -jl.s });
+          rot_cols(W, n, p, q, jr);
+          rot_cols(V, n, p, q, jr);
+          maxDiag = fmax(maxDiag, fmax(fabs(W[p * n + p]), fabs(W[q * n + q])));
+        }
+      }
+    }
+  }
+  for (int i = 0; i < n; i++) {
+    const double a = W[i * n + i];
+    sv[i] = fabs(a);
+    if (a < 0)
+      for (int r = 0; r < n; r++)
+        U[r * n + i] = -U[r * n + i];
+  }
+  for (int i = 0; i < n; i++)
+    sv[i] = mul(sv[i], scale);
+  int nonzero = n;
+  for (int i = 0; i < n; i++) {
+    int pos = i;
+    double mx = sv[i];
+    for (int j = i + 1; j < n; j++)
+      if (sv[j] > mx) {
+        mx = sv[j];
+        pos = j;
+      }
+    if (mx == 0) {
+      nonzero = i;
+      break;
+    }
+    if (pos != i) {
+      const double s0 = sv[i];
+      sv[i] = sv[pos];
+      sv[pos] = s0;
+      for (int r = 0; r < n; r++) {
+        const double u0 = U[r * n + i];
+        U[r * n + i] = U[r * n + pos];
+        U[r * n + pos] = u0;
+        const double v0 = V[r * n + i];
+        V[r * n + i] = V[r * n + pos];
+        V[r * n + pos] = v0;
+      }
+    }
+  }
+  const double thr = fmax(mul(sv[0], mul((double)(n > 1 ? n : 1), eps)), tiny);
+  int i = nonzero - 1;
+  while (i >= 0 && sv[i] < thr)
+    --i;
+  const int rank = i + 1;
+  for (int cc = 0; cc < rank; cc++) {
+    double s = 0;
+    for (int r = 0; r < n; r++)
+      s = add(s, mul(U[r * n + cc], b[r]));
+    tmp[cc] = mul(dvd(1.0, sv[cc]), s);
+  }
+  for (int r = 0; r < n; r++) {
+    double s = 0;
+    for (int cc = 0; cc < rank; cc++)
+      s = add(s, mul(V[r * n + cc], tmp[cc]));
+    x[r] = s;
+  }
+}
+
+// Square-root-free Cholesky (LDL^T) solve of the symmetric normal equations
+// in FP64.  Returns false when a pivot is not clearly positive relative to
+// the largest one (pivot ratio below `min_ratio`), i.e. when the system is too
+// ill-conditioned for the unpivoted factorisation to match the SVD solve; the
+// caller then uses svd_solve.  A (n x n) is overwritten by L and D.
+__device__ inline bool ldlt_solve(double* A, const double* b, double* x, int n, double min_ratio)
+{
+  double dmax = 0;
+  for (int j = 0; j < n; j++) {
+    double d = A[j * n + j];
+    for (int k = 0; k < j; k++)
+      d = sub(d, mul(mul(A[j * n + k], A[j * n + k]), A[k * n + k]));
+    if (!(d > 0))
+      return false;
+    dmax = fmax(dmax, d);
+    A[j * n + j] = d;
+    for (int i = j + 1; i < n; i++) {
+      double s = A[i * n + j];
+      for (int k = 0; k < j; k++)
+        s = sub(s, mul(mul(A[i * n + k], A[j * n + k]), A[k * n + k]));
+      A[i * n + j] = dvd(s, d);
+    }
+  }
+  for (int j = 0; j < n; j++)
+    if (A[j * n + j] < mul(min_ratio, dmax))
+      return false;
+  // L z = b, D y = z, L^T x = y
+  for (int i = 0; i < n; i++) {
+    double s = b[i];
+    for (int k = 0; k < i; k++)
+      s = sub(s, mul(A[i * n + k], x[k]));
+    x[i] = s;
+  }
+  for (int i = 0; i < n; i++)
+    x[i] = dvd(x[i], A[i * n + i]);
+  for (int i = n - 1; i >= 0; i--) {
+    double s = x[i];
+    for (int k = i + 1; k < n; k++)
+      s = sub(s, mul(A[k * n + i], x[k]));
+    x[i] = s;
+  }
+  return true;
+}
+
+} // namespace fedm

@@ -1,0 +1,199 @@
+/*
+ * fastedm_gb300.h -- C ABI of the GB300 (sm_103a) implementation of fastEDM's
+ * prediction path: lagged manifolds, pairwise distances with exact
+ * k-nearest-neighbour selection, simplex and S-map forecasts, and the
+ * convergent-cross-mapping library-size x replicate loop.
+ *
+ * The ABI takes plain pointers and sizes only.  Every entry point returns an
+ * int status from the reference's return-code table (src/common.h:3-13 of
+ * EDM-Developers/fastEDM-r): 0 SUCCESS, 1 BREAK_HIT, 400 INVALID_ALGORITHM,
+ * 503 INSUFFICIENT_UNIQUE, 908 NOT_IMPLEMENTED, 8000 UNKNOWN_ERROR.  CUDA
+ * failures map to 8000 with a message in fedm_last_error().  No C++
+ * exception crosses this boundary.  One context is not re-entrant; distinct
+ * contexts may be used from distinct threads.
+ */
+#ifndef FASTEDM_GB300_H
+#define FASTEDM_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FEDM_SUCCESS 0
+#define FEDM_BREAK_HIT 1
+#define FEDM_INVALID_ALGORITHM 400
+#define FEDM_INSUFFICIENT_UNIQUE 503
+#define FEDM_NOT_IMPLEMENTED 908
+#define FEDM_UNKNOWN_ERROR 8000
+
+/* Arithmetic of the distance / neighbour step.
+ *  FEDM_PRECISION_FP64:  every distance in FP64 in the reference's operation
+ *                        order ("plain FP64 GPU form").
+ *  FEDM_PRECISION_MIXED: FP32 candidate distances with a proven error margin,
+ *                        then an FP64 re-rank of every candidate inside the
+ *                        margin, so neighbour sets and distances are the same
+ *                        bits as FP64; the FP64 S-map solve uses a faster
+ *                        normal-equation path when it is well conditioned.
+ *                        Falls back to FP64 where its preconditions (no
+ *                        missing values, no panels, L2) do not hold. */
+#define FEDM_PRECISION_FP64 0
+#define FEDM_PRECISION_MIXED 1
+
+typedef struct fedm_ctx fedm_ctx;
+
+/* Opens a context on CUDA device `device` (its own stream and memory pool).
+ * Replaces the reference's process-global thread pools (src/edm.cpp:79-88). */
+int fedm_create(int device, fedm_ctx** out);
+void fedm_destroy(fedm_ctx* ctx);
+const char* fedm_last_error(const fedm_ctx* ctx);
+/* Selects FEDM_PRECISION_*; the default is FEDM_PRECISION_MIXED. */
+int fedm_set_precision(fedm_ctx* ctx, int precision);
+/* Optional cancellation callback, polled between GPU chunks (the
+ * reference's keep_going(), src/edm.cpp:572-591).  Returning 0 stops the run
+ * with FEDM_BREAK_HIT. */
+int fedm_set_keep_going(fedm_ctx* ctx, int (*keep_going)(void));
+
+/* Arguments of the reference's run_command (src/r.cpp:107-117) after
+ * edm()'s normalisation (R/edm.R:241-322).  NA is passed as NaN.  Optional
+ * arrays are NULL. */
+typedef struct fedm_args {
+  int n;
+  const double* t;
+  const double* x;
+  const double* y;          /* xmap variable; NULL => explore mode          */
+  const int* panel;         /* panel ids, NA = INT_MIN; NULL => no panels    */
+  const double* co_x;       /* coprediction variable; NULL => none           */
+  int num_extras;
+  const double* extras;     /* num_extras * n; extra e starts at e*n         */
+  const int* Es;
+  int nE;
+  int tau;
+  const double* thetas;
+  int n_thetas;
+  const int* libs;          /* NULL => library = NULL in R                   */
+  int n_libs;
+  int k;                    /* 0 default, -1 all (k = Inf in R)              */
+  int algorithm;            /* 0 simplex, 1 smap                             */
+  int num_reps;
+  int p;
+  int crossfold;
+  int full;
+  int shuffle;
+  int seed;
+  int save_predictions;
+  int save_copredictions;
+  int save_manifolds;
+  int save_smap_coeffs;
+  int dt;
+  int reldt;
+  double dt_weight;
+  int allow_missing;
+  double missing_distance;
+  double panel_weight;      /* -1 => panelWeight = Inf (skip other panels)   */
+  const double* panel_weights; /* n_panel_weights^2, column-major           */
+  int n_panel_weights;
+  int num_threads;          /* host threads for manifold construction        */
+  int low_memory;
+  int predict_with_past;
+} fedm_args;
+
+/* The list run_command returns (src/r.cpp:420-457), flattened.  NA is NaN
+ * (doubles) or INT_MIN (ints).  Matrices are column-major like R's. */
+typedef struct fedm_result {
+  int rc;
+  int n_stats;
+  const int* stat_E;
+  const int* stat_library;
+  const double* stat_theta;
+  const double* stat_rho;
+  const double* stat_mae;
+  int n_costats;
+  const int* costat_E;
+  const int* costat_library;
+  const double* costat_theta;
+  const double* costat_rho;
+  const double* costat_mae;
+  int kmin;
+  int kmax;
+  int pred_rows, pred_cols;
+  const double* predictions;
+  int copred_rows, copred_cols;
+  const double* copredictions;
+  int coeff_rows, coeff_cols;
+  const double* coeffs;
+  double missing_distance;  /* NaN unless allow_missing                       */
+  double dt_weight;         /* NaN unless dt or reldt                         */
+  void* internal;
+} fedm_result;
+
+/* Replaces run_command -> launch_tasks -> edm_task (src/r.cpp:107-468,
+ * src/edm.cpp:256-283, src/edm.cpp:285-548): all tasks of the call (every
+ * E x library size x replicate/fold, and the coprediction tasks) are
+ * configured on the host with the reference's splitter and RNG and executed
+ * as batched GPU launches.  *out must be released with fedm_free_result. */
+int fedm_run_command(fedm_ctx* ctx, const fedm_args* args, fedm_result** out);
+void fedm_free_result(fedm_result* r);
+
+/* One prediction task on explicit masks, the seam of edm_task /
+ * af_make_prediction (src/edm.cpp:285-548, decl :66-71): library rows
+ * `library_rows`, prediction rows `prediction_rows` (n bytes each).  The
+ * first call (buffers NULL) fills the sizes; the second fills the
+ * caller-allocated outputs:
+ *   predictions[n_thetas*n_pred] (theta-major), coeffs[n_pred*(e_actual+1)],
+ *   rc[n_thetas*n_pred], kused[n_pred], nn_offsets[n_pred+1],
+ *   nn_idx[total_nn], nn_dist[total_nn], stats_rho[n_thetas],
+ *   stats_mae[n_thetas]
+ * nn_idx are indices into the task's library manifold (rows kept after
+ * dropping missing targets), in the order make_prediction uses them
+ * (src/edm.cpp:608-619). */
+typedef struct fedm_task_io {
+  const unsigned char* library_rows;
+  const unsigned char* prediction_rows;
+  int E;
+  int k;
+  int copredict;
+  int distance;       /* 0 mean absolute error (L1), 1 Euclidean (L2)      */
+  int force_compute;
+  int n_pred, n_lib, e_actual, total_nn;
+  double* predictions;
+  double* coeffs;
+  int* rc;
+  int* kused;
+  int* nn_offsets;
+  int* nn_idx;
+  double* nn_dist;
+  double* stats_rho;
+  double* stats_mae;
+} fedm_task_io;
+
+int fedm_run_task(fedm_ctx* ctx, const fedm_args* args, fedm_task_io* io);
+
+/* Timing of the last fedm_run_command / fedm_run_task, from CUDA events on
+ * the context's stream: device time from the first kernel of each batch
+ * (inputs already uploaded) to its statistics, time of the dominant
+ * distance/neighbour kernel and its launch count, and the host wall time of
+ * the whole call (ms). */
+typedef struct fedm_timing {
+  double device_ms;
+  double knn_kernel_ms;
+  int knn_launches;
+  double host_ms;
+  long long distance_pairs;  /* (prediction, library) pairs examined        */
+  long long predictions;     /* (prediction point, theta) forecasts made    */
+  long long h2d_bytes;
+  long long d2h_bytes;
+  int fallback_points;       /* mixed path: points re-run in exact FP64      */
+  int kernel_launches;       /* kernels this library launched                */
+} fedm_timing;
+
+int fedm_last_timing(const fedm_ctx* ctx, fedm_timing* out);
+
+/* Measured arithmetic peak of this GPU in TFLOP/s (2 flops per fused
+ * multiply-add): kind 0 FP32 FFMA, 1 FP64 DFMA, 2 packed FP32 FFMA2.  A
+ * diagnostic for roofline fractions; it has no counterpart in the reference. */
+int fedm_measure_peak(fedm_ctx* ctx, int kind, double* tflops);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

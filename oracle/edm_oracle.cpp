@@ -61,6 +61,56 @@ inline int wrap_add(int a, long long b)
   return (int)(uint32_t)((uint32_t)a + (uint32_t)(int64_t)b);
 }
 
+// ------------------------------------------------------------------- exp
+// The reference calls std::exp (src/edm.cpp:723,745).  For bit-level
+// comparison with the GPU library the oracle can instead evaluate the same
+// IEEE-only exp formula the device uses: Cody-Waite reduction with a 32-bit
+// head of ln 2, a degree-13 Taylor polynomial with fused multiply-adds and an
+// exact 2^k scaling.  Mode 0 (default) = std::exp, mode 1 = that formula.
+int g_exp_mode = 0;
+
+double pow2i(int k)
+{
+  uint64_t b = (uint64_t)(k + 1023) << 52;
+  double d;
+  std::memcpy(&d, &b, 8);
+  return d;
+}
+
+double exp_rn(double x)
+{
+  if (!(x == x))
+    return x;
+  if (x > 709.782712893384)
+    return INFINITY;
+  if (x < -745.1332191019412)
+    return 0.0;
+  const double k = std::rint(x * 0x1.71547652b82fep+0);
+  double r = std::fma(-k, 0x1.62e42ff000000p-1, x);
+  r = std::fma(-k, -0x1.718432a1b0e26p-35, r);
+  static const double c[14] = { 1.0, 1.0, 0.5, 0x1.5555555555555p-3, 0x1.5555555555555p-5, 0x1.1111111111111p-7,
+                                0x1.6c16c16c16c17p-10, 0x1.a01a01a01a01ap-13, 0x1.a01a01a01a01ap-16,
+                                0x1.71de3a556c734p-19, 0x1.27e4fb7789f5cp-22, 0x1.ae64567f544e4p-26,
+                                0x1.1eed8eff8d898p-29, 0x1.6124613a86d09p-33 };
+  double p = c[13];
+  for (int i = 12; i >= 0; i--)
+    p = std::fma(p, r, c[i]);
+  int ki = (int)k;
+  if (ki < -1021) {
+    p = p * pow2i(-600);
+    ki += 600;
+  } else if (ki > 1023) {
+    p = p * 2.0;
+    ki -= 1;
+  }
+  return p * pow2i(ki);
+}
+
+inline double edm_exp(double x)
+{
+  return g_exp_mode ? exp_rn(x) : std::exp(x);
+}
+
 // ---------------------------------------------------------------- stats.cpp
 double seq_sum(const std::vector<double>& v)
 {
@@ -777,7 +827,7 @@ void simplex_prediction(int Mp_i, int t, const Options& opts, const Manifold& M,
   double sumw = 0.0;
   const double theta = opts.thetas[t];
   for (int j = 0; j < k; j++) {
-    w[j] = std::exp(-theta * (dists[j] / minDist));
+    w[j] = edm_exp(-theta * (dists[j] / minDist));
     sumw = sumw + w[j];
   }
   double r = 0.0;
@@ -799,7 +849,7 @@ void smap_prediction(int Mp_i, int t, const Options& opts, const Manifold& M, co
   mean /= (double)k;
   std::vector<double> w(k);
   for (int i = 0; i < k; i++)
-    w[i] = std::exp(-opts.thetas[t] * (dists[i] / mean));
+    w[i] = edm_exp(-opts.thetas[t] * (dists[i] / mean));
   std::vector<double> X((size_t)k * n), y(k);
   for (int i = 0; i < k; i++) {
     X[(size_t)i * n] = w[i];
@@ -1239,6 +1289,16 @@ std::vector<double> to_R_matrix(const std::vector<double>& v, int r, int c, cons
 } // namespace
 
 extern "C" {
+
+void oracle_set_exp_mode(int mode)
+{
+  g_exp_mode = mode;
+}
+
+double oracle_exp(double x)
+{
+  return exp_rn(x);
+}
 
 void oracle_mt_real2(unsigned long long seed, long long count, double* out)
 {

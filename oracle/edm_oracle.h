@@ -141,6 +141,11 @@ int oracle_task_run(const oracle_args* args, oracle_task_io* io);
 /* The usable-row mask run_command computes (src/r.cpp:256-257). */
 int oracle_usable(const oracle_args* args, int maxE, int copredict, unsigned char* usable_out);
 
+/* 0 (default): weights use std::exp like the reference.  1: weights use the
+ * IEEE-only exp formula the GPU library evaluates, for bit-level parity. */
+void oracle_set_exp_mode(int mode);
+double oracle_exp(double x);
+
 /* MT19937-64 stream as the splitter consumes it (getReal2). */
 void oracle_mt_real2(unsigned long long seed, long long count, double* out);
 

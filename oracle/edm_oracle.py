@@ -79,6 +79,9 @@ def load():
         _lib.oracle_task_run.argtypes = [C.POINTER(OracleArgs), C.POINTER(OracleTaskIO)]
         _lib.oracle_usable.argtypes = [C.POINTER(OracleArgs), C.c_int, C.c_int, C.c_void_p]
         _lib.oracle_mt_real2.argtypes = [C.c_ulonglong, C.c_longlong, C.c_void_p]
+        _lib.oracle_set_exp_mode.argtypes = [C.c_int]
+        _lib.oracle_exp.argtypes = [C.c_double]
+        _lib.oracle_exp.restype = C.c_double
     return _lib
 
 
@@ -294,3 +297,12 @@ def mt_real2(seed, count):
     out = np.zeros(count)
     lib.oracle_mt_real2(seed, count, out.ctypes.data)
     return out
+
+
+def set_exp_mode(mode):
+    """0: std::exp (the reference); 1: the GPU library's IEEE-only exp."""
+    load().oracle_set_exp_mode(int(mode))
+
+
+def exp_rn(x):
+    return load().oracle_exp(float(x))

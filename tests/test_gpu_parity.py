@@ -1,0 +1,154 @@
+"""GPU parity: the GB300 library through its C ABI against the CPU oracle.
+
+* every test block of the reference's test-ci.R, run through the GPU, must
+  meet the reference's golden values (1e-4) and agree with the oracle call
+  by call: identical return codes, k ranges and NA patterns; rho, MAE and
+  forecasts within 1e-9 relative (FP64 exact path) -- the oracle computes the
+  same FP64 operations in the same order, differences come from exp() and
+  reduction order only;
+* on explicit masks, neighbour indices and distances are bit-identical.
+"""
+import numpy as np
+import pytest
+
+import ci_cases
+import edm_oracle
+from fedm_loader import fedm, workloads
+
+pytestmark = pytest.mark.gpu
+
+RTOL = 1e-9
+ATOL = 1e-12
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _device_exp():
+    # the oracle evaluates the same IEEE-only exp formula as the device
+    edm_oracle.set_exp_mode(1)
+    yield
+    edm_oracle.set_exp_mode(0)
+
+
+@pytest.fixture(scope="module", params=[fedm.PRECISION_FP64, fedm.PRECISION_MIXED], ids=["fp64", "mixed"])
+def ctx(request):
+    c = fedm.Context(0, precision=request.param)
+    c.precision = request.param
+    yield c
+    c.close()
+
+
+def _close(a, b, what, rtol=RTOL, atol=ATOL):
+    a = np.asarray(a, dtype=float)
+    b = np.asarray(b, dtype=float)
+    assert a.shape == b.shape, (what, a.shape, b.shape)
+    assert np.array_equal(np.isnan(a), np.isnan(b)), (what, "NA pattern differs")
+    m = ~np.isnan(a)
+    assert np.allclose(a[m], b[m], rtol=rtol, atol=atol), (what, np.max(np.abs(a[m] - b[m])) if m.any() else 0)
+
+
+def compare(g, o):
+    assert g["rc"] == o["rc"], (g["rc"], o["rc"], g.get("error"))
+    for key in ("stats", "copredStats"):
+        assert (key in g) == (key in o), key
+        if key in o:
+            for f in ("E", "library", "theta"):
+                assert np.array_equal(g[key][f], o[key][f]), (key, f)
+            _close(g[key]["rho"], o[key]["rho"], key + ".rho")
+            _close(g[key]["mae"], o[key]["mae"], key + ".mae")
+    assert g.get("kMin") == o.get("kMin") and g.get("kMax") == o.get("kMax")
+    for key in ("predictions", "copredictions", "coeffs"):
+        assert (key in g) == (key in o), key
+        if key in o:
+            _close(g[key], o[key], key, rtol=1e-8, atol=1e-10)
+    for key in ("missingdistance", "dtWeight"):
+        assert (key in g) == (key in o)
+        if key in o:
+            assert g[key] == o[key], key
+
+
+@pytest.mark.parametrize("case", ci_cases.CASES, ids=lambda c: c.__name__)
+def test_reference_goldens_on_gpu(ctx, case):
+    def both(t, x, y=None, **kw):
+        g = fedm.edm(t, x, y, ctx=ctx, **kw)
+        o = edm_oracle.oracle_edm(t, x, y, **kw)
+        compare(g, o)
+        return g
+
+    case(both)
+
+
+def _task_pair(ctx, a, lib, pred, E, k, **kw):
+    g = ctx.run_task(a, lib, pred, E, k, **kw)
+    o = edm_oracle.oracle_task(a, lib, pred, E, k, **kw)
+    assert g["n_pred"] == o["n_pred"] and g["n_lib"] == o["n_lib"] and g["e_actual"] == o["e_actual"]
+    assert np.array_equal(g["kused"], o["kused"])
+    assert np.array_equal(g["nn_offsets"], o["nn_offsets"])
+    assert np.array_equal(g["nn_idx"], o["nn_idx"]), "neighbour indices differ"
+    assert np.array_equal(g["nn_dist"].view(np.int64), o["nn_dist"].view(np.int64)), "neighbour distances differ"
+    assert np.array_equal(g["rc"], o["rc"])
+    if ctx.precision == fedm.PRECISION_FP64:
+        # same operations in the same order on both sides: identical bits
+        assert np.array_equal(g["predictions"], o["predictions"]), "forecasts differ"
+        assert np.array_equal(g["coeffs"], o["coeffs"]), "coefficients differ"
+    else:
+        # mixed form: same neighbours; S-map systems solved by LDL^T when well
+        # conditioned (relative error ~ cond * 1e-16), else the same SVD
+        _close(g["predictions"], o["predictions"], "predictions", rtol=1e-7, atol=1e-9)
+        _close(g["coeffs"], o["coeffs"], "coeffs", rtol=1e-6, atol=1e-8)
+    _close(g["stats_rho"], o["stats_rho"], "rho")
+    _close(g["stats_mae"], o["stats_mae"], "mae")
+    return g, o
+
+
+def test_simplex_config_neighbours_bit_exact(ctx):
+    """250/250 split of the coupled logistic map, E = 1..10, k = E+1."""
+    w = workloads.simplex_config()
+    a = edm_oracle.normalise(w["t"], w["x"], E=1)
+    for E in w["Es"]:
+        _task_pair(ctx, a, w["library_rows"], w["prediction_rows"], E, E + 1)
+
+
+@pytest.mark.parametrize("algorithm", ["simplex", "smap"])
+@pytest.mark.parametrize("k", [0, 1, 3, 7, 40, -1, 500])
+def test_random_task_edges(ctx, algorithm, k):
+    """Ties (duplicated values), self matches, k beyond the library, k = all."""
+    rng = np.random.default_rng(11)
+    n = 300
+    x = np.round(rng.normal(size=n), 1)  # many exact ties
+    x[x == 0] = 0.1
+    t = np.arange(1, n + 1, dtype=float)
+    a = edm_oracle.normalise(t, x, E=3, theta=[0.0, 1.0, 3.0], algorithm=algorithm)
+    lib = rng.uniform(size=n) < 0.5
+    pred = np.ones(n, bool)
+    _task_pair(ctx, a, lib, pred, 3, k)
+
+
+def test_empty_library(ctx):
+    t = np.arange(1, 51, dtype=float)
+    x = np.sin(t)
+    a = edm_oracle.normalise(t, x, E=2)
+    lib = np.zeros(50, bool)
+    g, o = _task_pair(ctx, a, lib, np.ones(50, bool), 2, 3)
+    assert np.all(g["kused"] == -(2**31))
+
+
+@pytest.mark.parametrize("distance", [0, 1])
+def test_missing_panels_l1(ctx, distance):
+    rng = np.random.default_rng(5)
+    n = 240
+    t = np.arange(1, n + 1, dtype=float)
+    x = rng.normal(size=n)
+    x[rng.uniform(size=n) < 0.1] = np.nan
+    panel = (t > 120) * 1.0
+    a = edm_oracle.normalise(t, x, panel=panel, E=3, allowMissing=True, panelWeight=0.5)
+    lib = rng.uniform(size=n) < 0.6
+    _task_pair(ctx, a, lib, np.ones(n, bool), 3, 5, distance=distance)
+
+
+def test_force_compute_off(ctx):
+    t = np.arange(1, 81, dtype=float)
+    x = np.cos(0.3 * t)
+    a = edm_oracle.normalise(t, x, E=2, theta=[1.0, 2.0])
+    lib = np.zeros(80, bool)
+    lib[:4] = True
+    _task_pair(ctx, a, lib, np.ones(80, bool), 2, 6, force_compute=False)
