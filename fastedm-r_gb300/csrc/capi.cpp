@@ -163,6 +163,48 @@ int fedm_last_timing(const fedm_ctx* ctx, fedm_timing* out)
   return FEDM_SUCCESS;
 }
 
+int fedm_host_usable(const fedm_args* args, int maxE, int copredict, unsigned char* out)
+{
+  if (!args || !out)
+    return FEDM_UNKNOWN_ERROR;
+  return guarded(nullptr, [&] {
+    fedm::host_usable(*args, maxE, copredict, out);
+    return FEDM_SUCCESS;
+  });
+}
+
+int fedm_host_manifold(const fedm_args* args, int E, int copredict, double* out, int* e_actual)
+{
+  if (!args || !e_actual)
+    return FEDM_UNKNOWN_ERROR;
+  return guarded(nullptr, [&] {
+    *e_actual = fedm::host_manifold(*args, E, copredict, out);
+    return FEDM_SUCCESS;
+  });
+}
+
+int fedm_host_mt_real2(unsigned long long seed, long long count, double* out)
+{
+  if (!out || count < 0)
+    return FEDM_UNKNOWN_ERROR;
+  fedm::Mt64 m;
+  m.init(seed);
+  for (long long i = 0; i < count; i++)
+    out[i] = m.real2();
+  return FEDM_SUCCESS;
+}
+
+int fedm_host_plan(const fedm_args* args, int max_tasks, int* n_tasks, int* task_E, int* task_k, int* task_library,
+                   int* task_copredict, unsigned char* lib_masks, unsigned char* pred_masks)
+{
+  if (!args || !n_tasks)
+    return FEDM_UNKNOWN_ERROR;
+  return guarded(nullptr, [&] {
+    *n_tasks = fedm::host_plan(*args, max_tasks, task_E, task_k, task_library, task_copredict, lib_masks, pred_masks);
+    return FEDM_SUCCESS;
+  });
+}
+
 int fedm_measure_peak(fedm_ctx* ctx, int kind, double* tflops)
 {
   if (!ctx || !tflops || kind < 0 || kind > 2)

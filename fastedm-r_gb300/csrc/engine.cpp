@@ -374,6 +374,7 @@ void run_group(Context& ctx, const Options& o, const std::vector<Task>& tasks, c
     d.pred_off = it2->second;
     d.n_pred = (int)Pl->size();
     d.k = t.k;
+    d.k_req = t.k;
     d.task = j;
     d.save_coeffs = t.save_coeffs || job.detail;
     d.all_mode = (t.k < 0 || t.k >= d.n_lib) ? 1 : 0;
@@ -827,10 +828,10 @@ CommandResult run_command(Context& ctx, const fedm_args& a)
   std::vector<uint8_t> cousable;
   if (copredict_mode)
     cousable = gen.usable(maxE, true, threads);
+  RowTables rt = build_row_tables(gen);
   TaskPlan plan = configure_tasks(gen, o, P.Es, libraries, a.k, a.num_reps, a.crossfold, P.explore, a.full,
                                   a.shuffle, a.save_predictions, a.save_copredictions, a.save_smap_coeffs,
-                                  copredict_mode, usable, cousable, a.seed);
-  RowTables rt = build_row_tables(gen);
+                                  copredict_mode, usable, cousable, a.seed, &rt.lib_target, threads);
   DevRows drows = upload_rows(ctx, gen, rt, o);
 
   // row lists per mask (shared by every task that uses the mask)
@@ -838,7 +839,10 @@ CommandResult run_command(Context& ctx, const fedm_args& a)
   std::vector<uint8_t> lib_done(plan.masks.size(), 0), pred_done(plan.masks.size(), 0);
   for (const Task& t : plan.tasks) {
     if (!lib_done[t.lib_mask]) {
-      lib_lists[t.lib_mask] = lib_rows_of(plan.masks[t.lib_mask], rt);
+      if (!plan.lists_ready.empty() && plan.lists_ready[t.lib_mask])
+        lib_lists[t.lib_mask].swap(plan.lib_lists[t.lib_mask]);
+      else
+        lib_lists[t.lib_mask] = lib_rows_of(plan.masks[t.lib_mask], rt);
       lib_done[t.lib_mask] = 1;
     }
     if (!pred_done[t.pred_mask]) {
@@ -942,6 +946,68 @@ CommandResult run_command(Context& ctx, const fedm_args& a)
   ctx.timing.predictions = npred;
   ctx.timing.distance_pairs = pairs;
   return R;
+}
+
+// ------------------------------------------------------ host-only helpers
+void host_usable(const fedm_args& a, int maxE, int copredict, unsigned char* out)
+{
+  Prepared P;
+  prepare(a, P);
+  auto u = P.gen.usable(maxE, copredict != 0, host_threads(a));
+  std::copy(u.begin(), u.end(), out);
+}
+
+int host_manifold(const fedm_args& a, int E, int copredict, double* out)
+{
+  Prepared P;
+  prepare(a, P);
+  RowTables rt = build_row_tables(P.gen);
+  if (out) {
+    auto F = build_manifold(P.gen, rt, E, copredict != 0, host_threads(a));
+    std::copy(F.begin(), F.end(), out);
+  }
+  return P.gen.E_actual(E);
+}
+
+int host_plan(const fedm_args& a, int max_tasks, int* task_E, int* task_k, int* task_library, int* task_copredict,
+              unsigned char* lib_masks, unsigned char* pred_masks)
+{
+  Prepared P;
+  prepare(a, P);
+  const Generator& gen = P.gen;
+  const int threads = host_threads(a);
+  std::vector<uint8_t> usable = gen.usable(P.Es.back(), false, threads);
+  const int numUsable = (int)std::count(usable.begin(), usable.end(), (uint8_t)1);
+  std::vector<int> libraries = P.libraries;
+  if (!P.explore && libraries.empty())
+    libraries = { numUsable };
+  const bool co = !gen.co_x.empty();
+  std::vector<uint8_t> cousable;
+  if (co)
+    cousable = gen.usable(P.Es.back(), true, threads);
+  // every row counts as having a target here, so the parallel splitter's
+  // row lists are exactly the membership masks
+  std::vector<double> all_targets(gen.n, 0.0);
+  TaskPlan plan = configure_tasks(gen, P.opts, P.Es, libraries, a.k, a.num_reps, a.crossfold, P.explore, a.full,
+                                  a.shuffle, a.save_predictions, a.save_copredictions, a.save_smap_coeffs, co,
+                                  usable, cousable, a.seed, &all_targets, threads);
+  for (int i = 0; i < (int)plan.tasks.size() && i < max_tasks; i++) {
+    const Task& t = plan.tasks[i];
+    task_E[i] = t.E;
+    task_k[i] = t.k;
+    task_library[i] = t.library;
+    task_copredict[i] = t.copredict;
+    unsigned char* lm = lib_masks + (size_t)i * a.n;
+    if (!plan.lists_ready.empty() && plan.lists_ready[t.lib_mask]) {
+      std::fill(lm, lm + a.n, 0);
+      for (int r : plan.lib_lists[t.lib_mask])
+        lm[r] = 1;
+    } else {
+      std::copy(plan.masks[t.lib_mask].begin(), plan.masks[t.lib_mask].end(), lm);
+    }
+    std::copy(plan.masks[t.pred_mask].begin(), plan.masks[t.pred_mask].end(), pred_masks + (size_t)i * a.n);
+  }
+  return (int)plan.tasks.size();
 }
 
 // ------------------------------------------------------ single-task seam

@@ -54,6 +54,12 @@ struct CommandResult
 };
 
 CommandResult run_command(Context& ctx, const fedm_args& a);
+
+// Host-only pieces of the path (no device involved).
+void host_usable(const fedm_args& a, int maxE, int copredict, unsigned char* out);
+int host_manifold(const fedm_args& a, int E, int copredict, double* out);
+int host_plan(const fedm_args& a, int max_tasks, int* task_E, int* task_k, int* task_library, int* task_copredict,
+              unsigned char* lib_masks, unsigned char* pred_masks);
 int run_task(Context& ctx, const fedm_args& a, fedm_task_io& io);
 
 } // namespace fedm

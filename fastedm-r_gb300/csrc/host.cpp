@@ -2,6 +2,7 @@
 #include "host.h"
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <numeric>
 #include <thread>
@@ -286,15 +287,8 @@ std::vector<double> build_manifold(const Generator& g, const RowTables& rt, int 
   const int Ea = g.E_actual(E);
   std::vector<double> F((size_t)g.n * Ea);
   parallel_rows(g.n, threads, [&](int b, int e) {
-    for (int i = b; i < e; i++) {
-      if (g.obs[i] == MISSING_I && g.t[i] == MISSING_D) {
-        // rows without a time never enter a manifold; keep them defined
-        for (int j = 0; j < Ea; j++)
-          F[(size_t)i * Ea + j] = MISSING_D;
-        continue;
-      }
+    for (int i = b; i < e; i++)
       g.fill_row(i, E, use_co_x, g.dt_weight, rt.target_row[i], &F[(size_t)i * Ea]);
-    }
   });
   return F;
 }
@@ -321,6 +315,18 @@ void Mt64::refill()
   s[311] = s[155] ^ mix(s[311], s[0]);
   left = 312;
   next = 0;
+}
+
+void Mt64::skip(long long count)
+{
+  while (count > 0) {
+    if (left == 0)
+      refill();
+    const long long take = count < left ? count : left;
+    left -= (int)take;
+    next += (int)take;
+    count -= take;
+  }
 }
 
 double Mt64::real2()
@@ -385,6 +391,14 @@ int Splitter::next_library_size(int iter) const
     return c;
   }
   return full_ ? num_usable_ : num_usable_ / 2;
+}
+
+void Splitter::defer_fixed_size(Mt64& snapshot)
+{
+  // the state a shuffled fixed_size_library split starts from; the stream is
+  // then advanced past its num_usable draws
+  snapshot = rng_;
+  rng_.skip(num_usable_);
 }
 
 void Splitter::update(int library, int iter)
@@ -462,18 +476,28 @@ TaskPlan configure_tasks(const Generator& g, const Options& opts, const std::vec
                          const std::vector<int>& libraries, int k, int num_reps, int crossfold, bool explore,
                          bool full, bool shuffle, bool save_predictions, bool save_copredictions,
                          bool save_smap_coeffs, bool copredict_mode, const std::vector<uint8_t>& usable,
-                         const std::vector<uint8_t>& cousable, int seed)
+                         const std::vector<uint8_t>& cousable, int seed, const std::vector<double>* lib_target,
+                         int threads)
 {
   TaskPlan plan;
   Splitter sp(explore, full, shuffle, crossfold, usable, seed);
   const int num_libraries = explore ? 1 : (int)libraries.size();
   const int num_iters = num_reps > crossfold ? num_reps : crossfold;
   const int maxE = Es.back();
+  const bool deferred = lib_target != nullptr && !explore && shuffle;
+  struct Deferred
+  {
+    Mt64 state;
+    int library;
+    int mask;
+  };
+  std::vector<Deferred> splits;
   int cousable_mask = -1;
   if (copredict_mode) {
     plan.masks.push_back(cousable);
     cousable_mask = 0;
   }
+  int usable_mask = -1;
   bool new_split = true;
   int library_size = 0, lib_mask = -1, pred_mask = -1;
   for (int iter = 1; iter <= num_iters; iter++) {
@@ -501,15 +525,30 @@ TaskPlan configure_tasks(const Generator& g, const Options& opts, const std::vec
         t.save_prediction = save_predictions && last_iter && last;
         t.save_coeffs = save_smap_coeffs;
         if (new_split) {
-          sp.update(library, iter);
           new_split = false;
-          plan.masks.push_back(sp.lib());
-          lib_mask = (int)plan.masks.size() - 1;
-          // CCM prediction sets are all usable rows: reuse one mask
-          if (!explore && pred_mask >= 0 && plan.masks[pred_mask] == sp.pred()) {
+          if (deferred) {
+            // src/library_prediction_split.h:231-270 (shuffle branch), run
+            // later from a snapshot of the stream
+            Deferred d;
+            sp.defer_fixed_size(d.state);
+            d.library = library;
+            plan.masks.emplace_back();
+            d.mask = lib_mask = (int)plan.masks.size() - 1;
+            splits.push_back(d);
+            if (usable_mask < 0) {
+              plan.masks.push_back(usable);
+              usable_mask = (int)plan.masks.size() - 1;
+            }
+            pred_mask = usable_mask;
           } else {
-            plan.masks.push_back(sp.pred());
-            pred_mask = (int)plan.masks.size() - 1;
+            sp.update(library, iter);
+            plan.masks.push_back(sp.lib());
+            lib_mask = (int)plan.masks.size() - 1;
+            // cross-mapping prediction sets are all usable rows: reuse one mask
+            if (!(!explore && pred_mask >= 0 && plan.masks[pred_mask] == sp.pred())) {
+              plan.masks.push_back(sp.pred());
+              pred_mask = (int)plan.masks.size() - 1;
+            }
           }
         }
         t.library = library;
@@ -527,6 +566,47 @@ TaskPlan configure_tasks(const Generator& g, const Options& opts, const std::vec
         }
       }
     }
+  }
+  if (!splits.empty()) {
+    plan.lib_lists.resize(plan.masks.size());
+    plan.lists_ready.assign(plan.masks.size(), 0);
+    std::vector<int> urows;
+    for (int i = 0; i < (int)usable.size(); i++)
+      if (usable[i])
+        urows.push_back(i);
+    const int nu = (int)urows.size();
+    std::atomic<size_t> next{ 0 };
+    auto worker = [&] {
+      std::vector<double> u(nu), c(nu);
+      for (;;) {
+        const size_t j = next.fetch_add(1);
+        if (j >= splits.size())
+          break;
+        Deferred& d = splits[j];
+        for (int o = 0; o < nu; o++)
+          u[o] = d.state.real2();
+        double cutoff = 1.0;
+        if (d.library < nu) {
+          c = u;
+          std::nth_element(c.begin(), c.begin() + d.library, c.end());
+          cutoff = c[d.library];
+        }
+        std::vector<int>& out = plan.lib_lists[d.mask];
+        out.clear();
+        out.reserve(std::min(d.library, nu));
+        for (int o = 0; o < nu; o++)
+          if (u[o] < cutoff && (*lib_target)[urows[o]] != MISSING_D)
+            out.push_back(urows[o]);
+        plan.lists_ready[d.mask] = 1;
+      }
+    };
+    const int nt = std::max(1, std::min<int>(threads, (int)splits.size()));
+    std::vector<std::thread> pool;
+    for (int w = 1; w < nt; w++)
+      pool.emplace_back(worker);
+    worker();
+    for (auto& th : pool)
+      th.join();
   }
   return plan;
 }

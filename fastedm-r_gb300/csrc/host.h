@@ -96,6 +96,10 @@ struct Mt64
   void init(uint64_t seed);
   void refill();
   double real2();
+  // Advances the stream by `count` draws without producing them (refills
+  // only); the next real2() returns the value it would have returned after
+  // `count` calls.
+  void skip(long long count);
 };
 
 // src/library_prediction_split.h:17-286
@@ -105,6 +109,8 @@ public:
   Splitter(bool explore, bool full, bool shuffle, int crossfold, const std::vector<uint8_t>& usable, int seed);
   int next_library_size(int iter) const;
   void update(int library, int iter);
+  void defer_fixed_size(Mt64& snapshot);
+  int num_usable() const { return num_usable_; }
   const std::vector<uint8_t>& lib() const { return lib_; }
   const std::vector<uint8_t>& pred() const { return pred_; }
 
@@ -152,14 +158,24 @@ struct TaskPlan
 {
   std::vector<Task> tasks;
   std::vector<std::vector<uint8_t>> masks;
+  // Library row lists (mask rows whose target is observed) computed by the
+  // parallel CCM splitter; lists_ready[id] marks the mask ids they replace.
+  std::vector<std::vector<int>> lib_lists;
+  std::vector<uint8_t> lists_ready;
 };
 
 // src/edm.cpp:90-212 configure_tasks
+// With `lib_target` given, the shuffled fixed-size library splits of cross
+// mapping (src/library_prediction_split.h:231-270) are produced as row lists
+// by a parallel pass: one sequential sweep advances the MT19937-64 state and
+// snapshots it at each split, then threads regenerate each split's uniforms,
+// select the cutoff and emit the rows.  Without it every split is a mask.
 TaskPlan configure_tasks(const Generator& g, const Options& opts, const std::vector<int>& Es,
                          const std::vector<int>& libraries, int k, int num_reps, int crossfold, bool explore,
                          bool full, bool shuffle, bool save_predictions, bool save_copredictions,
                          bool save_smap_coeffs, bool copredict_mode, const std::vector<uint8_t>& usable,
-                         const std::vector<uint8_t>& cousable, int seed);
+                         const std::vector<uint8_t>& cousable, int seed,
+                         const std::vector<double>* lib_target = nullptr, int threads = 1);
 
 // Cleans one input vector: every non-normal value becomes MISSING_D
 // (src/r.cpp:64-71).

@@ -23,7 +23,8 @@ struct DevTask
   long long point_base;  // first global point id of this task
   int lib_off, n_lib;    // slice of lib_rows
   int pred_off, n_pred;  // slice of pred_rows
-  int k;                 // neighbours requested (>0) or -1 (all valid)
+  int k;                 // neighbour slots the list kernels keep
+  int k_req;             // k as requested (kAdj): >0, 0 or -1 (all valid)
   int task;              // index of the task's rc / k / stats slots
   int save_coeffs;
   int all_mode;          // k < 0 or k >= n_lib: every valid neighbour, library order

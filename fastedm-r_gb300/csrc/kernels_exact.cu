@@ -181,8 +181,9 @@ __global__ void knn_exact_kernel(GroupParams g, ChunkBuffers c, int warps_per_bl
         __syncwarp();
       }
     }
-    int status = PT_OK, keff = k;
-    if (k > numValid) {
+    // src/edm.cpp:595-617 on the requested k (k_req = -1: all valid)
+    int status = PT_OK, keff = T.k_req < 0 ? numValid : T.k_req;
+    if (T.k_req > numValid) {
       if (g.force_compute)
         keff = numValid;
       else
@@ -253,6 +254,8 @@ __global__ void simplex_nn_kernel(GroupParams g, ChunkBuffers c)
     sumw = sumw + exp_rn(-theta * (dists[j] / minDist));
   double r = 0.0;
   for (int j = 0; j < ke; j++) {
+    // the weight is recomputed rather than stored: identical bits, no
+    // per-thread array of k doubles
     const double w = exp_rn(-theta * (dists[j] / minDist));
     r = r + g.lib_target[g.lib_rows[T.lib_off + inds[j]]] * (w / sumw);
   }
@@ -279,6 +282,7 @@ __device__ __forceinline__ void smap_finish(const GroupParams& g, const DevTask&
 }
 
 constexpr int SMALL_N = 8;
+constexpr int KW_LOCAL = 32;  // weights cached per thread (larger k recomputes)
 
 // src/edm.cpp:737-814 for a finite neighbour list, one thread per
 // (point, theta).  X^T X and X^T y are summed over the neighbours in order.
@@ -289,7 +293,7 @@ __global__ void smap_nn_kernel(GroupParams g, ChunkBuffers c, long long slab)
   const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   const int n = g.Ea + 1;
   double lW[SMALL_N * SMALL_N], lU[SMALL_N * SMALL_N], lV[SMALL_N * SMALL_N], lsv[SMALL_N], ltmp[SMALL_N],
-    lb[SMALL_N], lx[SMALL_N];
+    lb[SMALL_N], lx[SMALL_N], wbuf[KW_LOCAL];
   double *W = lW, *U = lU, *V = lV, *sv = lsv, *tmp = ltmp, *bv = lb, *xs = lx;
   if (n > SMALL_N) {
     double* s = c.scratch + tid * slab;
@@ -321,11 +325,16 @@ __global__ void smap_nn_kernel(GroupParams g, ChunkBuffers c, long long slab)
       mean += dists[j];
     mean /= (double)ke;
     const double theta = g.thetas[t];
+    // weights once per (point, theta) (src/edm.cpp:744-745); the X entries
+    // w * M(row, j) are re-formed where used, which gives the same bits
+    for (int i = 0; i < ke && i < KW_LOCAL; i++)
+      wbuf[i] = exp_rn(-theta * (dists[i] / mean));
+    auto weight = [&](int i) { return i < KW_LOCAL ? wbuf[i] : exp_rn(-theta * (dists[i] / mean)); };
     for (int a = 0; a < n; a++) {
       for (int b = a; b < n; b++) {
         double s = 0;
         for (int i = 0; i < ke; i++) {
-          const double w = exp_rn(-theta * (dists[i] / mean));
+          const double w = weight(i);
           const int row = g.lib_rows[T.lib_off + inds[i]];
           const double xa = a == 0 ? w : w * g.F[(size_t)row * g.Ea + a - 1];
           const double xb = b == 0 ? w : w * g.F[(size_t)row * g.Ea + b - 1];
@@ -336,7 +345,7 @@ __global__ void smap_nn_kernel(GroupParams g, ChunkBuffers c, long long slab)
       }
       double s = 0;
       for (int i = 0; i < ke; i++) {
-        const double w = exp_rn(-theta * (dists[i] / mean));
+        const double w = weight(i);
         const int row = g.lib_rows[T.lib_off + inds[i]];
         const double xa = a == 0 ? w : w * g.F[(size_t)row * g.Ea + a - 1];
         s += xa * (w * g.lib_target[row]);

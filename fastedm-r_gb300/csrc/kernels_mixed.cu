@@ -83,11 +83,25 @@ __device__ __forceinline__ double fp64_sq(const GroupParams& g, int row, const d
   return s;
 }
 
-template<int EA, int C>
-__device__ void finalize_point(const GroupParams& g, const MixedRun& m, const DevTask& T, long long p, int prow,
-                               const float (&D)[C], const int (&I)[C], int z, const int (&zi)[ZCAP])
+// Candidates of one point, handed to the out-of-line FP64 stage.
+template<int C>
+struct Cand
 {
-  const int k = T.k;
+  float D[C];
+  int I[C];
+  int z;
+  int zi[ZCAP];
+};
+
+template<int EA, int C>
+__device__ __noinline__ void finalize_point(const GroupParams& g, const MixedRun& m, const DevTask& T, long long p,
+                                            int prow, const Cand<C>& cand)
+{
+  const float(&D)[C] = cand.D;
+  const int(&I)[C] = cand.I;
+  const int z = cand.z;
+  const int(&zi)[ZCAP] = cand.zi;
+  const int k = T.k;  // list capacity (the requested k, or the library size for k = all)
   int lc = 0;
 #pragma unroll
   for (int j = 0; j < C; j++)
@@ -138,7 +152,8 @@ __device__ void finalize_point(const GroupParams& g, const MixedRun& m, const De
     }
   }
   const int numValid = T.n_lib - z + zvalid;
-  const int keff = k < numValid ? k : numValid;
+  const int kr = T.k_req < 0 ? numValid : T.k_req;
+  const int keff = kr < numValid ? kr : numValid;
   if (keff <= 0) {
     // src/edm.cpp:602-606: no forecast; rc(0) SUCCESS, later thetas untouched
     if (g.n_thetas > 1)
@@ -194,16 +209,22 @@ __device__ void finalize_point(const GroupParams& g, const MixedRun& m, const De
     double minD = cd[0];
     for (int j = 1; j < keff; j++)
       minD = cd[j] < minD ? cd[j] : minD;
+    double rel[C + ZCAP], tg[C + ZCAP];
+    for (int j = 0; j < keff; j++) {
+      rel[j] = dvd(cd[j], minD);
+      tg[j] = g.lib_target[rows[j]];
+    }
     for (int t = 0; t < g.n_thetas; t++) {
       const double theta = g.thetas[t];
+      double w[C + ZCAP];
       double sumw = 0.0;
-      for (int j = 0; j < keff; j++)
-        sumw = add(sumw, exp_rn(mul(-theta, dvd(cd[j], minD))));
-      double r = 0.0;
       for (int j = 0; j < keff; j++) {
-        const double w = exp_rn(mul(-theta, dvd(cd[j], minD)));
-        r = add(r, mul(g.lib_target[rows[j]], dvd(w, sumw)));
+        w[j] = exp_rn(mul(-theta, rel[j]));
+        sumw = add(sumw, w[j]);
       }
+      double r = 0.0;
+      for (int j = 0; j < keff; j++)
+        r = add(r, mul(tg[j], dvd(w[j], sumw)));
       g.pred[(size_t)t * g.total_points + p] = r;
     }
     return;
@@ -215,36 +236,45 @@ __device__ void finalize_point(const GroupParams& g, const MixedRun& m, const De
   for (int j = 0; j < keff; j++)
     mean = add(mean, cd[j]);
   mean = dvd(mean, (double)keff);
+  double rel[C + ZCAP];
+  for (int i = 0; i < keff; i++)
+    rel[i] = dvd(cd[i], mean);
   for (int t = 0; t < g.n_thetas; t++) {
     const double theta = g.thetas[t];
     double A[n * n], bv[n], xs[n];
+    // X = [w, w*M(row, .)] and w*target, formed once (same bits as the
+    // reference's X_ls_cj and y_ls, src/edm.cpp:749-772)
+    double X[C + ZCAP][n], yl[C + ZCAP];
+    for (int i = 0; i < keff; i++) {
+      const double w = exp_rn(mul(-theta, rel[i]));
+      X[i][0] = w;
+#pragma unroll
+      for (int j = 1; j < n; j++)
+        X[i][j] = mul(w, g.F[(size_t)rows[i] * EA + j - 1]);
+      yl[i] = mul(w, g.lib_target[rows[i]]);
+    }
+#pragma unroll
     for (int a = 0; a < n; a++) {
+#pragma unroll
       for (int b = a; b < n; b++) {
         double s = 0;
-        for (int i = 0; i < keff; i++) {
-          const double w = exp_rn(mul(-theta, dvd(cd[i], mean)));
-          const double xa = a == 0 ? w : mul(w, g.F[(size_t)rows[i] * EA + a - 1]);
-          const double xb = b == 0 ? w : mul(w, g.F[(size_t)rows[i] * EA + b - 1]);
-          s = add(s, mul(xa, xb));
-        }
+        for (int i = 0; i < keff; i++)
+          s = add(s, mul(X[i][a], X[i][b]));
         A[a * n + b] = s;
         A[b * n + a] = s;
       }
       double s = 0;
-      for (int i = 0; i < keff; i++) {
-        const double w = exp_rn(mul(-theta, dvd(cd[i], mean)));
-        const double xa = a == 0 ? w : mul(w, g.F[(size_t)rows[i] * EA + a - 1]);
-        s = add(s, mul(xa, mul(w, g.lib_target[rows[i]])));
-      }
+      for (int i = 0; i < keff; i++)
+        s = add(s, mul(X[i][a], yl[i]));
       bv[a] = s;
     }
-    double L[n * n];
-    for (int i = 0; i < n * n; i++)
-      L[i] = A[i];
-    if (!ldlt_solve(L, bv, xs, n, 1e-7)) {
-      double U[n * n], V[n * n], sv[n], tmp[n];
-      svd_solve(A, U, V, sv, tmp, bv, xs, n);
-    }
+    // The same JacobiSVD restatement as the FP64 form: S-map normal
+    // equations on low-dimensional attractors are routinely ill-conditioned
+    // (cond 1e11..1e15), and the reference's 5*eps*sigma_max truncation then
+    // decides forecasts at the rounding level, so only the identical
+    // operation sequence keeps |delta rho| at zero.
+    double U[n * n], V[n * n], sv[n], tmp[n];
+    svd_solve(A, U, V, sv, tmp, bv, xs, n);
     double r = xs[0];
     for (int j = 0; j < EA; j++)
       r = add(r, mul(y[j], xs[j + 1]));
@@ -255,11 +285,28 @@ __device__ void finalize_point(const GroupParams& g, const MixedRun& m, const De
   }
 }
 
+// One candidate value for one point: FP32 zeros go to the zero list, other
+// values below the C-th kept one are inserted in (value, index) order.
+template<int C>
+__device__ __forceinline__ void offer(float (&D)[C], int (&I)[C], int& z, int (&zi)[ZCAP], float v, int li)
+{
+  if (v < D[C - 1]) {
+    if (v == 0.f) {
+      if (z < ZCAP)
+        zi[z] = li;
+      z++;
+    } else {
+      topc_insert<C>(D, I, v, li);
+    }
+  }
+}
+
 template<int EA, int C>
 __global__ void __launch_bounds__(TPB, 2) knn_mixed_kernel(GroupParams g, MixedRun m)
 {
-  constexpr int S = EA <= 4 ? 4 : 8;
-  __shared__ __align__(16) float tile[TILE * S];
+  constexpr int S = EA <= 4 ? 4 : 8;  // row stride of the float manifold
+  // library rows staged as interleaved pairs: tile[pair][dim] = (row 2i, row 2i+1)
+  __shared__ __align__(16) float2 tile[(TILE / 2) * EA];
   __shared__ int s_item;
   const int tid = threadIdx.x;
   for (;;) {
@@ -276,10 +323,16 @@ __global__ void __launch_bounds__(TPB, 2) knn_mixed_kernel(GroupParams g, MixedR
     const bool a0 = pi0 < T.n_pred, a1 = pi1 < T.n_pred;
     const int prow0 = a0 ? g.pred_rows[T.pred_off + pi0] : 0;
     const int prow1 = a1 ? g.pred_rows[T.pred_off + pi1] : 0;
-    float2 ny[EA];
+    // negated prediction coordinates, duplicated in both halves; an idle slot
+    // sits at 1e30 so its squared distances overflow to +inf and never enter
+    float2 na[EA], nb[EA];
 #pragma unroll
-    for (int j = 0; j < EA; j++)
-      ny[j] = make_float2(a0 ? -m.Fp32[(size_t)prow0 * S + j] : -1e30f, a1 ? -m.Fp32[(size_t)prow1 * S + j] : -1e30f);
+    for (int j = 0; j < EA; j++) {
+      const float va = a0 ? -m.Fp32[(size_t)prow0 * S + j] : -1e30f;
+      const float vb = a1 ? -m.Fp32[(size_t)prow1 * S + j] : -1e30f;
+      na[j] = make_float2(va, va);
+      nb[j] = make_float2(vb, vb);
+    }
     float D0[C], D1[C];
     int I0[C], I1[C];
 #pragma unroll
@@ -294,53 +347,73 @@ __global__ void __launch_bounds__(TPB, 2) knn_mixed_kernel(GroupParams g, MixedR
       zi0[j] = zi1[j] = -1;
     for (int t0 = 0; t0 < T.n_lib; t0 += TILE) {
       const int cnt = min(TILE, T.n_lib - t0);
+      const int npairs = (cnt + 1) >> 1;
       __syncthreads();
-      for (int i = tid; i < cnt; i += TPB) {
-        const int row = g.lib_rows[T.lib_off + t0 + i];
-        const float4* src = reinterpret_cast<const float4*>(m.F32 + (size_t)row * S);
-        float4* dst = reinterpret_cast<float4*>(tile + i * S);
-        dst[0] = src[0];
-        if (S == 8)
-          dst[1] = src[1];
+      for (int i = tid; i < 2 * npairs; i += TPB) {
+        float* dst = reinterpret_cast<float*>(tile + (i >> 1) * EA) + (i & 1);
+        if (i < cnt) {
+          const float* src = m.F32 + (size_t)g.lib_rows[T.lib_off + t0 + i] * S;
+#pragma unroll
+          for (int j = 0; j < EA; j++)
+            dst[2 * j] = src[j];
+        } else {
+#pragma unroll
+          for (int j = 0; j < EA; j++)
+            dst[2 * j] = 1e30f;  // padding row: never a candidate
+        }
       }
       __syncthreads();
 #pragma unroll 2
-      for (int i = 0; i < cnt; i++) {
-        const float* xr = tile + i * S;
-        float2 df = __fadd2_rn(make_float2(xr[0], xr[0]), ny[0]);
-        float2 acc = __fmul2_rn(df, df);
+      for (int ip = 0; ip < npairs; ip++) {
+        const float2* xr = tile + ip * EA;
+        float2 x = xr[0];
+        float2 da = __fadd2_rn(x, na[0]);
+        float2 db = __fadd2_rn(x, nb[0]);
+        float2 sa = __fmul2_rn(da, da);
+        float2 sb = __fmul2_rn(db, db);
 #pragma unroll
         for (int j = 1; j < EA; j++) {
-          df = __fadd2_rn(make_float2(xr[j], xr[j]), ny[j]);
-          acc = __ffma2_rn(df, df, acc);
+          x = xr[j];
+          da = __fadd2_rn(x, na[j]);
+          db = __fadd2_rn(x, nb[j]);
+          sa = __ffma2_rn(da, da, sa);
+          sb = __ffma2_rn(db, db, sb);
         }
-        if (acc.x < D0[C - 1] || acc.y < D1[C - 1]) {
-          const int li = t0 + i;
-          if (acc.x < D0[C - 1]) {
-            if (acc.x == 0.f) {
-              if (z0 < ZCAP)
-                zi0[z0] = li;
-              z0++;
-            } else {
-              topc_insert<C>(D0, I0, acc.x, li);
-            }
-          }
-          if (acc.y < D1[C - 1]) {
-            if (acc.y == 0.f) {
-              if (z1 < ZCAP)
-                zi1[z1] = li;
-              z1++;
-            } else {
-              topc_insert<C>(D1, I1, acc.y, li);
-            }
-          }
+        if (fminf(sa.x, sa.y) < D0[C - 1] || fminf(sb.x, sb.y) < D1[C - 1]) {
+          const int li = t0 + 2 * ip;
+          offer<C>(D0, I0, z0, zi0, sa.x, li);
+          offer<C>(D0, I0, z0, zi0, sa.y, li + 1);
+          offer<C>(D1, I1, z1, zi1, sb.x, li);
+          offer<C>(D1, I1, z1, zi1, sb.y, li + 1);
         }
       }
     }
-    if (a0)
-      finalize_point<EA, C>(g, m, T, T.point_base + pi0, prow0, D0, I0, z0, zi0);
-    if (a1)
-      finalize_point<EA, C>(g, m, T, T.point_base + pi1, prow1, D1, I1, z1, zi1);
+    if (a0) {
+      Cand<C> c;
+#pragma unroll
+      for (int j = 0; j < C; j++) {
+        c.D[j] = D0[j];
+        c.I[j] = I0[j];
+      }
+      c.z = z0;
+#pragma unroll
+      for (int j = 0; j < ZCAP; j++)
+        c.zi[j] = zi0[j];
+      finalize_point<EA, C>(g, m, T, T.point_base + pi0, prow0, c);
+    }
+    if (a1) {
+      Cand<C> c;
+#pragma unroll
+      for (int j = 0; j < C; j++) {
+        c.D[j] = D1[j];
+        c.I[j] = I1[j];
+      }
+      c.z = z1;
+#pragma unroll
+      for (int j = 0; j < ZCAP; j++)
+        c.zi[j] = zi1[j];
+      finalize_point<EA, C>(g, m, T, T.point_base + pi1, prow1, c);
+    }
   }
 }
 

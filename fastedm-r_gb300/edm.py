@@ -74,6 +74,7 @@ class Timing(C.Structure):
 EXPORTS = [
     "fedm_create", "fedm_destroy", "fedm_last_error", "fedm_set_precision", "fedm_set_keep_going",
     "fedm_run_command", "fedm_free_result", "fedm_run_task", "fedm_last_timing", "fedm_measure_peak",
+    "fedm_host_usable", "fedm_host_manifold", "fedm_host_mt_real2", "fedm_host_plan",
 ]
 
 _lib = None
@@ -96,6 +97,10 @@ def load():
         lib.fedm_run_task.argtypes = [C.c_void_p, C.POINTER(Args), C.POINTER(TaskIO)]
         lib.fedm_last_timing.argtypes = [C.c_void_p, C.POINTER(Timing)]
         lib.fedm_measure_peak.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_double)]
+        lib.fedm_host_usable.argtypes = [C.POINTER(Args), C.c_int, C.c_int, C.c_void_p]
+        lib.fedm_host_manifold.argtypes = [C.POINTER(Args), C.c_int, C.c_int, C.c_void_p, C.POINTER(C.c_int)]
+        lib.fedm_host_mt_real2.argtypes = [C.c_ulonglong, C.c_longlong, C.c_void_p]
+        lib.fedm_host_plan.argtypes = [C.POINTER(Args), C.c_int, C.POINTER(C.c_int)] + [C.c_void_p] * 6
         _lib = lib
     return _lib
 
@@ -335,3 +340,48 @@ def edm(t, x, y=None, ctx=None, **kw):
     """The reference's R edm(), on the GPU."""
     ctx = ctx or default_context()
     return ctx.run_command(normalise(t, x, y, **kw))
+
+
+# ---------------------------------------------------------------- host side
+def host_usable(a, maxE, copredict=False):
+    lib = load()
+    keep = []
+    s = make_args(a, keep)
+    u = np.zeros(a["n"], np.uint8)
+    if lib.fedm_host_usable(C.byref(s), maxE, int(copredict), u.ctypes.data) != 0:
+        raise RuntimeError("fedm_host_usable failed")
+    return u.astype(bool)
+
+
+def host_manifold(a, E, copredict=False):
+    """Manifold rows of every observation, [n x E_actual]."""
+    lib = load()
+    keep = []
+    s = make_args(a, keep)
+    ea = C.c_int()
+    lib.fedm_host_manifold(C.byref(s), E, int(copredict), None, C.byref(ea))
+    out = np.zeros((a["n"], ea.value))
+    if lib.fedm_host_manifold(C.byref(s), E, int(copredict), out.ctypes.data, C.byref(ea)) != 0:
+        raise RuntimeError("fedm_host_manifold failed")
+    return out
+
+
+def host_mt_real2(seed, count):
+    out = np.zeros(count)
+    load().fedm_host_mt_real2(seed, count, out.ctypes.data)
+    return out
+
+
+def host_plan(a):
+    lib = load()
+    keep = []
+    s = make_args(a, keep)
+    nt = C.c_int()
+    lib.fedm_host_plan(C.byref(s), 0, C.byref(nt), None, None, None, None, None, None)
+    m, n = nt.value, a["n"]
+    E, k, L, co = (np.zeros(max(m, 1), np.int32) for _ in range(4))
+    lm = np.zeros((max(m, 1), n), np.uint8)
+    pm = np.zeros((max(m, 1), n), np.uint8)
+    lib.fedm_host_plan(C.byref(s), m, C.byref(nt), E.ctypes.data, k.ctypes.data, L.ctypes.data, co.ctypes.data,
+                       lm.ctypes.data, pm.ctypes.data)
+    return dict(E=E[:m], k=k[:m], library=L[:m], copredict=co[:m], lib=lm[:m].astype(bool), pred=pm[:m].astype(bool))

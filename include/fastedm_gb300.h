@@ -188,6 +188,24 @@ typedef struct fedm_timing {
 
 int fedm_last_timing(const fedm_ctx* ctx, fedm_timing* out);
 
+/* Host-side pieces of the path; they touch no GPU.
+ *  fedm_host_usable:   the usable-row mask of run_command
+ *                      (src/r.cpp:256-257 -> src/manifold.cpp:314-360).
+ *  fedm_host_manifold: the lagged manifold row of every observation for E
+ *                      (src/manifold.cpp:156-238), [n x e_actual]; out may
+ *                      be NULL to query e_actual.
+ *  fedm_host_mt_real2: the splitter's MT19937-64 stream
+ *                      (src/vendor/mersennetwister.h:137-146).
+ *  fedm_host_plan:     configure_tasks' task list (src/edm.cpp:90-212): per
+ *                      task E, k, reported library size, coprediction flag
+ *                      and library / prediction masks ([max_tasks x n]).
+ *                      *n_tasks is always set. */
+int fedm_host_usable(const fedm_args* args, int maxE, int copredict, unsigned char* out);
+int fedm_host_manifold(const fedm_args* args, int E, int copredict, double* out, int* e_actual);
+int fedm_host_mt_real2(unsigned long long seed, long long count, double* out);
+int fedm_host_plan(const fedm_args* args, int max_tasks, int* n_tasks, int* task_E, int* task_k, int* task_library,
+                   int* task_copredict, unsigned char* lib_masks, unsigned char* pred_masks);
+
 /* Measured arithmetic peak of this GPU in TFLOP/s (2 flops per fused
  * multiply-add): kind 0 FP32 FFMA, 1 FP64 DFMA, 2 packed FP32 FFMA2.  A
  * diagnostic for roofline fractions; it has no counterpart in the reference. */

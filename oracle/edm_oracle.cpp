@@ -68,6 +68,9 @@ inline int wrap_add(int a, long long b)
 // head of ln 2, a degree-13 Taylor polynomial with fused multiply-adds and an
 // exact 2^k scaling.  Mode 0 (default) = std::exp, mode 1 = that formula.
 int g_exp_mode = 0;
+// Benchmark sampling only: predict every g_pred_stride-th row of each task's
+// prediction set (1 = all rows, the reference's behaviour).
+int g_pred_stride = 1;
 
 double pow2i(int k)
 {
@@ -1286,6 +1289,87 @@ std::vector<double> to_R_matrix(const std::vector<double>& v, int r, int c, cons
   return m;
 }
 
+
+struct TaskSpec
+{
+  int E, k, library;
+  bool copredict, savePrediction, saveSMAPCoeffs;
+  std::vector<bool> lib, pred;
+};
+
+// src/edm.cpp:90-212
+std::vector<TaskSpec> configure(const oracle_args* a, const Prepared& P, const Generator& gen,
+                                const std::vector<bool>& usable, const std::vector<int>& libraries)
+{
+  std::vector<TaskSpec> out;
+  const bool explore = P.explore;
+  const int maxE = P.Es.back();
+  const bool copredictMode = !gen.co_x.empty();
+  Splitter splitter(explore, a->full, a->shuffle, a->crossfold, usable, a->seed);
+  int numLibraries = explore ? 1 : (int)libraries.size();
+  int numIters = a->num_reps > a->crossfold ? a->num_reps : a->crossfold;
+  std::vector<bool> cousable;
+  if (copredictMode)
+    cousable = gen.generate_usable(maxE, true);
+  bool newSplit = true;
+  int librarySize = 0;
+  for (int iter = 1; iter <= numIters; iter++) {
+    if (explore) {
+      newSplit = true;
+      librarySize = splitter.next_library_size(iter);
+    }
+    for (int i = 0; i < (int)P.Es.size(); i++) {
+      int E = P.Es[i];
+      for (int l = 0; l == 0 || l < (int)libraries.size(); l++) {
+        if (!explore)
+          newSplit = true;
+        int library = explore ? librarySize : libraries[l];
+        int kAdj;
+        if (a->k > 0)
+          kAdj = a->k;
+        else if (a->k < 0)
+          kAdj = -1;
+        else {
+          int isSMap = P.opts.algorithm == Algorithm::SMap;
+          int defK = gen.E_actual(E) + 1 + isSMap;
+          kAdj = defK < library ? defK : library;
+        }
+        bool lastConfig = (E == maxE) && (l + 1 == numLibraries);
+        TaskSpec t;
+        t.E = E;
+        t.k = kAdj;
+        t.library = library;
+        t.copredict = false;
+        if (explore)
+          t.savePrediction = a->save_predictions && ((iter == a->num_reps) || (a->crossfold > 0)) && lastConfig;
+        else
+          t.savePrediction = a->save_predictions && (iter == a->num_reps) && lastConfig;
+        t.saveSMAPCoeffs = a->save_smap_coeffs;
+        if (newSplit) {
+          splitter.update(library, iter);
+          newSplit = false;
+        }
+        t.lib = splitter.lib;
+        t.pred = splitter.pred;
+        out.push_back(t);
+        if (copredictMode) {
+          TaskSpec c = t;
+          c.copredict = true;
+          if (explore)
+            c.savePrediction =
+              a->save_copredictions && ((iter == a->num_reps) || (a->crossfold > 0)) && lastConfig;
+          else
+            c.savePrediction = a->save_copredictions && (iter == a->num_reps) && lastConfig;
+          c.saveSMAPCoeffs = false;
+          c.pred = cousable;
+          out.push_back(c);
+        }
+      }
+    }
+  }
+  return out;
+}
+
 } // namespace
 
 extern "C" {
@@ -1293,6 +1377,11 @@ extern "C" {
 void oracle_set_exp_mode(int mode)
 {
   g_exp_mode = mode;
+}
+
+void oracle_set_pred_stride(int stride)
+{
+  g_pred_stride = stride > 1 ? stride : 1;
 }
 
 double oracle_exp(double x)
@@ -1340,69 +1429,24 @@ oracle_result* oracle_run_command(const oracle_args* a)
     std::vector<int> libraries = P.libraries;
     if (!P.explore && libraries.empty())
       libraries = { numUsable };
-    bool copredictMode = !gen.co_x.empty();
-    bool explore = P.explore;
 
     // src/edm.cpp:90-212 configure_tasks, executed in order (run_tasks)
-    Splitter splitter(explore, a->full, a->shuffle, a->crossfold, usable, a->seed);
-    int numLibraries = explore ? 1 : (int)libraries.size();
-    int numIters = a->num_reps > a->crossfold ? a->num_reps : a->crossfold;
-    std::vector<bool> cousable;
-    if (copredictMode)
-      cousable = gen.generate_usable(maxE, true);
-    bool newSplit = true;
-    int librarySize = 0;
+    std::vector<TaskSpec> specs = configure(a, P, gen, usable, libraries);
     std::vector<PredictionResult> results;
-    int numTasks = 0;
-    for (int iter = 1; iter <= numIters; iter++) {
-      if (explore) {
-        newSplit = true;
-        librarySize = splitter.next_library_size(iter);
+    for (TaskSpec& ts : specs) {
+      if (g_pred_stride > 1) {
+        int c = 0;
+        for (size_t r = 0; r < ts.pred.size(); r++)
+          if (ts.pred[r] && (c++ % g_pred_stride) != 0)
+            ts.pred[r] = false;
       }
-      for (int i = 0; i < (int)P.Es.size(); i++) {
-        int E = P.Es[i];
-        for (int l = 0; l == 0 || l < (int)libraries.size(); l++) {
-          if (!explore)
-            newSplit = true;
-          int library = explore ? librarySize : libraries[l];
-          int kAdj;
-          if (a->k > 0)
-            kAdj = a->k;
-          else if (a->k < 0)
-            kAdj = -1;
-          else {
-            int isSMap = opts.algorithm == Algorithm::SMap;
-            int defK = gen.E_actual(E) + 1 + isSMap;
-            kAdj = defK < library ? defK : library;
-          }
-          bool lastConfig = (E == maxE) && (l + 1 == numLibraries);
-          if (explore)
-            opts.savePrediction =
-              a->save_predictions && ((iter == a->num_reps) || (a->crossfold > 0)) && lastConfig;
-          else
-            opts.savePrediction = a->save_predictions && (iter == a->num_reps) && lastConfig;
-          opts.saveSMAPCoeffs = a->save_smap_coeffs;
-          if (newSplit) {
-            splitter.update(library, iter);
-            newSplit = false;
-          }
-          opts.copredict = false;
-          opts.k = kAdj;
-          opts.library = library;
-          results.push_back(edm_task(gen, opts, E, splitter.lib, splitter.pred));
-          numTasks++;
-          if (copredictMode) {
-            opts.copredict = true;
-            if (explore)
-              opts.savePrediction =
-                a->save_copredictions && ((iter == a->num_reps) || (a->crossfold > 0)) && lastConfig;
-            else
-              opts.savePrediction = a->save_copredictions && (iter == a->num_reps) && lastConfig;
-            opts.saveSMAPCoeffs = false;
-            results.push_back(edm_task(gen, opts, E, splitter.lib, cousable));
-          }
-        }
-      }
+      Options o2 = opts;
+      o2.k = ts.k;
+      o2.library = ts.library;
+      o2.copredict = ts.copredict;
+      o2.savePrediction = ts.savePrediction;
+      o2.saveSMAPCoeffs = ts.saveSMAPCoeffs;
+      results.push_back(edm_task(gen, o2, ts.E, ts.lib, ts.pred));
     }
 
     // src/r.cpp:348-457 result marshalling
@@ -1481,6 +1525,34 @@ oracle_result* oracle_run_command(const oracle_args* a)
     R.rc = UNKNOWN_ERROR;
   }
   return &R;
+}
+
+int oracle_plan(const oracle_args* a, int max_tasks, int* n_tasks, int* task_E, int* task_k, int* task_library,
+                int* task_copredict, unsigned char* lib_masks, unsigned char* pred_masks)
+{
+  try {
+    Prepared P = prepare(a);
+    std::vector<bool> usable = P.gen->generate_usable(P.Es.back(), false);
+    int numUsable = (int)std::count(usable.begin(), usable.end(), true);
+    std::vector<int> libraries = P.libraries;
+    if (!P.explore && libraries.empty())
+      libraries = { numUsable };
+    auto specs = configure(a, P, *P.gen, usable, libraries);
+    *n_tasks = (int)specs.size();
+    for (int i = 0; i < (int)specs.size() && i < max_tasks; i++) {
+      task_E[i] = specs[i].E;
+      task_k[i] = specs[i].k;
+      task_library[i] = specs[i].library;
+      task_copredict[i] = specs[i].copredict;
+      for (int r = 0; r < a->n; r++) {
+        lib_masks[(size_t)i * a->n + r] = specs[i].lib[r];
+        pred_masks[(size_t)i * a->n + r] = specs[i].pred[r];
+      }
+    }
+    return 0;
+  } catch (...) {
+    return UNKNOWN_ERROR;
+  }
 }
 
 void oracle_free_result(oracle_result* r)

@@ -138,12 +138,22 @@ int oracle_task_sizes(const oracle_args* args, oracle_task_io* io);
 /* Second pass: fills the output arrays. Returns the task's max rc. */
 int oracle_task_run(const oracle_args* args, oracle_task_io* io);
 
+/* The task list configure_tasks builds (src/edm.cpp:90-212): per task E,
+ * kAdj, reported library size, coprediction flag and the library /
+ * prediction membership masks ([max_tasks x n] each).  *n_tasks is always
+ * set; at most max_tasks entries are written. */
+int oracle_plan(const oracle_args* args, int max_tasks, int* n_tasks, int* task_E, int* task_k, int* task_library,
+                int* task_copredict, unsigned char* lib_masks, unsigned char* pred_masks);
+
 /* The usable-row mask run_command computes (src/r.cpp:256-257). */
 int oracle_usable(const oracle_args* args, int maxE, int copredict, unsigned char* usable_out);
 
 /* 0 (default): weights use std::exp like the reference.  1: weights use the
  * IEEE-only exp formula the GPU library evaluates, for bit-level parity. */
 void oracle_set_exp_mode(int mode);
+/* Benchmark sampling: predict only every stride-th row of each prediction
+ * set (1, the default, is the reference's behaviour). */
+void oracle_set_pred_stride(int stride);
 double oracle_exp(double x);
 
 /* MT19937-64 stream as the splitter consumes it (getReal2). */

@@ -80,6 +80,8 @@ def load():
         _lib.oracle_usable.argtypes = [C.POINTER(OracleArgs), C.c_int, C.c_int, C.c_void_p]
         _lib.oracle_mt_real2.argtypes = [C.c_ulonglong, C.c_longlong, C.c_void_p]
         _lib.oracle_set_exp_mode.argtypes = [C.c_int]
+        _lib.oracle_set_pred_stride.argtypes = [C.c_int]
+        _lib.oracle_plan.argtypes = [C.POINTER(OracleArgs), C.c_int] + [C.c_void_p] * 7
         _lib.oracle_exp.argtypes = [C.c_double]
         _lib.oracle_exp.restype = C.c_double
     return _lib
@@ -306,3 +308,25 @@ def set_exp_mode(mode):
 
 def exp_rn(x):
     return load().oracle_exp(float(x))
+
+
+def plan(a):
+    """configure_tasks' task list: dict of arrays plus [tasks x n] masks."""
+    lib = load()
+    keep = []
+    s = make_args(a, keep)
+    nt = C.c_int()
+    lib.oracle_plan(C.byref(s), 0, C.byref(nt), None, None, None, None, None, None)
+    m = nt.value
+    n = a["n"]
+    E, k, L, co = (np.zeros(max(m, 1), np.int32) for _ in range(4))
+    lm = np.zeros((max(m, 1), n), np.uint8)
+    pm = np.zeros((max(m, 1), n), np.uint8)
+    lib.oracle_plan(C.byref(s), m, C.byref(nt), E.ctypes.data, k.ctypes.data, L.ctypes.data, co.ctypes.data,
+                    lm.ctypes.data, pm.ctypes.data)
+    return dict(E=E[:m], k=k[:m], library=L[:m], copredict=co[:m], lib=lm[:m].astype(bool), pred=pm[:m].astype(bool))
+
+
+def set_pred_stride(stride):
+    """Benchmark sampling: predict every stride-th row of each prediction set."""
+    load().oracle_set_pred_stride(int(stride))
