@@ -203,21 +203,25 @@ def run_ours(a):
         traffic = pj.get("bytes_per_full_launch")
 
     # plain FP64 GPU form and |delta rho| on a 2-replicate sample
-    sample_reps = 2
-    ctx64 = fedm.Context(local, precision=fedm.PRECISION_FP64)
-    t_fp64 = 0.0
-    p_fp64 = 0
-    drho = 0.0
-    for alg in ("simplex", "smap"):
-        args = ccm_args(fedm, w, alg, sample_reps)
-        r64 = ctx64.run_command(args)
-        tm = ctx64.timing()
-        t_fp64 += tm["device_ms"] / 1e3
-        p_fp64 += tm["predictions"]
-        rmx = ctx.run_command(args)
-        drho = max(drho, float(np.max(np.abs(np.asarray(r64["stats"]["rho"]) - np.asarray(rmx["stats"]["rho"])))))
-    ctx64.close()
-    fp64_value = p_fp64 / t_fp64
+    fp64 = None
+    if not a.no_fp64:
+        sample_reps = 2
+        ctx64 = fedm.Context(local, precision=fedm.PRECISION_FP64)
+        t_fp64 = 0.0
+        p_fp64 = 0
+        drho = 0.0
+        for alg in ("simplex", "smap"):
+            args = ccm_args(fedm, w, alg, sample_reps)
+            r64 = ctx64.run_command(args)
+            tm = ctx64.timing()
+            t_fp64 += tm["device_ms"] / 1e3
+            p_fp64 += tm["predictions"]
+            rmx = ctx.run_command(args)
+            drho = max(drho, float(np.max(np.abs(np.asarray(r64["stats"]["rho"]) - np.asarray(rmx["stats"]["rho"])))))
+        ctx64.close()
+        fp64 = {"value": p_fp64 / t_fp64, "unit": "predictions/s",
+                "sample": f"{sample_reps} replicates, both algorithms", "mixed_over_fp64": value / (p_fp64 / t_fp64),
+                "max_abs_drho_vs_fp64": drho}
 
     cpu = None
     if world == 1 and not a.no_cpu:
@@ -245,8 +249,7 @@ def run_ours(a):
             "hbm": {"achieved_gbs": alg_bytes / (knn_ms_step * 1e-3) / 1e9, "peak_gbs": HBM_GBS,
                     "frac": alg_bytes / (knn_ms_step * 1e-3) / 1e9 / HBM_GBS, "peak_source": "MEASURED_PEAKS.json"},
         },
-        "fp64_plain": {"value": fp64_value, "unit": "predictions/s", "sample": f"{sample_reps} replicates, both algorithms",
-                       "mixed_over_fp64": value / fp64_value, "max_abs_drho_vs_fp64": drho},
+        "fp64_plain": fp64,
         "fallback_points_per_step": int(s0["fallback_points"]),
         "clocks": clocks,
         "cpu_baseline": cpu,
@@ -327,6 +330,8 @@ def main():
     ap.add_argument("--ref-libs", dest="ref_libs", type=int, default=None,
                     help="library sizes in each CPU reference sample (default: all)")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-fp64", dest="no_fp64", action="store_true",
+                    help="skip the plain FP64 sample (profiling runs)")
     a = ap.parse_args()
     if a.impl == "reference":
         run_reference(a)

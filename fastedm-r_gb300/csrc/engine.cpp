@@ -470,8 +470,10 @@ void run_group(Context& ctx, const Options& o, const std::vector<Task>& tasks, c
   // chunking: neighbour lists, statuses and the all-mode Gram buffer
   const long long budget = 2LL << 30;
   long long per_point = (long long)kcap * 12 + 8;
+  if (any_all)
+    per_point += max_nlib_all * 8;  // the point's distances
   if (any_all && o.algorithm == 1)
-    per_point += (long long)nth * (n * n + n) * 8;
+    per_point += (long long)nth * all_mode_slab(Ea) * 8;
   long long chunk = std::max<long long>(1, std::min<long long>(std::max<long long>(P, 1), budget / per_point));
   ChunkBuffers c{};
   c.kcap = kcap;
@@ -480,14 +482,12 @@ void run_group(Context& ctx, const Options& o, const std::vector<Task>& tasks, c
   c.nn_count = (int*)ctx.buf("nn_count", (size_t)chunk * 4);
   c.status = (int*)ctx.buf("status", (size_t)chunk * 4);
   if (any_all && o.algorithm == 1)
-    c.gram = (double*)ctx.buf("gram", (size_t)chunk * nth * (n * n + n) * 8);
+    c.gram = (double*)ctx.buf("gram", (size_t)chunk * nth * all_mode_slab(Ea) * 8);
   long long scratch = 1;
   if (any_all)
-    scratch = std::max(scratch, all_mode_scratch_doubles(ctx.num_sms, max_nlib_all));
+    scratch = std::max(scratch, chunk * max_nlib_all);
   if ((any_finite || any_mixed) && o.algorithm == 1)
     scratch = std::max(scratch, smap_nn_scratch_doubles(ctx.num_sms, n, kcap));
-  if (any_all && o.algorithm == 1 && n > 8)
-    scratch = std::max(scratch, (long long)ctx.num_sms * 4 * 128 * (3LL * n * n + 3LL * n));
   c.scratch = (double*)ctx.buf("scratch", (size_t)scratch * 8);
   c.scratch_doubles = scratch;
 
@@ -590,12 +590,43 @@ void run_group(Context& ctx, const Options& o, const std::vector<Task>& tasks, c
     m.err_abs = std::ldexp(R, -21) + 1e-21;
     const int C = kmix <= 6 ? 8 : 16;
     if (job.detail) {
-      m.kslots = C;
       m.nn_idx = (int*)ctx.buf("mix_nn_idx", (size_t)std::max<long long>(P, 1) * C * 4);
       m.nn_dist = (double*)ctx.buf("mix_nn_dist", (size_t)std::max<long long>(P, 1) * C * 8);
     }
-    timed([&] { launch_knn_mixed(g, m, C, ctx.num_sms, s); });
     ctx.timing.kernel_launches += (job.dFp != job.dF ? 2 : 1) + 1;  // centring, counter fill
+    m.kslots = C;
+    if (o.algorithm == 1 && ctx.smap_deferred) {
+      // S-map alternative: scan + re-rank in batches of items; each batch's
+      // neighbour lists go to a separate register-resident SVD kernel
+      const long long batch_points = 8LL << 20;
+      const int batch_items = (int)std::max<long long>(1, batch_points / MIX_POINTS);
+      const long long cap = std::min<long long>((long long)batch_items * MIX_POINTS, std::max<long long>(P, 1));
+      m.defer = 1;
+      m.l_cap = (int)cap;
+      m.l_point = (long long*)ctx.buf("l_point", (size_t)cap * 8);
+      m.l_prow = (int*)ctx.buf("l_prow", (size_t)cap * 4);
+      m.l_task = (int*)ctx.buf("l_task", (size_t)cap * 4);
+      m.l_k = (int*)ctx.buf("l_k", (size_t)cap * 4);
+      m.l_rows = (int*)ctx.buf("l_rows", (size_t)cap * C * 4);
+      m.l_dist = (double*)ctx.buf("l_dist", (size_t)cap * C * 8);
+      m.l_count = (int*)ctx.buf("l_count", 4);
+      for (int b0 = 0; b0 < m.n_items; b0 += batch_items) {
+        if (ctx.keep_going && !ctx.keep_going())
+          throw Error{ RC_BREAK_HIT, "cancelled" };
+        m.item_begin = b0;
+        m.item_end = std::min(m.n_items, b0 + batch_items);
+        fill_i32(m.counter, 1, 0, s);
+        fill_i32(m.l_count, 1, 0, s);
+        timed([&] { launch_knn_mixed(g, m, C, ctx.num_sms, s); });
+        launch_smap_lists(g, m, ctx.num_sms, s);
+        ctx.check("smap lists");
+        ctx.timing.kernel_launches += 4;
+      }
+    } else {
+      m.item_begin = 0;
+      m.item_end = m.n_items;
+      timed([&] { launch_knn_mixed(g, m, C, ctx.num_sms, s); });
+    }
     int nfb = 0;
     ctx.download(&nfb, m.fb_count, 4);
     ck(cudaStreamSynchronize(s), "sync");

@@ -25,6 +25,10 @@ public:
   cudaStream_t stream = nullptr;
   int precision = FEDM_PRECISION_MIXED;
   int (*keep_going)(void) = nullptr;
+  // S-map in the mixed path: solve inside the scan kernel (false, default:
+  // the FP64 solve overlaps the FP32 scan of other warps) or in a separate
+  // kernel over batched neighbour lists (true)
+  bool smap_deferred = false;
   std::string last_error;
   fedm_timing timing{};
 

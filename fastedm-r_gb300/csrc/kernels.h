@@ -90,9 +90,9 @@ struct ChunkBuffers
   double* nn_dist;           // [chunk x kcap]
   int* nn_count;             // [chunk] k used
   int* status;               // [chunk]
-  double* scratch;           // per-warp / per-thread scratch
+  double* scratch;           // smap_nn solver scratch, or all-mode distances [chunk x max_nlib]
   long long scratch_doubles; // its size
-  double* gram;              // [chunk x n_thetas x (n*n + n)] for the all-mode S-map
+  double* gram;              // all-mode S-map solver scratch, [chunk x n_thetas x slab]
   const long long* plist;    // optional: chunk point q is plist[q] (p_begin = 0, p_end = count)
 };
 
@@ -103,7 +103,7 @@ void launch_smap_nn(const GroupParams& g, const ChunkBuffers& c, int num_sms, cu
 void launch_all_mode(const GroupParams& g, const ChunkBuffers& c, int num_sms, long long max_nlib, cudaStream_t s);
 void launch_stats(const GroupParams& g, const DevTask* tasks_host_unused, int n_tasks, double* rho, double* mae,
                   cudaStream_t s);
-long long all_mode_scratch_doubles(int num_sms, long long max_nlib);
+long long all_mode_slab(int Ea);  // doubles of solver scratch per (point, theta)
 long long smap_nn_scratch_doubles(int num_sms, int n, int kcap);
 
 // Mixed-precision neighbour scan for the common case (L2, no missing values,
@@ -127,7 +127,24 @@ struct MixedRun
   int* nn_idx;         // optional [total_points x kslots] final neighbour lists
   double* nn_dist;
   int kslots;
+  int item_begin;      // first item of this launch (the queue head starts here)
+  int item_end;        // one past the last item of this launch
+  // S-map: when set, the neighbour lists are appended here and solved by
+  // launch_smap_lists instead of in the scan kernel
+  int defer;
+  long long* l_point;  // [cap] global point id
+  int* l_prow;         // [cap] prediction row
+  int* l_task;         // [cap] task slot
+  int* l_k;            // [cap] neighbours used
+  int* l_rows;         // [cap x kslots] library rows of the neighbours
+  double* l_dist;      // [cap x kslots] their FP64 distances
+  int* l_count;
+  int l_cap;
 };
+
+// Solves the deferred S-map systems of launch_knn_mixed (one thread per
+// point, all thetas; the SVD is unrolled for the compile-time size).
+void launch_smap_lists(const GroupParams& g, const MixedRun& m, int num_sms, cudaStream_t s);
 
 void launch_knn_mixed(const GroupParams& g, const MixedRun& m, int C, int num_sms, cudaStream_t s);
 void center_to_f32(const double* F, long long n, int Ea, const double* center, float* F32, int stride,

@@ -360,36 +360,18 @@ __global__ void smap_nn_kernel(GroupParams g, ChunkBuffers c, long long slab)
 
 // ------------------------------------------------------ all-neighbour mode
 // k = -1 (or k >= library size): every valid neighbour in library order
-// (src/edm.cpp:613-617).  One warp per point; the point's distances are kept
-// in the warp's scratch row and the weighted sums are warp reductions.
-__device__ __forceinline__ double warp_sum_d(double v)
-{
-  for (int o = 16; o > 0; o >>= 1)
-    v += __shfl_xor_sync(FULL, v, o);
-  return v;
-}
-__device__ __forceinline__ double warp_min_d(double v)
-{
-  for (int o = 16; o > 0; o >>= 1)
-    v = fmin(v, __shfl_xor_sync(FULL, v, o));
-  return v;
-}
-
-__global__ void all_mode_kernel(GroupParams g, ChunkBuffers c, long long max_nlib, int per_warp_bytes)
+// (src/edm.cpp:613-617).  all_dist_kernel writes each point's distances to
+// its row of the chunk's distance buffer (-1 marks an invalid pair); then
+// one thread per (point, theta) reduces them sequentially in library order,
+// the order the reference's loops use, so the results are the same bits.
+__global__ void all_dist_kernel(GroupParams g, ChunkBuffers c, long long max_nlib, int per_warp_bytes)
 {
   extern __shared__ __align__(16) unsigned char smem[];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5, wpb = blockDim.x >> 5;
-  const long long gw = (long long)blockIdx.x * wpb + wib;
-  const long long nwarps = (long long)gridDim.x * wpb;
-  double* scr = c.scratch + gw * max_nlib;
-  const int n = g.Ea + 1;
-  const int nent = n * (n + 1) / 2 + n;
-  unsigned char* base = smem + (size_t)wib * per_warp_bytes;
-  double* sy = (double*)base;           // [Ea]
-  double* sX = sy + g.Ea;               // [32 x (n+1)]
-  double* sG = sX + 32 * (n + 1);       // [nent]
-  for (long long p = c.p_begin + gw; p < c.p_end; p += nwarps) {
-    const long long q = p - c.p_begin;
+  const long long chunk = c.p_end - c.p_begin;
+  double* sy = (double*)(smem + (size_t)wib * per_warp_bytes);
+  for (long long q = (long long)blockIdx.x * wpb + wib; q < chunk; q += (long long)gridDim.x * wpb) {
+    const long long p = point_of(c, q);
     const DevTask T = g.tasks[find_task(g, p)];
     if (!T.all_mode)
       continue;
@@ -399,152 +381,111 @@ __global__ void all_mode_kernel(GroupParams g, ChunkBuffers c, long long max_nli
     const int ppanel = g.panel ? g.panel[prow] : 0;
     const double ptime = g.point_time[prow];
     __syncwarp();
-    double lmin = DBL_MAX, lsum = 0;
+    double* dq = c.scratch + q * max_nlib;
     int lcnt = 0;
     for (int i = lane; i < T.n_lib; i += 32) {
       double d;
-      if (exact_distance(g, g.lib_rows[T.lib_off + i], prow, sy, ppanel, ptime, d)) {
-        scr[i] = d;
-        lmin = fmin(lmin, d);
-        lsum += d;
-        lcnt++;
-      } else {
-        scr[i] = -1.0;
-      }
+      const bool ok = exact_distance(g, g.lib_rows[T.lib_off + i], prow, sy, ppanel, ptime, d);
+      dq[i] = ok ? d : -1.0;
+      lcnt += ok;
     }
     const int cnt = __reduce_add_sync(FULL, lcnt);
-    const double dmin = warp_min_d(lmin);
-    const double mean = warp_sum_d(lsum) / (double)cnt;
     int status = PT_OK;
-    if (!g.force_compute && T.k > 0 && T.k > cnt)
+    if (!g.force_compute && T.k_req > 0 && T.k_req > cnt)
       status = PT_INSUFFICIENT;
     else if (cnt == 0)
       status = g.force_compute ? PT_EARLY_SUCCESS : PT_INSUFFICIENT;
-    if (status != PT_OK) {
-      if (lane < g.n_thetas)
-        for (int t = lane; t < g.n_thetas; t += 32)
-          early_rc(g, T.task, status, t);
-      if (lane == 0 && g.kused)
+    if (lane == 0) {
+      c.status[q] = status;
+      c.nn_count[q] = cnt;
+      if (status == PT_OK)
+        note_k(g, T.task, p, cnt);
+      else if (g.kused)
         g.kused[p] = INT_MIN;
-      __syncwarp();
-      continue;
     }
-    if (lane == 0)
-      note_k(g, T.task, p, cnt);
-    for (int t = 0; t < g.n_thetas; t++) {
-      const double theta = g.thetas[t];
-      if (g.algorithm == 0) {
-        double ls = 0;
-        for (int i = lane; i < T.n_lib; i += 32)
-          if (scr[i] >= 0)
-            ls = ls + exp_rn(-theta * (scr[i] / dmin));
-        const double sumw = warp_sum_d(ls);
-        double lr = 0;
-        for (int i = lane; i < T.n_lib; i += 32)
-          if (scr[i] >= 0) {
-            const double w = exp_rn(-theta * (scr[i] / dmin));
-            lr = lr + g.lib_target[g.lib_rows[T.lib_off + i]] * (w / sumw);
-          }
-        const double r = warp_sum_d(lr);
-        if (lane == 0)
-          g.pred[(size_t)t * g.total_points + p] = r;
-      } else {
-        for (int e = lane; e < nent; e += 32)
-          sG[e] = 0;
-        __syncwarp();
-        for (int b0 = 0; b0 < T.n_lib; b0 += 32) {
-          const int i = b0 + lane;
-          double* xr = sX + lane * (n + 1);
-          if (i < T.n_lib && scr[i] >= 0) {
-            const double w = exp_rn(-theta * (scr[i] / mean));
-            const int row = g.lib_rows[T.lib_off + i];
-            xr[0] = w;
-            for (int j = 1; j < n; j++)
-              xr[j] = w * g.F[(size_t)row * g.Ea + j - 1];
-            xr[n] = w * g.lib_target[row];
-          } else {
-            for (int j = 0; j <= n; j++)
-              xr[j] = 0;
-          }
-          __syncwarp();
-          for (int e = lane; e < nent; e += 32) {
-            int a, b;
-            if (e < n * (n + 1) / 2) {
-              // e -> (a, b) with a <= b, row-major upper triangle
-              a = 0;
-              int rem = e;
-              while (rem >= n - a) {
-                rem -= n - a;
-                a++;
-              }
-              b = a + rem;
-            } else {
-              a = e - n * (n + 1) / 2;
-              b = n;  // the y column
-            }
-            double acc = sG[e];
-            for (int r = 0; r < 32; r++)
-              acc += sX[r * (n + 1) + a] * sX[r * (n + 1) + b];
-            sG[e] = acc;
-          }
-          __syncwarp();
-        }
-        double* G = c.gram + (q * g.n_thetas + t) * (long long)(n * n + n);
-        for (int e = lane; e < nent; e += 32) {
-          if (e < n * (n + 1) / 2) {
-            int a = 0, rem = e;
-            while (rem >= n - a) {
-              rem -= n - a;
-              a++;
-            }
-            const int b = a + rem;
-            G[a * n + b] = sG[e];
-            G[b * n + a] = sG[e];
-          } else {
-            G[n * n + (e - n * (n + 1) / 2)] = sG[e];
-          }
-        }
-        __syncwarp();
-      }
-    }
-    if (lane == 0)
-      c.status[q] = PT_OK;
+    __syncwarp();
   }
 }
 
-// Solves the all-mode S-map systems written by all_mode_kernel.
-__global__ void smap_all_solve_kernel(GroupParams g, ChunkBuffers c, long long slab)
+__global__ void all_forecast_kernel(GroupParams g, ChunkBuffers c, long long max_nlib, long long slab)
 {
   const long long chunk = c.p_end - c.p_begin;
-  const long long nthreads = (long long)gridDim.x * blockDim.x;
-  const long long tid = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= chunk * g.n_thetas)
+    return;
+  const int t = (int)(idx / chunk);
+  const long long q = idx - (long long)t * chunk;
+  const long long p = point_of(c, q);
+  const DevTask T = g.tasks[find_task(g, p)];
+  if (!T.all_mode)
+    return;
+  const int st = c.status[q];
+  if (st != PT_OK) {
+    early_rc(g, T.task, st, t);
+    return;
+  }
+  const double* dq = c.scratch + q * max_nlib;
+  const double theta = g.thetas[t];
+  if (g.algorithm == 0) {
+    // src/edm.cpp:707-735
+    double minDist = DBL_MAX;
+    for (int i = 0; i < T.n_lib; i++)
+      if (dq[i] >= 0 && dq[i] < minDist)
+        minDist = dq[i];
+    double sumw = 0.0;
+    for (int i = 0; i < T.n_lib; i++)
+      if (dq[i] >= 0)
+        sumw = sumw + exp_rn(-theta * (dq[i] / minDist));
+    double r = 0.0;
+    for (int i = 0; i < T.n_lib; i++)
+      if (dq[i] >= 0) {
+        const double w = exp_rn(-theta * (dq[i] / minDist));
+        r = r + g.lib_target[g.lib_rows[T.lib_off + i]] * (w / sumw);
+      }
+    g.pred[(size_t)t * g.total_points + p] = r;
+    return;
+  }
+  // src/edm.cpp:737-814 over every valid neighbour
   const int n = g.Ea + 1;
-  double lW[SMALL_N * SMALL_N], lU[SMALL_N * SMALL_N], lV[SMALL_N * SMALL_N], lsv[SMALL_N], ltmp[SMALL_N],
-    lx[SMALL_N];
-  double *W = lW, *U = lU, *V = lV, *sv = lsv, *tmp = ltmp, *xs = lx;
-  if (n > SMALL_N) {
-    double* s = c.scratch + tid * slab;
-    W = s;
-    U = W + n * n;
-    V = U + n * n;
-    sv = V + n * n;
-    tmp = sv + n;
-    xs = tmp + n;
-  }
-  for (long long idx = tid; idx < chunk * g.n_thetas; idx += nthreads) {
-    const int t = (int)(idx / chunk);
-    const long long q = idx - (long long)t * chunk;
-    const long long p = c.p_begin + q;
-    const DevTask T = g.tasks[find_task(g, p)];
-    if (!T.all_mode || c.status[q] != PT_OK)
+  const int ke = c.nn_count[q];
+  double mean = 0;
+  for (int i = 0; i < T.n_lib; i++)
+    if (dq[i] >= 0)
+      mean += dq[i];
+  mean /= (double)ke;
+  double* W = c.gram + idx * slab;  // [n*n] normal matrix, then U, V, sv, tmp, b, x
+  double* U = W + n * n;
+  double* V = U + n * n;
+  double* sv = V + n * n;
+  double* tmp = sv + n;
+  double* bv = tmp + n;
+  double* xs = bv + n;
+  for (int e = 0; e < n * n; e++)
+    W[e] = 0;
+  for (int a = 0; a < n; a++)
+    bv[a] = 0;
+  for (int i = 0; i < T.n_lib; i++) {
+    if (dq[i] < 0)
       continue;
-    const double* G = c.gram + (q * g.n_thetas + t) * (long long)(n * n + n);
-    for (int i = 0; i < n * n; i++)
-      W[i] = G[i];
-    svd_solve(W, U, V, sv, tmp, G + n * n, xs, n);
-    const int prow = g.pred_rows[T.pred_off + (int)(p - T.point_base)];
-    smap_finish(g, T, p, prow, t, xs, n);
+    const double w = exp_rn(-theta * (dq[i] / mean));
+    const int row = g.lib_rows[T.lib_off + i];
+    const double* fr = g.F + (size_t)row * g.Ea;
+    const double yl = w * g.lib_target[row];
+    for (int a = 0; a < n; a++) {
+      const double xa = a == 0 ? w : w * fr[a - 1];
+      for (int b = a; b < n; b++) {
+        const double xb = b == 0 ? w : w * fr[b - 1];
+        W[a * n + b] += xa * xb;
+      }
+      bv[a] += xa * yl;
+    }
   }
+  for (int a = 0; a < n; a++)
+    for (int b = 0; b < a; b++)
+      W[a * n + b] = W[b * n + a];
+  svd_solve(W, U, V, sv, tmp, bv, xs, n);
+  const int prow = g.pred_rows[T.pred_off + (int)(p - T.point_base)];
+  smap_finish(g, T, p, prow, t, xs, n);
 }
 
 // ----------------------------------------------------------------- stats
@@ -624,12 +565,8 @@ int knn_warps_per_block(int Ea, int kcap, int& per_warp)
 
 int all_warps_per_block(int Ea, int& per_warp)
 {
-  const int n = Ea + 1;
-  per_warp = ((Ea + 32 * (n + 1) + n * (n + 1) / 2 + n) * 8 + 15) / 16 * 16;
-  int w = 4;
-  while (w > 1 && (long long)w * per_warp > 200 * 1024)
-    w >>= 1;
-  return w;
+  per_warp = (Ea * 8 + 15) / 16 * 16;
+  return 8;
 }
 
 } // namespace
@@ -688,42 +625,26 @@ void launch_smap_nn(const GroupParams& g, const ChunkBuffers& c, int num_sms, cu
   smap_nn_kernel<<<(int)blocks, 128, 0, s>>>(g, c, slab);
 }
 
-long long all_mode_scratch_doubles(int num_sms, long long max_nlib)
+long long all_mode_slab(int Ea)
 {
-  return (long long)num_sms * 8 * 4 * (max_nlib > 0 ? max_nlib : 1);
+  const int n = Ea + 1;
+  return 3LL * n * n + 4LL * n;
 }
 
 void launch_all_mode(const GroupParams& g, const ChunkBuffers& c, int num_sms, long long max_nlib, cudaStream_t s)
 {
   int per_warp;
   const int w = all_warps_per_block(g.Ea, per_warp);
-  const size_t smem = (size_t)w * per_warp;
-  if (smem > 48 * 1024)
-    cudaFuncSetAttribute(all_mode_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  const long long warps_avail = c.scratch_doubles / (max_nlib > 0 ? max_nlib : 1);
-  long long blocks = warps_avail / w;
   const long long chunk = c.p_end - c.p_begin;
-  if (blocks > (chunk + w - 1) / w)
-    blocks = (chunk + w - 1) / w;
+  long long blocks = (chunk + w - 1) / w;
+  if (blocks > (long long)num_sms * 64)
+    blocks = (long long)num_sms * 64;
   if (blocks < 1)
     blocks = 1;
-  all_mode_kernel<<<(int)blocks, 32 * w, smem, s>>>(g, c, max_nlib, per_warp);
-  if (g.algorithm == 1) {
-    const int n = g.Ea + 1;
-    const long long slab = 3LL * n * n + 3LL * n;
-    const long long total = chunk * g.n_thetas;
-    long long b2 = (total + 127) / 128;
-    if (n > SMALL_N) {
-      const long long cap = c.scratch_doubles / (128 * slab);
-      if (b2 > cap)
-        b2 = cap;
-    } else if (b2 > (long long)num_sms * 64) {
-      b2 = (long long)num_sms * 64;
-    }
-    if (b2 < 1)
-      b2 = 1;
-    smap_all_solve_kernel<<<(int)b2, 128, 0, s>>>(g, c, slab);
-  }
+  all_dist_kernel<<<(int)blocks, 32 * w, (size_t)w * per_warp, s>>>(g, c, max_nlib, per_warp);
+  const long long total = chunk * g.n_thetas;
+  if (total > 0)
+    all_forecast_kernel<<<(int)((total + 127) / 128), 128, 0, s>>>(g, c, max_nlib, all_mode_slab(g.Ea));
 }
 
 void launch_stats(const GroupParams& g, const DevTask*, int n_tasks, double* rho, double* mae, cudaStream_t s)

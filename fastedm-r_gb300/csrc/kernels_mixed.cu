@@ -25,6 +25,7 @@
 #include "exp_rn.cuh"
 #include "kernels.h"
 #include "smap_solve.cuh"
+#include "smap_solve_n.cuh"
 
 namespace fedm {
 
@@ -83,6 +84,10 @@ __device__ __forceinline__ double fp64_sq(const GroupParams& g, int row, const d
   return s;
 }
 
+template<int EA>
+__device__ __noinline__ void smap_point(const GroupParams& g, long long p, int prow, bool save, int keff,
+                                        const int* rows, const double* cd);
+
 // Candidates of one point, handed to the out-of-line FP64 stage.
 template<int C>
 struct Cand
@@ -93,7 +98,7 @@ struct Cand
   int zi[ZCAP];
 };
 
-template<int EA, int C>
+template<int EA, int C, int ALG>
 __device__ __noinline__ void finalize_point(const GroupParams& g, const MixedRun& m, const DevTask& T, long long p,
                                             int prow, const Cand<C>& cand)
 {
@@ -203,8 +208,20 @@ __device__ __noinline__ void finalize_point(const GroupParams& g, const MixedRun
   int rows[C + ZCAP];
   for (int j = 0; j < keff; j++)
     rows[j] = g.lib_rows[T.lib_off + ci[j]];
+  if (m.defer) {
+    const int slot = atomicAdd(m.l_count, 1);
+    m.l_point[slot] = p;
+    m.l_prow[slot] = prow;
+    m.l_task[slot] = T.task | (T.save_coeffs ? (1 << 30) : 0);
+    m.l_k[slot] = keff;
+    for (int j = 0; j < keff; j++) {
+      m.l_rows[(size_t)slot * m.kslots + j] = rows[j];
+      m.l_dist[(size_t)slot * m.kslots + j] = cd[j];
+    }
+    return;
+  }
 
-  if (g.algorithm == 0) {
+  if constexpr (ALG == 0) {
     // simplex (src/edm.cpp:707-735)
     double minD = cd[0];
     for (int j = 1; j < keff; j++)
@@ -229,64 +246,11 @@ __device__ __noinline__ void finalize_point(const GroupParams& g, const MixedRun
     }
     return;
   }
-  // S-map (src/edm.cpp:737-814): weighted normal equations, LDL^T when well
-  // conditioned, else the JacobiSVD restatement the exact path uses.
-  constexpr int n = EA + 1;
-  double mean = 0;
-  for (int j = 0; j < keff; j++)
-    mean = add(mean, cd[j]);
-  mean = dvd(mean, (double)keff);
-  double rel[C + ZCAP];
-  for (int i = 0; i < keff; i++)
-    rel[i] = dvd(cd[i], mean);
-  for (int t = 0; t < g.n_thetas; t++) {
-    const double theta = g.thetas[t];
-    double A[n * n], bv[n], xs[n];
-    // X = [w, w*M(row, .)] and w*target, formed once (same bits as the
-    // reference's X_ls_cj and y_ls, src/edm.cpp:749-772)
-    double X[C + ZCAP][n], yl[C + ZCAP];
-    for (int i = 0; i < keff; i++) {
-      const double w = exp_rn(mul(-theta, rel[i]));
-      X[i][0] = w;
-#pragma unroll
-      for (int j = 1; j < n; j++)
-        X[i][j] = mul(w, g.F[(size_t)rows[i] * EA + j - 1]);
-      yl[i] = mul(w, g.lib_target[rows[i]]);
-    }
-#pragma unroll
-    for (int a = 0; a < n; a++) {
-#pragma unroll
-      for (int b = a; b < n; b++) {
-        double s = 0;
-        for (int i = 0; i < keff; i++)
-          s = add(s, mul(X[i][a], X[i][b]));
-        A[a * n + b] = s;
-        A[b * n + a] = s;
-      }
-      double s = 0;
-      for (int i = 0; i < keff; i++)
-        s = add(s, mul(X[i][a], yl[i]));
-      bv[a] = s;
-    }
-    // The same JacobiSVD restatement as the FP64 form: S-map normal
-    // equations on low-dimensional attractors are routinely ill-conditioned
-    // (cond 1e11..1e15), and the reference's 5*eps*sigma_max truncation then
-    // decides forecasts at the rounding level, so only the identical
-    // operation sequence keeps |delta rho| at zero.
-    double U[n * n], V[n * n], sv[n], tmp[n];
-    svd_solve(A, U, V, sv, tmp, bv, xs, n);
-    double r = xs[0];
-    for (int j = 0; j < EA; j++)
-      r = add(r, mul(y[j], xs[j + 1]));
-    if (g.coeffs && T.save_coeffs && t == g.n_thetas - 1)
-      for (int j = 0; j < n; j++)
-        g.coeffs[(size_t)p * n + j] = fabs(xs[j]) < 1.0e-11 ? MISS : xs[j];
-    g.pred[(size_t)t * g.total_points + p] = r;
+  else {
+    smap_point<EA>(g, p, prow, T.save_coeffs != 0, keff, rows, cd);
   }
 }
 
-// One candidate value for one point: FP32 zeros go to the zero list, other
-// values below the C-th kept one are inserted in (value, index) order.
 template<int C>
 __device__ __forceinline__ void offer(float (&D)[C], int (&I)[C], int& z, int (&zi)[ZCAP], float v, int li)
 {
@@ -301,8 +265,8 @@ __device__ __forceinline__ void offer(float (&D)[C], int (&I)[C], int& z, int (&
   }
 }
 
-template<int EA, int C>
-__global__ void __launch_bounds__(TPB, 2) knn_mixed_kernel(GroupParams g, MixedRun m)
+template<int EA, int C, int ALG>
+__global__ void __launch_bounds__(TPB, ALG == 1 ? 1 : 2) knn_mixed_kernel(GroupParams g, MixedRun m)
 {
   constexpr int S = EA <= 4 ? 4 : 8;  // row stride of the float manifold
   // library rows staged as interleaved pairs: tile[pair][dim] = (row 2i, row 2i+1)
@@ -312,10 +276,10 @@ __global__ void __launch_bounds__(TPB, 2) knn_mixed_kernel(GroupParams g, MixedR
   for (;;) {
     __syncthreads();
     if (tid == 0)
-      s_item = atomicAdd(m.counter, 1);
+      s_item = m.item_begin + atomicAdd(m.counter, 1);
     __syncthreads();
     const int item = s_item;
-    if (item >= m.n_items)
+    if (item >= m.item_end)
       return;
     const int2 it = m.items[item];
     const DevTask T = g.tasks[it.x];
@@ -399,7 +363,7 @@ __global__ void __launch_bounds__(TPB, 2) knn_mixed_kernel(GroupParams g, MixedR
 #pragma unroll
       for (int j = 0; j < ZCAP; j++)
         c.zi[j] = zi0[j];
-      finalize_point<EA, C>(g, m, T, T.point_base + pi0, prow0, c);
+      finalize_point<EA, C, ALG>(g, m, T, T.point_base + pi0, prow0, c);
     }
     if (a1) {
       Cand<C> c;
@@ -412,38 +376,171 @@ __global__ void __launch_bounds__(TPB, 2) knn_mixed_kernel(GroupParams g, MixedR
 #pragma unroll
       for (int j = 0; j < ZCAP; j++)
         c.zi[j] = zi1[j];
-      finalize_point<EA, C>(g, m, T, T.point_base + pi1, prow1, c);
+      finalize_point<EA, C, ALG>(g, m, T, T.point_base + pi1, prow1, c);
     }
   }
 }
 
-template<int EA, int C>
+// S-map forecast of one point from its neighbour rows and FP64 distances,
+// all thetas (src/edm.cpp:737-814); the normal matrix, the rotation
+// accumulators and the right-hand side stay in registers.
+template<int EA>
+__device__ __noinline__ void smap_point(const GroupParams& g, long long p, int prow, bool save, int keff,
+                                        const int* rows, const double* cd)
+{
+  constexpr int n = EA + 1;
+  double y[EA];
+#pragma unroll
+  for (int j = 0; j < EA; j++)
+    y[j] = g.Fp[(size_t)prow * EA + j];
+  double mean = 0;
+  for (int j = 0; j < keff; j++)
+    mean = add(mean, cd[j]);
+  mean = dvd(mean, (double)keff);
+  for (int t = 0; t < g.n_thetas; t++) {
+    const double theta = g.thetas[t];
+    double W[n][n], bv[n], xs[n];
+#pragma unroll
+    for (int a = 0; a < n; a++) {
+      bv[a] = 0;
+#pragma unroll
+      for (int b = 0; b < n; b++)
+        W[a][b] = 0;
+    }
+    for (int i = 0; i < keff; i++) {
+      const double w = exp_rn(mul(-theta, dvd(cd[i], mean)));
+      const int row = rows[i];
+      double xr[n];
+      xr[0] = w;
+#pragma unroll
+      for (int j = 1; j < n; j++)
+        xr[j] = mul(w, g.F[(size_t)row * EA + j - 1]);
+      const double yl = mul(w, g.lib_target[row]);
+#pragma unroll
+      for (int a = 0; a < n; a++) {
+#pragma unroll
+        for (int b = a; b < n; b++)
+          W[a][b] = add(W[a][b], mul(xr[a], xr[b]));
+        bv[a] = add(bv[a], mul(xr[a], yl));
+      }
+    }
+#pragma unroll
+    for (int a = 0; a < n; a++)
+#pragma unroll
+      for (int b = 0; b < a; b++)
+        W[a][b] = W[b][a];
+    svd_solve_n<n>(W, bv, xs);
+    double r = xs[0];
+#pragma unroll
+    for (int j = 0; j < EA; j++)
+      r = add(r, mul(y[j], xs[j + 1]));
+    if (g.coeffs && save && t == g.n_thetas - 1) {
+#pragma unroll
+      for (int j = 0; j < n; j++)
+        g.coeffs[(size_t)p * n + j] = fabs(xs[j]) < 1.0e-11 ? MISS : xs[j];
+    }
+    g.pred[(size_t)t * g.total_points + p] = r;
+  }
+}
+
+template<int EA>
+__global__ void __launch_bounds__(128) smap_lists_kernel(GroupParams g, MixedRun m)
+{
+  constexpr int n = EA + 1;
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= *m.l_count)
+    return;
+  const long long p = m.l_point[q];
+  const int prow = m.l_prow[q];
+  const int tk = m.l_task[q];
+  const bool save = (tk >> 30) & 1;
+  const int keff = m.l_k[q];
+  const int* rows = m.l_rows + (size_t)q * m.kslots;
+  const double* cd = m.l_dist + (size_t)q * m.kslots;
+  double y[EA];
+#pragma unroll
+  for (int j = 0; j < EA; j++)
+    y[j] = g.Fp[(size_t)prow * EA + j];
+  // src/edm.cpp:744-745: w = exp(-theta * d / mean(d))
+  double mean = 0;
+  for (int j = 0; j < keff; j++)
+    mean = add(mean, cd[j]);
+  mean = dvd(mean, (double)keff);
+  for (int t = 0; t < g.n_thetas; t++) {
+    const double theta = g.thetas[t];
+    double W[n][n], bv[n], xs[n];
+#pragma unroll
+    for (int a = 0; a < n; a++) {
+      bv[a] = 0;
+#pragma unroll
+      for (int b = 0; b < n; b++)
+        W[a][b] = 0;
+    }
+    // X^T X and X^T y summed over the neighbours in order: each entry sees the
+    // same additions as the reference's products (src/edm.cpp:749-782)
+    for (int i = 0; i < keff; i++) {
+      const double w = exp_rn(mul(-theta, dvd(cd[i], mean)));
+      const int row = rows[i];
+      double xr[n];
+      xr[0] = w;
+#pragma unroll
+      for (int j = 1; j < n; j++)
+        xr[j] = mul(w, g.F[(size_t)row * EA + j - 1]);
+      const double yl = mul(w, g.lib_target[row]);
+#pragma unroll
+      for (int a = 0; a < n; a++) {
+#pragma unroll
+        for (int b = a; b < n; b++)
+          W[a][b] = add(W[a][b], mul(xr[a], xr[b]));
+        bv[a] = add(bv[a], mul(xr[a], yl));
+      }
+    }
+#pragma unroll
+    for (int a = 0; a < n; a++)
+#pragma unroll
+      for (int b = 0; b < a; b++)
+        W[a][b] = W[b][a];
+    svd_solve_n<n>(W, bv, xs);
+    double r = xs[0];
+#pragma unroll
+    for (int j = 0; j < EA; j++)
+      r = add(r, mul(y[j], xs[j + 1]));
+    if (g.coeffs && save && t == g.n_thetas - 1) {
+#pragma unroll
+      for (int j = 0; j < n; j++)
+        g.coeffs[(size_t)p * n + j] = fabs(xs[j]) < 1.0e-11 ? MISS : xs[j];
+    }
+    g.pred[(size_t)t * g.total_points + p] = r;
+  }
+}
+
+template<int EA, int C, int ALG>
 void launch_one(const GroupParams& g, const MixedRun& m, int num_sms, cudaStream_t s)
 {
   int per_sm = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, knn_mixed_kernel<EA, C>, TPB, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, knn_mixed_kernel<EA, C, ALG>, TPB, 0);
   if (per_sm < 1)
     per_sm = 1;
   long long blocks = (long long)num_sms * per_sm;
-  if (blocks > m.n_items)
-    blocks = m.n_items;
+  if (blocks > m.item_end - m.item_begin)
+    blocks = m.item_end - m.item_begin;
   if (blocks < 1)
     blocks = 1;
-  knn_mixed_kernel<EA, C><<<(int)blocks, TPB, 0, s>>>(g, m);
+  knn_mixed_kernel<EA, C, ALG><<<(int)blocks, TPB, 0, s>>>(g, m);
 }
 
-template<int C>
+template<int C, int ALG>
 void launch_c(const GroupParams& g, const MixedRun& m, int num_sms, cudaStream_t s)
 {
   switch (g.Ea) {
-    case 1: launch_one<1, C>(g, m, num_sms, s); break;
-    case 2: launch_one<2, C>(g, m, num_sms, s); break;
-    case 3: launch_one<3, C>(g, m, num_sms, s); break;
-    case 4: launch_one<4, C>(g, m, num_sms, s); break;
-    case 5: launch_one<5, C>(g, m, num_sms, s); break;
-    case 6: launch_one<6, C>(g, m, num_sms, s); break;
-    case 7: launch_one<7, C>(g, m, num_sms, s); break;
-    case 8: launch_one<8, C>(g, m, num_sms, s); break;
+    case 1: launch_one<1, C, ALG>(g, m, num_sms, s); break;
+    case 2: launch_one<2, C, ALG>(g, m, num_sms, s); break;
+    case 3: launch_one<3, C, ALG>(g, m, num_sms, s); break;
+    case 4: launch_one<4, C, ALG>(g, m, num_sms, s); break;
+    case 5: launch_one<5, C, ALG>(g, m, num_sms, s); break;
+    case 6: launch_one<6, C, ALG>(g, m, num_sms, s); break;
+    case 7: launch_one<7, C, ALG>(g, m, num_sms, s); break;
+    case 8: launch_one<8, C, ALG>(g, m, num_sms, s); break;
     default: break;
   }
 }
@@ -460,14 +557,40 @@ __global__ void center_kernel(const double* F, long long n, int Ea, const double
 
 } // namespace
 
+void launch_smap_lists(const GroupParams& g, const MixedRun& m, int num_sms, cudaStream_t s)
+{
+  (void)num_sms;
+  const int blocks = (m.l_cap + 127) / 128;
+  if (blocks <= 0)
+    return;
+  switch (g.Ea) {
+    case 1: smap_lists_kernel<1><<<blocks, 128, 0, s>>>(g, m); break;
+    case 2: smap_lists_kernel<2><<<blocks, 128, 0, s>>>(g, m); break;
+    case 3: smap_lists_kernel<3><<<blocks, 128, 0, s>>>(g, m); break;
+    case 4: smap_lists_kernel<4><<<blocks, 128, 0, s>>>(g, m); break;
+    case 5: smap_lists_kernel<5><<<blocks, 128, 0, s>>>(g, m); break;
+    case 6: smap_lists_kernel<6><<<blocks, 128, 0, s>>>(g, m); break;
+    case 7: smap_lists_kernel<7><<<blocks, 128, 0, s>>>(g, m); break;
+    case 8: smap_lists_kernel<8><<<blocks, 128, 0, s>>>(g, m); break;
+    default: break;
+  }
+}
+
 void launch_knn_mixed(const GroupParams& g, const MixedRun& m, int C, int num_sms, cudaStream_t s)
 {
-  if (m.n_items <= 0)
+  if (m.item_end <= m.item_begin)
     return;
-  if (C <= 8)
-    launch_c<8>(g, m, num_sms, s);
-  else
-    launch_c<16>(g, m, num_sms, s);
+  if (g.algorithm == 1) {
+    if (C <= 8)
+      launch_c<8, 1>(g, m, num_sms, s);
+    else
+      launch_c<16, 1>(g, m, num_sms, s);
+  } else {
+    if (C <= 8)
+      launch_c<8, 0>(g, m, num_sms, s);
+    else
+      launch_c<16, 0>(g, m, num_sms, s);
+  }
 }
 
 void center_to_f32(const double* F, long long n, int Ea, const double* center, float* F32, int stride,

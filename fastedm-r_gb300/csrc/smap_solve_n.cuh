@@ -1,0 +1,208 @@
+// The JacobiSVD restatement of smap_solve.cuh for a compile-time size N,
+// fully unrolled so the work matrix and both rotation accumulators live in
+// registers.  Every floating-point operation and its order are those of
+// svd_solve(): the results are the same bits.
+#pragma once
+
+#include <cfloat>
+
+#include "smap_solve.cuh"
+
+namespace fedm {
+
+template<int N>
+__device__ __forceinline__ void svd_solve_n(double (&W)[N][N], const double (&b)[N], double (&x)[N])
+{
+  const double tiny = DBL_MIN, eps = DBL_EPSILON, precision = 2 * DBL_EPSILON;
+  double scale = 0;
+#pragma unroll
+  for (int i = 0; i < N; i++)
+#pragma unroll
+    for (int j = 0; j < N; j++)
+      scale = fmax(scale, fabs(W[i][j]));
+  if (!isfinite(scale)) {
+#pragma unroll
+    for (int i = 0; i < N; i++)
+      x[i] = 0;
+    return;
+  }
+  if (scale == 0)
+    scale = 1;
+  double U[N][N], V[N][N];
+#pragma unroll
+  for (int i = 0; i < N; i++)
+#pragma unroll
+    for (int j = 0; j < N; j++) {
+      W[i][j] = dvd(W[i][j], scale);
+      U[i][j] = i == j ? 1.0 : 0.0;
+      V[i][j] = i == j ? 1.0 : 0.0;
+    }
+  double maxDiag = 0;
+#pragma unroll
+  for (int i = 0; i < N; i++)
+    maxDiag = fmax(maxDiag, fabs(W[i][i]));
+  bool finished = false;
+  int sweeps = 0;
+  while (!finished && sweeps < 100) {
+    finished = true;
+    sweeps++;
+#pragma unroll
+    for (int p = 1; p < N; p++) {
+#pragma unroll
+      for (int q = 0; q < p; q++) {
+        const double threshold = fmax(tiny, mul(precision, maxDiag));
+        if (fabs(W[p][q]) > threshold || fabs(W[q][p]) > threshold) {
+          finished = false;
+          // real_2x2_jacobi_svd on rows/cols p, q
+          const double m00 = W[p][p], m01 = W[p][q], m10 = W[q][p], m11 = W[q][q];
+          double r1c, r1s;
+          const double t = add(m00, m11), d = sub(m10, m01);
+          if (fabs(d) < tiny) {
+            r1s = 0;
+            r1c = 1;
+          } else {
+            const double u = dvd(t, d);
+            const double tmp = __dsqrt_rn(add(1.0, mul(u, u)));
+            r1s = dvd(1.0, tmp);
+            r1c = dvd(u, tmp);
+          }
+          const double n00 = add(mul(r1c, m00), mul(r1s, m10));
+          const double n01 = add(mul(r1c, m01), mul(r1s, m11));
+          const double n11 = add(mul(-r1s, m01), mul(r1c, m11));
+          const double deno = mul(2.0, fabs(n01));
+          double jrc, jrs;
+          if (deno < tiny) {
+            jrc = 1;
+            jrs = 0;
+          } else {
+            const double tau = dvd(sub(n00, n11), deno);
+            const double w = __dsqrt_rn(add(mul(tau, tau), 1.0));
+            const double tt = tau > 0 ? dvd(1.0, add(tau, w)) : dvd(1.0, sub(tau, w));
+            const double sign_t = tt > 0 ? 1.0 : -1.0;
+            const double nn = dvd(1.0, __dsqrt_rn(add(mul(tt, tt), 1.0)));
+            jrs = mul(mul(mul(-sign_t, dvd(n01, fabs(n01))), fabs(tt)), nn);
+            jrc = nn;
+          }
+          const double jtc = jrc, jts = -jrs;
+          const double jlc = sub(mul(r1c, jtc), mul(r1s, jts));
+          const double jls = add(mul(r1c, jts), mul(r1s, jtc));
+          // W.applyOnTheLeft(p, q, jl)
+#pragma unroll
+          for (int i = 0; i < N; i++) {
+            const double xv = W[p][i], yv = W[q][i];
+            W[p][i] = add(mul(jlc, xv), mul(jls, yv));
+            W[q][i] = add(mul(-jls, xv), mul(jlc, yv));
+          }
+          // U.applyOnTheRight(p, q, jl^T): rotation (c, -s) applied transposed
+          {
+            const double c = jlc, s = jls;  // transpose of (jlc, -jls)
+#pragma unroll
+            for (int i = 0; i < N; i++) {
+              const double xv = U[i][p], yv = U[i][q];
+              U[i][p] = add(mul(c, xv), mul(s, yv));
+              U[i][q] = add(mul(-s, xv), mul(c, yv));
+            }
+          }
+          // W.applyOnTheRight(p, q, jr) and V.applyOnTheRight(p, q, jr)
+          {
+            const double c = jrc, s = -jrs;
+#pragma unroll
+            for (int i = 0; i < N; i++) {
+              const double xv = W[i][p], yv = W[i][q];
+              W[i][p] = add(mul(c, xv), mul(s, yv));
+              W[i][q] = add(mul(-s, xv), mul(c, yv));
+            }
+#pragma unroll
+            for (int i = 0; i < N; i++) {
+              const double xv = V[i][p], yv = V[i][q];
+              V[i][p] = add(mul(c, xv), mul(s, yv));
+              V[i][q] = add(mul(-s, xv), mul(c, yv));
+            }
+          }
+          maxDiag = fmax(maxDiag, fmax(fabs(W[p][p]), fabs(W[q][q])));
+        }
+      }
+    }
+  }
+  double sv[N];
+#pragma unroll
+  for (int i = 0; i < N; i++) {
+    const double a = W[i][i];
+    sv[i] = fabs(a);
+    if (a < 0) {
+#pragma unroll
+      for (int r = 0; r < N; r++)
+        U[r][i] = -U[r][i];
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < N; i++)
+    sv[i] = mul(sv[i], scale);
+  int nonzero = N;
+  bool stop = false;
+#pragma unroll
+  for (int i = 0; i < N; i++) {
+    if (!stop) {
+      int pos = i;
+      double mx = sv[i];
+#pragma unroll
+      for (int j = i + 1; j < N; j++)
+        if (sv[j] > mx) {
+          mx = sv[j];
+          pos = j;
+        }
+      if (mx == 0) {
+        nonzero = i;
+        stop = true;
+      } else if (pos != i) {
+#pragma unroll
+        for (int j = i + 1; j < N; j++) {
+          if (pos == j) {
+            const double s0 = sv[i];
+            sv[i] = sv[j];
+            sv[j] = s0;
+#pragma unroll
+            for (int r = 0; r < N; r++) {
+              const double u0 = U[r][i];
+              U[r][i] = U[r][j];
+              U[r][j] = u0;
+              const double v0 = V[r][i];
+              V[r][i] = V[r][j];
+              V[r][j] = v0;
+            }
+          }
+        }
+      }
+    }
+  }
+  const double thr = fmax(mul(sv[0], mul((double)(N > 1 ? N : 1), eps)), tiny);
+  int rank = 0;
+#pragma unroll
+  for (int i = 0; i < N; i++)
+    if (i < nonzero && !(sv[i] < thr))
+      rank = i + 1;
+  // rank() walks down from nonzero-1 while sv < thr; with sv sorted in
+  // decreasing order that is the count of leading entries >= thr
+  double tmp[N];
+#pragma unroll
+  for (int cc = 0; cc < N; cc++) {
+    if (cc < rank) {
+      double s = 0;
+#pragma unroll
+      for (int r = 0; r < N; r++)
+        s = add(s, mul(U[r][cc], b[r]));
+      tmp[cc] = mul(dvd(1.0, sv[cc]), s);
+    }
+  }
+#pragma unroll
+  for (int r = 0; r < N; r++) {
+    double s = 0;
+#pragma unroll
+    for (int cc = 0; cc < N; cc++)
+      if (cc < rank)
+        s = add(s, mul(V[r][cc], tmp[cc]));
+    x[r] = s;
+  }
+}
+
+} // namespace fedm

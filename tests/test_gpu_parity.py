@@ -86,15 +86,10 @@ def _task_pair(ctx, a, lib, pred, E, k, **kw):
     assert np.array_equal(g["nn_idx"], o["nn_idx"]), "neighbour indices differ"
     assert np.array_equal(g["nn_dist"].view(np.int64), o["nn_dist"].view(np.int64)), "neighbour distances differ"
     assert np.array_equal(g["rc"], o["rc"])
-    if ctx.precision == fedm.PRECISION_FP64:
-        # same operations in the same order on both sides: identical bits
-        assert np.array_equal(g["predictions"], o["predictions"]), "forecasts differ"
-        assert np.array_equal(g["coeffs"], o["coeffs"]), "coefficients differ"
-    else:
-        # mixed form: same neighbours; S-map systems solved by LDL^T when well
-        # conditioned (relative error ~ cond * 1e-16), else the same SVD
-        _close(g["predictions"], o["predictions"], "predictions", rtol=1e-7, atol=1e-9)
-        _close(g["coeffs"], o["coeffs"], "coeffs", rtol=1e-6, atol=1e-8)
+    # both forms: the same neighbours (bit-exact), then the same FP64
+    # operations in the same order as the oracle: identical bits
+    assert np.array_equal(g["predictions"], o["predictions"]), "forecasts differ"
+    assert np.array_equal(g["coeffs"], o["coeffs"]), "coefficients differ"
     _close(g["stats_rho"], o["stats_rho"], "rho")
     _close(g["stats_mae"], o["stats_mae"], "mae")
     return g, o
