@@ -87,6 +87,9 @@ __device__ __forceinline__ double fp64_sq(const GroupParams& g, int row, const d
 template<int EA>
 __device__ __noinline__ void smap_point(const GroupParams& g, long long p, int prow, bool save, int keff,
                                         const int* rows, const double* cd);
+template<int EA>
+__device__ __noinline__ void smap_point_local(const GroupParams& g, long long p, int prow, bool save, int keff,
+                                              const int* rows, const double* cd);
 
 // Candidates of one point, handed to the out-of-line FP64 stage.
 template<int C>
@@ -247,7 +250,7 @@ __device__ __noinline__ void finalize_point(const GroupParams& g, const MixedRun
     return;
   }
   else {
-    smap_point<EA>(g, p, prow, T.save_coeffs != 0, keff, rows, cd);
+    smap_point_local<EA>(g, p, prow, T.save_coeffs != 0, keff, rows, cd);
   }
 }
 
@@ -266,7 +269,7 @@ __device__ __forceinline__ void offer(float (&D)[C], int (&I)[C], int& z, int (&
 }
 
 template<int EA, int C, int ALG>
-__global__ void __launch_bounds__(TPB, ALG == 1 ? 1 : 2) knn_mixed_kernel(GroupParams g, MixedRun m)
+__global__ void __launch_bounds__(TPB, 2) knn_mixed_kernel(GroupParams g, MixedRun m)
 {
   constexpr int S = EA <= 4 ? 4 : 8;  // row stride of the float manifold
   // library rows staged as interleaved pairs: tile[pair][dim] = (row 2i, row 2i+1)
@@ -436,6 +439,62 @@ __device__ __noinline__ void smap_point(const GroupParams& g, long long p, int p
       r = add(r, mul(y[j], xs[j + 1]));
     if (g.coeffs && save && t == g.n_thetas - 1) {
 #pragma unroll
+      for (int j = 0; j < n; j++)
+        g.coeffs[(size_t)p * n + j] = fabs(xs[j]) < 1.0e-11 ? MISS : xs[j];
+    }
+    g.pred[(size_t)t * g.total_points + p] = r;
+  }
+}
+
+// The same forecast with the solver's matrices in per-thread local memory;
+// used inside the scan kernel, whose register budget (two 256-thread CTAs
+// per SM) leaves no room for them.  Identical operations and bits.
+template<int EA>
+__device__ __noinline__ void smap_point_local(const GroupParams& g, long long p, int prow, bool save, int keff,
+                                              const int* rows, const double* cd)
+{
+  constexpr int n = EA + 1;
+  double y[EA];
+#pragma unroll
+  for (int j = 0; j < EA; j++)
+    y[j] = g.Fp[(size_t)prow * EA + j];
+  double mean = 0;
+  for (int j = 0; j < keff; j++)
+    mean = add(mean, cd[j]);
+  mean = dvd(mean, (double)keff);
+  for (int t = 0; t < g.n_thetas; t++) {
+    const double theta = g.thetas[t];
+    double W[n * n], bv[n], xs[n], U[n * n], V[n * n], sv[n], tmp[n];
+    for (int e = 0; e < n * n; e++)
+      W[e] = 0;
+    for (int a = 0; a < n; a++)
+      bv[a] = 0;
+    for (int i = 0; i < keff; i++) {
+      const double w = exp_rn(mul(-theta, dvd(cd[i], mean)));
+      const int row = rows[i];
+      double xr[n];
+      xr[0] = w;
+#pragma unroll
+      for (int j = 1; j < n; j++)
+        xr[j] = mul(w, g.F[(size_t)row * EA + j - 1]);
+      const double yl = mul(w, g.lib_target[row]);
+#pragma unroll
+      for (int a = 0; a < n; a++) {
+#pragma unroll
+        for (int b = a; b < n; b++)
+          W[a * n + b] = add(W[a * n + b], mul(xr[a], xr[b]));
+        bv[a] = add(bv[a], mul(xr[a], yl));
+      }
+    }
+    for (int a = 0; a < n; a++)
+      for (int b = 0; b < a; b++)
+        W[a * n + b] = W[b * n + a];
+    svd_solve(W, U, V, sv, tmp, bv, xs, n);
+    double r = xs[0];
+#pragma unroll
+    for (int j = 0; j < EA; j++)
+      r = add(r, mul(y[j], xs[j + 1]));
+    if (g.coeffs && save && t == g.n_thetas - 1) {
       for (int j = 0; j < n; j++)
         g.coeffs[(size_t)p * n + j] = fabs(xs[j]) < 1.0e-11 ? MISS : xs[j];
     }
