@@ -24,6 +24,7 @@ CU_FLAGS = {
     "kernels_exact.cu": ["--fmad=false"],
     "kernels_util.cu": [],
     "kernels_mixed.cu": [],
+    "static_entry.cu": [],
 }
 CPP = ["host.cpp", "engine.cpp", "capi.cpp"]
 

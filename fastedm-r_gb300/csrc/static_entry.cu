@@ -1,0 +1,207 @@
+// fedm_predict_static: one neighbour search + forecast on caller-owned device
+// buffers that allocates no device memory.
+//
+// Some callers cannot let a library allocate GPU memory.  Embedding hosts that
+// hand the process a fixed device-memory budget (an R session or a service
+// whose allocator owns the GPU) see an unplanned cudaMalloc fail or fragment
+// their pool.  Latency-sensitive pipelines avoid cudaMalloc/cudaFree because
+// both can synchronise the device and stall unrelated streams.  This entry
+// point serves them: its working memory (neighbour lists, statuses, index
+// lists, the task descriptor) lives in one file-scope __device__ array of
+// fixed size, FEDM_STATIC_SCRATCH_BYTES, that every GPU which loads the
+// library holds until the process exits.
+//
+// The array is shared by every call on a device and keeps the previous
+// call's contents; each call re-initialises everything it reads.  Calls that
+// overlap on the GPU (on two streams, or from two host threads) race on it
+// and must be serialised by the caller.
+#include <cuda_runtime.h>
+
+#include <climits>
+#include <cstdio>
+#include <mutex>
+
+#include "../../include/fastedm_gb300.h"
+#include "kernels.h"
+
+namespace fedm {
+
+namespace {
+
+constexpr size_t kScratchBytes = (size_t)FEDM_STATIC_SCRATCH_BYTES;
+
+__device__ __align__(256) unsigned char g_static_scratch[kScratchBytes];
+
+// Device address of g_static_scratch per device, looked up once per device
+// with that device current (in host code the symbol name is only a handle).
+std::mutex g_mu;
+void* g_addr[64] = {};
+
+void* scratch_address(int device, int& rc)
+{
+  std::lock_guard<std::mutex> lock(g_mu);
+  if (device < 0 || device >= 64) {
+    rc = FEDM_UNKNOWN_ERROR;
+    return nullptr;
+  }
+  if (!g_addr[device]) {
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_static_scratch);
+    if (e != cudaSuccess || !p) {
+      std::fprintf(stderr, "fedm_predict_static: cudaGetSymbolAddress failed: %s\n", cudaGetErrorString(e));
+      rc = FEDM_UNKNOWN_ERROR;
+      return nullptr;
+    }
+    g_addr[device] = p;
+  }
+  rc = FEDM_SUCCESS;
+  return g_addr[device];
+}
+
+__global__ void iota_kernel(int* a, int n, int* b, int m)
+{
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n || i < m; i += gridDim.x * blockDim.x) {
+    if (i < n)
+      a[i] = i;
+    if (i < m)
+      b[i] = i;
+  }
+}
+
+__global__ void fill_missing_kernel(double* p, long long n, int* kused, int n_pred)
+{
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    p[i] = 1.0e+100;
+  if (kused)
+    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n_pred;
+         i += (long long)gridDim.x * blockDim.x)
+      kused[i] = INT_MIN;
+}
+
+size_t align256(size_t v)
+{
+  return (v + 255) & ~(size_t)255;
+}
+
+} // namespace
+
+} // namespace fedm
+
+extern "C" int fedm_predict_static(const double* lib_manifold, const double* lib_targets, int n_lib,
+                                   const double* pred_manifold, int n_pred, int e_actual, int k, int algorithm,
+                                   const double* thetas, int n_thetas, double* predictions, int* kused,
+                                   void* stream)
+{
+  using namespace fedm;
+  if (!lib_manifold || !lib_targets || !pred_manifold || !thetas || !predictions || n_lib < 0 || n_pred < 0 ||
+      e_actual < 1 || n_thetas < 1 || (algorithm != 0 && algorithm != 1) || k < 1)
+    return FEDM_UNKNOWN_ERROR;
+  if (n_lib > FEDM_STATIC_MAX_LIB || n_pred > FEDM_STATIC_MAX_PRED || k > FEDM_STATIC_MAX_K ||
+      e_actual > FEDM_STATIC_MAX_E || n_thetas > FEDM_STATIC_MAX_THETAS) {
+    std::fprintf(stderr,
+                 "fedm_predict_static: size beyond the static scratch limits (n_lib %d/%d, n_pred %d/%d, k %d/%d, "
+                 "e_actual %d/%d, n_thetas %d/%d)\n",
+                 n_lib, FEDM_STATIC_MAX_LIB, n_pred, FEDM_STATIC_MAX_PRED, k, FEDM_STATIC_MAX_K, e_actual,
+                 FEDM_STATIC_MAX_E, n_thetas, FEDM_STATIC_MAX_THETAS);
+    return FEDM_NOT_IMPLEMENTED;
+  }
+  if (n_pred == 0)
+    return FEDM_SUCCESS;
+  int device = 0;
+  if (cudaGetDevice(&device) != cudaSuccess)
+    return FEDM_UNKNOWN_ERROR;
+  int rc = 0;
+  unsigned char* base = (unsigned char*)scratch_address(device, rc);
+  if (!base)
+    return rc;
+  int num_sms = 1;
+  cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, device);
+  cudaStream_t s = (cudaStream_t)stream;
+
+  // carve the scratch: task, counters, thetas, index lists, neighbour lists
+  size_t off = 0;
+  auto take = [&](size_t bytes) {
+    unsigned char* p = base + off;
+    off += align256(bytes);
+    return p;
+  };
+  DevTask* d_task = (DevTask*)take(sizeof(DevTask));
+  int* d_flags = (int*)take(4 * sizeof(int));  // task rc, kmin, kmax, error flag
+  double* d_thetas = (double*)take((size_t)n_thetas * 8);
+  int* d_lib_rows = (int*)take((size_t)(n_lib > 0 ? n_lib : 1) * 4);
+  int* d_pred_rows = (int*)take((size_t)n_pred * 4);
+  int* d_count = (int*)take((size_t)n_pred * 4);
+  int* d_status = (int*)take((size_t)n_pred * 4);
+  int* d_nn_idx = (int*)take((size_t)n_pred * k * 4);
+  double* d_nn_dist = (double*)take((size_t)n_pred * k * 8);
+  double* d_solver = (double*)take(8);
+  if (off > kScratchBytes)
+    return FEDM_NOT_IMPLEMENTED;  // cannot happen within the stated limits
+
+  DevTask task{};
+  task.point_base = 0;
+  task.lib_off = 0;
+  task.n_lib = n_lib;
+  task.pred_off = 0;
+  task.n_pred = n_pred;
+  task.k = k;
+  task.k_req = k;
+  task.task = 0;
+  task.save_coeffs = 0;
+  task.all_mode = 0;
+  task.mixed = 0;
+  const int init_flags[4] = { 0, INT_MAX, INT_MIN, 0 };
+  if (cudaMemcpyAsync(d_task, &task, sizeof(task), cudaMemcpyHostToDevice, s) != cudaSuccess ||
+      cudaMemcpyAsync(d_flags, init_flags, sizeof(init_flags), cudaMemcpyHostToDevice, s) != cudaSuccess ||
+      cudaMemcpyAsync(d_thetas, thetas, (size_t)n_thetas * 8, cudaMemcpyHostToDevice, s) != cudaSuccess)
+    return FEDM_UNKNOWN_ERROR;
+  const int m = n_lib > n_pred ? n_lib : n_pred;
+  iota_kernel<<<(m + 255) / 256 < 1024 ? (m + 255) / 256 : 1024, 256, 0, s>>>(d_lib_rows, n_lib, d_pred_rows,
+                                                                              n_pred);
+  // forecasts start as MISSING like edm_task's buffers (src/edm.cpp:345-350)
+  const long long np = (long long)n_pred * n_thetas;
+  fill_missing_kernel<<<(int)((np + 255) / 256 < 1024 ? (np + 255) / 256 : 1024), 256, 0, s>>>(predictions, np,
+                                                                                          kused, n_pred);
+
+  GroupParams g{};
+  g.F = lib_manifold;
+  g.Fp = pred_manifold;
+  g.lib_target = lib_targets;
+  g.pred_target = lib_targets;
+  // the time tables are read only by the past-only rule, which is off here;
+  // they still point at arrays long enough for every row index used
+  g.lib_target_time = lib_targets;    // n_lib entries, indexed by library row
+  g.point_time = pred_manifold;       // >= n_pred entries, indexed by prediction row
+  g.lib_rows = d_lib_rows;
+  g.pred_rows = d_pred_rows;
+  g.tasks = d_task;
+  g.n_tasks = 1;
+  g.Ea = e_actual;
+  g.n_thetas = n_thetas;
+  g.thetas = d_thetas;
+  g.algorithm = algorithm;
+  g.force_compute = 1;
+  g.total_points = n_pred;
+  g.pred = predictions;
+  g.kused = kused;
+  g.task_rc = d_flags;
+  g.task_kmin = d_flags + 1;
+  g.task_kmax = d_flags + 2;
+  g.err_flag = d_flags + 3;
+  ChunkBuffers c{};
+  c.p_begin = 0;
+  c.p_end = n_pred;
+  c.kcap = k;
+  c.nn_idx = d_nn_idx;
+  c.nn_dist = d_nn_dist;
+  c.nn_count = d_count;
+  c.status = d_status;
+  c.scratch = d_solver;
+  c.scratch_doubles = 1;
+  launch_knn_exact(g, c, num_sms, s);
+  if (algorithm == 0)
+    launch_simplex_nn(g, c, s);
+  else
+    launch_smap_nn(g, c, num_sms, s);
+  return cudaGetLastError() == cudaSuccess ? FEDM_SUCCESS : FEDM_UNKNOWN_ERROR;
+}

@@ -206,6 +206,44 @@ int fedm_host_mt_real2(unsigned long long seed, long long count, double* out);
 int fedm_host_plan(const fedm_args* args, int max_tasks, int* n_tasks, int* task_E, int* task_k, int* task_library,
                    int* task_copredict, unsigned char* lib_masks, unsigned char* pred_masks);
 
+/* Allocation-free prediction for one task on caller-owned device buffers.
+ * No counterpart in the reference: it exists for callers that cannot let a
+ * library allocate GPU memory -- hosts that hand the process a fixed device
+ * memory budget (the allocator belongs to someone else, so an unplanned
+ * cudaMalloc fails or fragments it) and latency-sensitive pipelines that
+ * avoid cudaMalloc/cudaFree because both can synchronise the device.
+ *
+ * Inputs (device pointers): lib_manifold [n_lib x e_actual] and lib_targets
+ * [n_lib] (library rows whose target is observed, as edm_task's M),
+ * pred_manifold [n_pred x e_actual]; thetas is a HOST array of n_thetas.
+ * Outputs (device pointers): predictions [n_thetas x n_pred] (theta-major,
+ * MISSING = 1e100 where no forecast is made), kused [n_pred] (may be NULL).
+ * algorithm 0 simplex, 1 S-map; 1 <= k; exact FP64 path, L2 distance, no
+ * missing values, panels or past-only rule; work is queued on `stream` (a
+ * cudaStream_t, NULL = legacy default stream) and the call returns before it
+ * finishes.
+ *
+ * Working memory is one file-scope __device__ array of
+ * FEDM_STATIC_SCRATCH_BYTES (32 MiB) that every GPU loading the library holds
+ * until exit.  Limits: n_lib <= FEDM_STATIC_MAX_LIB, n_pred <=
+ * FEDM_STATIC_MAX_PRED, k <= FEDM_STATIC_MAX_K, e_actual <= FEDM_STATIC_MAX_E,
+ * n_thetas <= FEDM_STATIC_MAX_THETAS; larger requests return
+ * FEDM_NOT_IMPLEMENTED with a message on stderr.  The first call on a device
+ * looks the array's device address up (cudaGetSymbolAddress) with that device
+ * current; make that first call before any stream capture.  All calls on a
+ * device share the array and it keeps the last call's contents (each call
+ * re-initialises what it reads): calls that overlap on the GPU race and must
+ * be serialised by the caller. */
+#define FEDM_STATIC_SCRATCH_BYTES (32 << 20)
+#define FEDM_STATIC_MAX_LIB (1 << 20)
+#define FEDM_STATIC_MAX_PRED 65536
+#define FEDM_STATIC_MAX_K 32
+#define FEDM_STATIC_MAX_E 7
+#define FEDM_STATIC_MAX_THETAS 64
+int fedm_predict_static(const double* lib_manifold, const double* lib_targets, int n_lib,
+                        const double* pred_manifold, int n_pred, int e_actual, int k, int algorithm,
+                        const double* thetas, int n_thetas, double* predictions, int* kused, void* stream);
+
 /* Measured arithmetic peak of this GPU in TFLOP/s (2 flops per fused
  * multiply-add): kind 0 FP32 FFMA, 1 FP64 DFMA, 2 packed FP32 FFMA2.  A
  * diagnostic for roofline fractions; it has no counterpart in the reference. */
