@@ -25,6 +25,7 @@ CU_FLAGS = {
     "kernels_util.cu": [],
     "kernels_mixed.cu": [],
     "static_entry.cu": [],
+    "kernels_adjoint.cu": [],
 }
 CPP = ["host.cpp", "engine.cpp", "capi.cpp"]
 

@@ -205,6 +205,31 @@ int fedm_host_plan(const fedm_args* args, int max_tasks, int* n_tasks, int* task
   });
 }
 
+int fedm_smap_fwd(fedm_ctx* ctx, const double* lib_manifold, const double* lib_targets, int n_lib,
+                  const double* pred_manifold, const double* pred_targets, int n_pred, int e_actual, double theta,
+                  const double* w, double* mse, double* predictions)
+{
+  if (!ctx || !lib_manifold || !lib_targets || !pred_manifold || !pred_targets || !w || !mse)
+    return FEDM_UNKNOWN_ERROR;
+  return guarded(ctx, [&] {
+    return fedm::smap_grad(*ctx->c, lib_manifold, lib_targets, n_lib, pred_manifold, pred_targets, n_pred, e_actual,
+                           theta, w, mse, predictions, nullptr, nullptr);
+  });
+}
+
+int fedm_smap_bwd(fedm_ctx* ctx, const double* lib_manifold, const double* lib_targets, int n_lib,
+                  const double* pred_manifold, const double* pred_targets, int n_pred, int e_actual, double theta,
+                  const double* w, double* mse, double* dmse_dtheta, double* dmse_dw)
+{
+  if (!ctx || !lib_manifold || !lib_targets || !pred_manifold || !pred_targets || !w || !mse || !dmse_dtheta ||
+      !dmse_dw)
+    return FEDM_UNKNOWN_ERROR;
+  return guarded(ctx, [&] {
+    return fedm::smap_grad(*ctx->c, lib_manifold, lib_targets, n_lib, pred_manifold, pred_targets, n_pred, e_actual,
+                           theta, w, mse, nullptr, dmse_dtheta, dmse_dw);
+  });
+}
+
 int fedm_measure_peak(fedm_ctx* ctx, int kind, double* tflops)
 {
   if (!ctx || !tflops || kind < 0 || kind > 2)

@@ -979,6 +979,87 @@ CommandResult run_command(Context& ctx, const fedm_args& a)
   return R;
 }
 
+// ------------------------------------------------------ differentiable S-map
+int smap_grad(Context& ctx, const double* lib, const double* lib_t, int n_lib, const double* pred,
+              const double* pred_t, int n_pred, int e_actual, double theta, const double* w, double* mse,
+              double* predictions, double* dtheta, double* dw)
+{
+  if (e_actual < 1 || e_actual > 8)
+    throw Error{ RC_NOT_IMPLEMENTED, "differentiable S-map supports 1 <= E_actual <= 8" };
+  if (n_lib < 1 || n_pred < 1)
+    throw Error{ RC_UNKNOWN_ERROR, "empty library or prediction set" };
+  ctx.timing = fedm_timing{};
+  const double t0 = now_ms();
+  ck(cudaSetDevice(ctx.device), "cudaSetDevice");
+  cudaStream_t s = ctx.stream;
+  const size_t E = (size_t)e_actual;
+  AdjointParams a{};
+  double* d_lib = (double*)ctx.buf("adj_lib", (size_t)n_lib * E * 8);
+  double* d_lt = (double*)ctx.buf("adj_lib_t", (size_t)n_lib * 8);
+  double* d_pred = (double*)ctx.buf("adj_pred", (size_t)n_pred * E * 8);
+  double* d_pt = (double*)ctx.buf("adj_pred_t", (size_t)n_pred * 8);
+  double* d_w = (double*)ctx.buf("adj_w", E * 8);
+  double* d_out = (double*)ctx.buf("adj_out", (size_t)n_pred * (E + 3) * 8);
+  ctx.upload(d_lib, lib, (size_t)n_lib * E * 8);
+  ctx.upload(d_lt, lib_t, (size_t)n_lib * 8);
+  ctx.upload(d_pred, pred, (size_t)n_pred * E * 8);
+  ctx.upload(d_pt, pred_t, (size_t)n_pred * 8);
+  ctx.upload(d_w, w, E * 8);
+  a.lib = d_lib;
+  a.lib_t = d_lt;
+  a.pred = d_pred;
+  a.pred_t = d_pt;
+  a.w = d_w;
+  a.theta = theta;
+  a.n_lib = n_lib;
+  a.n_pred = n_pred;
+  a.e_actual = e_actual;
+  a.backward = dtheta != nullptr;
+  a.out = d_out;
+  cudaEvent_t e0, e1;
+  ck(cudaEventCreate(&e0), "event");
+  ck(cudaEventCreate(&e1), "event");
+  ck(cudaEventRecord(e0, s), "event");
+  launch_smap_grad(a, s);
+  ctx.check("smap_grad");
+  ck(cudaEventRecord(e1, s), "event");
+  std::vector<double> out((size_t)n_pred * (E + 3));
+  ctx.download(out.data(), d_out, out.size() * 8);
+  ck(cudaStreamSynchronize(s), "sync");
+  float ms = 0;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  // fixed-order host reduction over prediction points
+  double se = 0, gt = 0;
+  std::vector<double> gw(E, 0.0);
+  for (int p = 0; p < n_pred; p++) {
+    const double* o = &out[(size_t)p * (E + 3)];
+    se += o[0] * o[0];
+    if (predictions)
+      predictions[p] = o[1];
+    if (dtheta) {
+      gt += o[2];
+      for (size_t j = 0; j < E; j++)
+        gw[j] += o[3 + j];
+    }
+  }
+  *mse = se / n_pred;
+  if (dtheta) {
+    *dtheta = gt / n_pred;
+    for (size_t j = 0; j < E; j++)
+      dw[j] = gw[j] / n_pred;
+  }
+  ctx.timing.device_ms = ms;
+  ctx.timing.knn_kernel_ms = ms;
+  ctx.timing.knn_launches = 1;
+  ctx.timing.kernel_launches = 1;
+  ctx.timing.distance_pairs = (long long)n_pred * n_lib * (dtheta ? 3 : 2);
+  ctx.timing.predictions = n_pred;
+  ctx.timing.host_ms = now_ms() - t0;
+  return RC_SUCCESS;
+}
+
 // ------------------------------------------------------ host-only helpers
 void host_usable(const fedm_args& a, int maxE, int copredict, unsigned char* out)
 {

@@ -147,6 +147,21 @@ struct MixedRun
 void launch_smap_lists(const GroupParams& g, const MixedRun& m, int num_sms, cudaStream_t s);
 
 void launch_knn_mixed(const GroupParams& g, const MixedRun& m, int C, int num_sms, cudaStream_t s);
+
+// Differentiable S-map over every library neighbour (kernels_adjoint.cu).
+struct AdjointParams
+{
+  const double* lib;     // [n_lib x e_actual] library manifold
+  const double* lib_t;   // [n_lib] library targets
+  const double* pred;    // [n_pred x e_actual] prediction manifold
+  const double* pred_t;  // [n_pred] prediction targets
+  const double* w;       // [e_actual] per-lag embedding weights
+  double theta;
+  int n_lib, n_pred, e_actual;
+  int backward;          // 0: r, yhat only; 1: also 2 r dyhat/dtheta and 2 r dyhat/dw
+  double* out;           // [n_pred x (e_actual + 3)]
+};
+void launch_smap_grad(const AdjointParams& a, cudaStream_t s);
 void center_to_f32(const double* F, long long n, int Ea, const double* center, float* F32, int stride,
                    cudaStream_t s);
 

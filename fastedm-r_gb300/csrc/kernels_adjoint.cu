@@ -1,0 +1,240 @@
+// Differentiable S-map: forecast, one-step MSE and its gradient with respect
+// to theta and to per-lag embedding weights w (no counterpart in the
+// reference, which has no gradients).  The forward pass is the reference's
+// S-map over every library neighbour (src/edm.cpp:737-814 with k = all) on
+// coordinates z = w * m; at w = 1 the distances are the reference's bits.
+//
+// Per prediction point p (one warp, library rows lane-strided):
+//   pass 1  d_i = |z_i - z_p| (zero distances excluded, src/distances.cpp:218),
+//           mu = mean d, dmu/dw_j = mean (z_ij - z_pj)(m_ij - m_pj) / d_i
+//   pass 2  a_i^2 = exp(-2 theta d_i / mu), A = sum a^2 u u^T, b = sum a^2 u t
+//           with u_i = [1, z_i]; c = A^+ b, g = A^+ v (v = [1, z_p]), by the
+//           JacobiSVD restatement; yhat = v.c
+//   pass 3  s_i = g.u_i, e_i = t_i - u_i.c and the sums
+//           Q = sum a^2 s e d, R_j = sum a^2 s e dd_i/dw_j,
+//           S_j = sum a^2 e m_ij, T_j = sum a^2 s m_ij
+//   dyhat/dtheta = -(2/mu) Q
+//   dyhat/dw_j  = m_pj c_{j+1} - (2 theta/mu) R_j + (2 theta dmu/dw_j/mu^2) Q
+//                 + g_{j+1} S_j - c_{j+1} T_j
+// (from dyhat = dv.c + g.(db - dA c), A symmetric).  Each point writes r,
+// and 2 r dyhat/d(.) ; the host sums them in a fixed order.
+#include <cfloat>
+
+#include "exp_rn.cuh"
+#include "kernels.h"
+#include "smap_solve.cuh"
+
+namespace fedm {
+
+namespace {
+
+constexpr unsigned FULL = 0xffffffffu;
+
+__device__ __forceinline__ double wsum(double v)
+{
+  for (int o = 16; o > 0; o >>= 1)
+    v += __shfl_xor_sync(FULL, v, o);
+  return v;
+}
+
+template<int EA>
+__global__ void __launch_bounds__(128) smap_grad_kernel(AdjointParams a)
+{
+  constexpr int n = EA + 1;
+  constexpr int NA = n * (n + 1) / 2;
+  const int lane = threadIdx.x & 31;
+  const int wpb = blockDim.x >> 5;
+  const int pnt = blockIdx.x * wpb + (threadIdx.x >> 5);
+  if (pnt >= a.n_pred)
+    return;
+  double w[EA], y[EA], zp[EA];
+#pragma unroll
+  for (int j = 0; j < EA; j++) {
+    w[j] = a.w[j];
+    y[j] = a.pred[(size_t)pnt * EA + j];
+    zp[j] = mul(w[j], y[j]);
+  }
+  // pass 1: distances, their mean and its derivative
+  double sd = 0, dmu[EA];
+  int cnt = 0;
+#pragma unroll
+  for (int j = 0; j < EA; j++)
+    dmu[j] = 0;
+  for (int i = lane; i < a.n_lib; i += 32) {
+    const double* m = a.lib + (size_t)i * EA;
+    // distance in the reference's operation order (unfused), so at w = 1 it
+    // is the same bits as src/distances.cpp:176-225
+    double diff[EA], s = 0.0;
+#pragma unroll
+    for (int j = 0; j < EA; j++) {
+      diff[j] = sub(mul(w[j], m[j]), zp[j]);
+      s = add(s, mul(diff[j], diff[j]));
+    }
+    if (s != 0) {
+      const double d = __dsqrt_rn(s);
+      sd += d;
+      cnt++;
+#pragma unroll
+      for (int j = 0; j < EA; j++)
+        dmu[j] += diff[j] * (m[j] - y[j]) / d;
+    }
+  }
+  const double total = wsum(sd);
+  const double nv = (double)__reduce_add_sync(FULL, cnt);
+  const double mu = total / nv;
+#pragma unroll
+  for (int j = 0; j < EA; j++)
+    dmu[j] = wsum(dmu[j]) / nv;
+  // pass 2: normal equations
+  double A[NA], b[n];
+#pragma unroll
+  for (int e = 0; e < NA; e++)
+    A[e] = 0;
+#pragma unroll
+  for (int e = 0; e < n; e++)
+    b[e] = 0;
+  for (int i = lane; i < a.n_lib; i += 32) {
+    const double* m = a.lib + (size_t)i * EA;
+    double u[n], s = 0.0;
+    u[0] = 1.0;
+#pragma unroll
+    for (int j = 0; j < EA; j++) {
+      u[j + 1] = mul(w[j], m[j]);
+      const double df = sub(u[j + 1], zp[j]);
+      s = add(s, mul(df, df));
+    }
+    if (s == 0)
+      continue;
+    const double aw = exp_rn(mul(-a.theta, dvd(__dsqrt_rn(s), mu)));
+    const double a2 = aw * aw;
+    const double t = a.lib_t[i];
+    int e = 0;
+#pragma unroll
+    for (int r = 0; r < n; r++) {
+#pragma unroll
+      for (int c = r; c < n; c++)
+        A[e++] += a2 * u[r] * u[c];
+      b[r] += a2 * u[r] * t;
+    }
+  }
+#pragma unroll
+  for (int e = 0; e < NA; e++)
+    A[e] = wsum(A[e]);
+#pragma unroll
+  for (int e = 0; e < n; e++)
+    b[e] = wsum(b[e]);
+  double c[n], gv[n];
+  {
+    // every lane solves the same system (identical inputs, identical bits)
+    double W[n * n], U[n * n], V[n * n], sv[n], tmp[n], v[n];
+    int e = 0;
+    for (int r = 0; r < n; r++)
+      for (int cc = r; cc < n; cc++) {
+        W[r * n + cc] = A[e];
+        W[cc * n + r] = A[e];
+        e++;
+      }
+    svd_solve(W, U, V, sv, tmp, b, c, n);
+    e = 0;
+    for (int r = 0; r < n; r++)
+      for (int cc = r; cc < n; cc++) {
+        W[r * n + cc] = A[e];
+        W[cc * n + r] = A[e];
+        e++;
+      }
+    v[0] = 1.0;
+#pragma unroll
+    for (int j = 0; j < EA; j++)
+      v[j + 1] = zp[j];
+    svd_solve(W, U, V, sv, tmp, v, gv, n);
+  }
+  double yhat = c[0];
+#pragma unroll
+  for (int j = 0; j < EA; j++)
+    yhat += zp[j] * c[j + 1];
+  const double r = yhat - a.pred_t[pnt];
+  double* out = a.out + (size_t)pnt * (EA + 3);
+  if (!a.backward) {
+    if (lane == 0) {
+      out[0] = r;
+      out[1] = yhat;
+    }
+    return;
+  }
+  // pass 3: adjoint sums
+  double Q = 0, R[EA], S[EA], Tt[EA];
+#pragma unroll
+  for (int j = 0; j < EA; j++)
+    R[j] = S[j] = Tt[j] = 0;
+  for (int i = lane; i < a.n_lib; i += 32) {
+    const double* m = a.lib + (size_t)i * EA;
+    double u[n], diff[EA], s = 0.0;
+    u[0] = 1.0;
+#pragma unroll
+    for (int j = 0; j < EA; j++) {
+      u[j + 1] = mul(w[j], m[j]);
+      diff[j] = sub(u[j + 1], zp[j]);
+      s = add(s, mul(diff[j], diff[j]));
+    }
+    if (s == 0)
+      continue;
+    const double d = __dsqrt_rn(s);
+    const double aw = exp_rn(mul(-a.theta, dvd(d, mu)));
+    const double a2 = aw * aw;
+    double su = 0, uc = 0;
+#pragma unroll
+    for (int k = 0; k < n; k++) {
+      su += gv[k] * u[k];
+      uc += u[k] * c[k];
+    }
+    const double ei = a.lib_t[i] - uc;
+    const double ase = a2 * su * ei;
+    Q += ase * d;
+#pragma unroll
+    for (int j = 0; j < EA; j++) {
+      R[j] += ase * (diff[j] * (m[j] - y[j]) / d);
+      S[j] += a2 * ei * m[j];
+      Tt[j] += a2 * su * m[j];
+    }
+  }
+  Q = wsum(Q);
+#pragma unroll
+  for (int j = 0; j < EA; j++) {
+    R[j] = wsum(R[j]);
+    S[j] = wsum(S[j]);
+    Tt[j] = wsum(Tt[j]);
+  }
+  if (lane == 0) {
+    out[0] = r;
+    out[1] = yhat;
+    out[2] = 2 * r * (-(2 / mu) * Q);
+#pragma unroll
+    for (int j = 0; j < EA; j++) {
+      const double dy = y[j] * c[j + 1] - (2 * a.theta / mu) * R[j] + (2 * a.theta * dmu[j] / (mu * mu)) * Q +
+                        gv[j + 1] * S[j] - c[j + 1] * Tt[j];
+      out[3 + j] = 2 * r * dy;
+    }
+  }
+}
+
+} // namespace
+
+void launch_smap_grad(const AdjointParams& a, cudaStream_t s)
+{
+  const int blocks = (a.n_pred + 3) / 4;
+  if (blocks <= 0)
+    return;
+  switch (a.e_actual) {
+    case 1: smap_grad_kernel<1><<<blocks, 128, 0, s>>>(a); break;
+    case 2: smap_grad_kernel<2><<<blocks, 128, 0, s>>>(a); break;
+    case 3: smap_grad_kernel<3><<<blocks, 128, 0, s>>>(a); break;
+    case 4: smap_grad_kernel<4><<<blocks, 128, 0, s>>>(a); break;
+    case 5: smap_grad_kernel<5><<<blocks, 128, 0, s>>>(a); break;
+    case 6: smap_grad_kernel<6><<<blocks, 128, 0, s>>>(a); break;
+    case 7: smap_grad_kernel<7><<<blocks, 128, 0, s>>>(a); break;
+    case 8: smap_grad_kernel<8><<<blocks, 128, 0, s>>>(a); break;
+    default: break;
+  }
+}
+
+} // namespace fedm

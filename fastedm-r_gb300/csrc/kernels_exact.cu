@@ -137,7 +137,27 @@ __global__ void knn_exact_kernel(GroupParams g, ChunkBuffers c, int warps_per_bl
     __syncwarp();
     const int k = T.k;
     int count = 0, numValid = 0;
-    for (int b0 = 0; b0 < T.n_lib; b0 += 32) {
+    // capacity for the whole library: every valid neighbour is kept, so the
+    // list is simply the valid entries in library order (no ranking needed)
+    const bool collect_all = k >= T.n_lib;
+    for (int b0 = 0; b0 < T.n_lib && collect_all; b0 += 32) {
+      const int i = b0 + lane;
+      double d = 0;
+      bool valid = false;
+      if (i < T.n_lib)
+        valid = exact_distance(g, g.lib_rows[T.lib_off + i], prow, sy, ppanel, ptime, d);
+      const unsigned vm = __ballot_sync(FULL, valid);
+      if (valid) {
+        const int slot = count + __popc(vm & ((1u << lane) - 1u));
+        sD[slot] = d;
+        sI[slot] = i;
+      }
+      count += __popc(vm);
+    }
+    if (collect_all)
+      numValid = count;
+    __syncwarp();
+    for (int b0 = 0; b0 < T.n_lib && !collect_all; b0 += 32) {
       const int i = b0 + lane;
       double d = 0;
       bool valid = false;
@@ -194,7 +214,12 @@ __global__ void knn_exact_kernel(GroupParams g, ChunkBuffers c, int warps_per_bl
     int* oi = c.nn_idx + q * c.kcap;
     double* od = c.nn_dist + q * c.kcap;
     if (status == PT_OK) {
-      if (keff == numValid) {
+      if (collect_all && keff == numValid) {
+        for (int e = lane; e < count; e += 32) {
+          oi[e] = sI[e];
+          od[e] = sD[e];
+        }
+      } else if (keff == numValid) {
         // all valid neighbours, in library order (src/edm.cpp:615-616)
         for (int e = lane; e < count; e += 32) {
           int r = 0;

@@ -75,6 +75,7 @@ EXPORTS = [
     "fedm_create", "fedm_destroy", "fedm_last_error", "fedm_set_precision", "fedm_set_keep_going",
     "fedm_run_command", "fedm_free_result", "fedm_run_task", "fedm_last_timing", "fedm_measure_peak",
     "fedm_host_usable", "fedm_host_manifold", "fedm_host_mt_real2", "fedm_host_plan",
+    "fedm_smap_fwd", "fedm_smap_bwd", "fedm_predict_static",
 ]
 
 _lib = None
@@ -97,6 +98,10 @@ def load():
         lib.fedm_run_task.argtypes = [C.c_void_p, C.POINTER(Args), C.POINTER(TaskIO)]
         lib.fedm_last_timing.argtypes = [C.c_void_p, C.POINTER(Timing)]
         lib.fedm_measure_peak.argtypes = [C.c_void_p, C.c_int, C.POINTER(C.c_double)]
+        grad_args = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_int,
+                     C.c_double, C.c_void_p, C.POINTER(C.c_double)]
+        lib.fedm_smap_fwd.argtypes = grad_args + [C.c_void_p]
+        lib.fedm_smap_bwd.argtypes = grad_args + [C.POINTER(C.c_double), C.c_void_p]
         lib.fedm_host_usable.argtypes = [C.POINTER(Args), C.c_int, C.c_int, C.c_void_p]
         lib.fedm_host_manifold.argtypes = [C.POINTER(Args), C.c_int, C.c_int, C.c_void_p, C.POINTER(C.c_int)]
         lib.fedm_host_mt_real2.argtypes = [C.c_ulonglong, C.c_longlong, C.c_void_p]
@@ -146,6 +151,30 @@ class Context:
         if self.lib.fedm_measure_peak(self.h, kind, C.byref(v)) != 0:
             raise RuntimeError(self.last_error())
         return v.value
+
+    def smap_grad(self, lib, lib_t, pred, pred_t, theta, w, backward=True):
+        """Differentiable S-map over every library neighbour with per-lag
+        weights w: (mse, dmse/dtheta, dmse/dw, predictions)."""
+        arrs = [np.ascontiguousarray(v, dtype=np.float64) for v in (lib, lib_t, pred, pred_t, w)]
+        lib, lib_t, pred, pred_t, w = arrs
+        E = lib.shape[1]
+        mse = C.c_double()
+        if backward:
+            dth = C.c_double()
+            dw = np.zeros(E)
+            rc = self.lib.fedm_smap_bwd(self.h, lib.ctypes.data, lib_t.ctypes.data, lib.shape[0], pred.ctypes.data,
+                                        pred_t.ctypes.data, pred.shape[0], E, float(theta), w.ctypes.data,
+                                        C.byref(mse), C.byref(dth), dw.ctypes.data)
+            if rc != 0:
+                raise RuntimeError(f"fedm_smap_bwd rc={rc}: {self.last_error()}")
+            return mse.value, dth.value, dw, None
+        yh = np.zeros(pred.shape[0])
+        rc = self.lib.fedm_smap_fwd(self.h, lib.ctypes.data, lib_t.ctypes.data, lib.shape[0], pred.ctypes.data,
+                                    pred_t.ctypes.data, pred.shape[0], E, float(theta), w.ctypes.data, C.byref(mse),
+                                    yh.ctypes.data)
+        if rc != 0:
+            raise RuntimeError(f"fedm_smap_fwd rc={rc}: {self.last_error()}")
+        return mse.value, None, None, yh
 
     def run_command(self, a):
         keep = []

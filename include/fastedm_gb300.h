@@ -206,6 +206,26 @@ int fedm_host_mt_real2(unsigned long long seed, long long count, double* out);
 int fedm_host_plan(const fedm_args* args, int max_tasks, int* n_tasks, int* task_E, int* task_k, int* task_library,
                    int* task_copredict, unsigned char* lib_masks, unsigned char* pred_masks);
 
+/* Differentiable S-map over every library neighbour (k = all) with per-lag
+ * embedding weights w: coordinates z = w * m enter both the distances and the
+ * local regression.  No counterpart in the reference (it has no gradients);
+ * at w = 1 the forward pass is the reference's S-map with k = all
+ * (src/edm.cpp:737-814).  Host arrays: lib_manifold [n_lib x e_actual],
+ * lib_targets [n_lib], pred_manifold [n_pred x e_actual], pred_targets
+ * [n_pred], w [e_actual]; 1 <= e_actual <= 8.
+ *  fedm_smap_fwd: mse = mean (yhat - target)^2 over prediction points;
+ *                 predictions [n_pred] (may be NULL).
+ *  fedm_smap_bwd: mse and its gradient dmse_dtheta, dmse_dw [e_actual],
+ *                 from the adjoint of the weighted normal equations (the
+ *                 weights are recomputed in the backward pass, nothing of
+ *                 size n_pred x n_lib is stored). */
+int fedm_smap_fwd(fedm_ctx* ctx, const double* lib_manifold, const double* lib_targets, int n_lib,
+                  const double* pred_manifold, const double* pred_targets, int n_pred, int e_actual, double theta,
+                  const double* w, double* mse, double* predictions);
+int fedm_smap_bwd(fedm_ctx* ctx, const double* lib_manifold, const double* lib_targets, int n_lib,
+                  const double* pred_manifold, const double* pred_targets, int n_pred, int e_actual, double theta,
+                  const double* w, double* mse, double* dmse_dtheta, double* dmse_dw);
+
 /* Allocation-free prediction for one task on caller-owned device buffers.
  * No counterpart in the reference: it exists for callers that cannot let a
  * library allocate GPU memory -- hosts that hand the process a fixed device

@@ -1527,6 +1527,112 @@ oracle_result* oracle_run_command(const oracle_args* a)
   return &R;
 }
 
+// Differentiable S-map reference gradient (no counterpart in the fastEDM
+// reference): S-map over every library neighbour on coordinates z = w * m,
+// MSE over prediction points, and dMSE/dtheta, dMSE/dw by the adjoint of the
+// weighted normal equations (c = A^+ b, g = A^+ v, dyhat = dv.c +
+// g.(db - dA c)), evaluated sequentially in FP64.  Distances follow
+// src/distances.cpp:176-225 (zero distances excluded); weights
+// src/edm.cpp:744-745; the solve is the JacobiSVD restatement above.
+int oracle_smap_grad(const double* lib, const double* lib_t, int n_lib, const double* pred, const double* pred_t,
+                     int n_pred, int E, double theta, const double* w, double* mse, double* dtheta, double* dw,
+                     double* yhat_out)
+{
+  const int n = E + 1;
+  double se = 0, gt = 0;
+  std::vector<double> gw(E, 0.0), d(n_lib), a2(n_lib), dmu(E);
+  for (int p = 0; p < n_pred; p++) {
+    const double* y = pred + (size_t)p * E;
+    std::vector<double> zp(E);
+    for (int j = 0; j < E; j++)
+      zp[j] = w[j] * y[j];
+    double sum = 0;
+    int cnt = 0;
+    std::fill(dmu.begin(), dmu.end(), 0.0);
+    for (int i = 0; i < n_lib; i++) {
+      const double* m = lib + (size_t)i * E;
+      double s = 0;
+      for (int j = 0; j < E; j++) {
+        const double df = w[j] * m[j] - zp[j];
+        s += df * df;
+      }
+      d[i] = s != 0 ? std::sqrt(s) : -1.0;
+      if (s != 0) {
+        sum += d[i];
+        cnt++;
+        for (int j = 0; j < E; j++)
+          dmu[j] += (w[j] * m[j] - zp[j]) * (m[j] - y[j]) / d[i];
+      }
+    }
+    const double mu = sum / cnt;
+    for (int j = 0; j < E; j++)
+      dmu[j] /= cnt;
+    std::vector<double> A((size_t)n * n, 0.0), b(n, 0.0), u(n);
+    for (int i = 0; i < n_lib; i++) {
+      if (d[i] < 0)
+        continue;
+      const double aw = edm_exp(-theta * (d[i] / mu));
+      a2[i] = aw * aw;
+      u[0] = 1;
+      for (int j = 0; j < E; j++)
+        u[j + 1] = w[j] * lib[(size_t)i * E + j];
+      for (int r = 0; r < n; r++) {
+        for (int c = 0; c < n; c++)
+          A[(size_t)r * n + c] += a2[i] * u[r] * u[c];
+        b[r] += a2[i] * u[r] * lib_t[i];
+      }
+    }
+    std::vector<double> v(n);
+    v[0] = 1;
+    for (int j = 0; j < E; j++)
+      v[j + 1] = zp[j];
+    std::vector<double> c = jacobi_svd_solve(A, n, b), g = jacobi_svd_solve(A, n, v);
+    double yh = c[0];
+    for (int j = 0; j < E; j++)
+      yh += zp[j] * c[j + 1];
+    if (yhat_out)
+      yhat_out[p] = yh;
+    const double r = yh - pred_t[p];
+    se += r * r;
+    if (!dtheta)
+      continue;
+    double Q = 0;
+    std::vector<double> R(E, 0.0), S(E, 0.0), T(E, 0.0);
+    for (int i = 0; i < n_lib; i++) {
+      if (d[i] < 0)
+        continue;
+      const double* m = lib + (size_t)i * E;
+      u[0] = 1;
+      for (int j = 0; j < E; j++)
+        u[j + 1] = w[j] * m[j];
+      double su = 0, uc = 0;
+      for (int k = 0; k < n; k++) {
+        su += g[k] * u[k];
+        uc += u[k] * c[k];
+      }
+      const double ei = lib_t[i] - uc;
+      Q += a2[i] * su * ei * d[i];
+      for (int j = 0; j < E; j++) {
+        R[j] += a2[i] * su * ei * ((w[j] * m[j] - zp[j]) * (m[j] - y[j]) / d[i]);
+        S[j] += a2[i] * ei * m[j];
+        T[j] += a2[i] * su * m[j];
+      }
+    }
+    gt += 2 * r * (-(2 / mu) * Q);
+    for (int j = 0; j < E; j++)
+      gw[j] += 2 * r *
+               (y[j] * c[j + 1] - (2 * theta / mu) * R[j] + (2 * theta * dmu[j] / (mu * mu)) * Q + g[j + 1] * S[j] -
+                c[j + 1] * T[j]);
+  }
+  *mse = se / n_pred;
+  if (dtheta) {
+    *dtheta = gt / n_pred;
+    for (int j = 0; j < E; j++)
+      dw[j] = gw[j] / n_pred;
+  }
+  return 0;
+}
+
 int oracle_plan(const oracle_args* a, int max_tasks, int* n_tasks, int* task_E, int* task_k, int* task_library,
                 int* task_copredict, unsigned char* lib_masks, unsigned char* pred_masks)
 {

@@ -145,6 +145,13 @@ int oracle_task_run(const oracle_args* args, oracle_task_io* io);
 int oracle_plan(const oracle_args* args, int max_tasks, int* n_tasks, int* task_E, int* task_k, int* task_library,
                 int* task_copredict, unsigned char* lib_masks, unsigned char* pred_masks);
 
+/* Differentiable S-map check (no counterpart in the reference): MSE over
+ * prediction points of S-map with every library neighbour on coordinates
+ * z = w * m, and (dtheta non-NULL) dMSE/dtheta, dMSE/dw[E]; yhat may be NULL. */
+int oracle_smap_grad(const double* lib, const double* lib_t, int n_lib, const double* pred, const double* pred_t,
+                     int n_pred, int E, double theta, const double* w, double* mse, double* dtheta, double* dw,
+                     double* yhat);
+
 /* The usable-row mask run_command computes (src/r.cpp:256-257). */
 int oracle_usable(const oracle_args* args, int maxE, int copredict, unsigned char* usable_out);
 

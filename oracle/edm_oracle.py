@@ -81,6 +81,8 @@ def load():
         _lib.oracle_mt_real2.argtypes = [C.c_ulonglong, C.c_longlong, C.c_void_p]
         _lib.oracle_set_exp_mode.argtypes = [C.c_int]
         _lib.oracle_set_pred_stride.argtypes = [C.c_int]
+        _lib.oracle_smap_grad.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_int,
+                                          C.c_double, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
         _lib.oracle_plan.argtypes = [C.POINTER(OracleArgs), C.c_int] + [C.c_void_p] * 7
         _lib.oracle_exp.argtypes = [C.c_double]
         _lib.oracle_exp.restype = C.c_double
@@ -330,3 +332,21 @@ def plan(a):
 def set_pred_stride(stride):
     """Benchmark sampling: predict every stride-th row of each prediction set."""
     load().oracle_set_pred_stride(int(stride))
+
+
+def smap_grad(lib, lib_t, pred, pred_t, theta, w, backward=True):
+    """CPU FP64 differentiable S-map: (mse, dtheta, dw, yhat)."""
+    L = load()
+    lib = np.ascontiguousarray(lib, dtype=np.float64)
+    pred = np.ascontiguousarray(pred, dtype=np.float64)
+    lib_t = np.ascontiguousarray(lib_t, dtype=np.float64)
+    pred_t = np.ascontiguousarray(pred_t, dtype=np.float64)
+    w = np.ascontiguousarray(w, dtype=np.float64)
+    E = lib.shape[1]
+    mse, dth = C.c_double(), C.c_double()
+    dw = np.zeros(E)
+    yh = np.zeros(pred.shape[0])
+    L.oracle_smap_grad(lib.ctypes.data, lib_t.ctypes.data, lib.shape[0], pred.ctypes.data, pred_t.ctypes.data,
+                       pred.shape[0], E, float(theta), w.ctypes.data, C.byref(mse),
+                       C.byref(dth) if backward else None, dw.ctypes.data if backward else None, yh.ctypes.data)
+    return mse.value, (dth.value if backward else None), (dw if backward else None), yh

@@ -1,0 +1,108 @@
+"""GPU parity on the benchmark configurations' shapes (seeded synthetic data).
+
+* S-map theta sweep with k = all (config 2 shape), at an oracle-tractable
+  size: through the task seam (bit-exact) and through run_command.
+* Uneven multispatial panels with missing values and dt (config 4 shape),
+  reduced to 48 panels: run_command with mixed and independent panels.
+* Config 2 at full size (10 000 / 10 000): with theta = 0 every weight is 1,
+  so S-map is ordinary least squares on the library; the forecasts must match
+  numpy's lstsq (a check that needs no oracle).
+* Batched CCM (config 3 shape) on a reduced grid: every replicate's rho
+  against the oracle, for both precisions.
+"""
+import numpy as np
+import pytest
+
+import edm_oracle
+from fedm_loader import fedm, workloads
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _device_exp():
+    edm_oracle.set_exp_mode(1)
+    yield
+    edm_oracle.set_exp_mode(0)
+
+
+@pytest.fixture(scope="module", params=[fedm.PRECISION_FP64, fedm.PRECISION_MIXED], ids=["fp64", "mixed"])
+def ctx(request):
+    c = fedm.Context(0, precision=request.param)
+    yield c
+    c.close()
+
+
+def _stats_close(g, o, key="stats", rtol=1e-9):
+    assert g["rc"] == o["rc"]
+    for f in ("E", "library", "theta"):
+        assert np.array_equal(g[key][f], o[key][f])
+    for f in ("rho", "mae"):
+        a, b = np.asarray(g[key][f]), np.asarray(o[key][f])
+        assert np.array_equal(np.isnan(a), np.isnan(b))
+        m = ~np.isnan(a)
+        assert np.allclose(a[m], b[m], rtol=rtol, atol=1e-12), (f, np.max(np.abs(a[m] - b[m])))
+
+
+def test_smap_theta_sweep_all_neighbours_task(ctx):
+    w = workloads.smap_config(T=1200)
+    a = edm_oracle.normalise(w["t"], w["x"], E=5, theta=w["thetas"][::4], algorithm="smap", numThreads=16)
+    g = ctx.run_task(a, w["library_rows"], w["prediction_rows"], 5, -1)
+    o = edm_oracle.oracle_task(a, w["library_rows"], w["prediction_rows"], 5, -1)
+    assert np.array_equal(g["nn_idx"], o["nn_idx"])
+    assert np.array_equal(g["predictions"], o["predictions"])
+    assert np.array_equal(g["coeffs"], o["coeffs"])
+
+
+def test_smap_theta_sweep_all_neighbours_command(ctx):
+    w = workloads.smap_config(T=1600)
+    kw = dict(E=5, k=float("inf"), theta=w["thetas"][::8], algorithm="smap", savePredictions=True,
+              saveSMAPCoeffs=True)
+    g = fedm.edm(w["t"], w["x"], ctx=ctx, **kw)
+    o = edm_oracle.oracle_edm(w["t"], w["x"], numThreads=16, **kw)
+    _stats_close(g, o)
+    assert np.array_equal(g["predictions"], o["predictions"], equal_nan=True)
+    assert np.array_equal(g["coeffs"], o["coeffs"], equal_nan=True)
+
+
+@pytest.mark.parametrize("panel_weight", [0.0, float("inf")], ids=["mixed_panels", "independent_panels"])
+@pytest.mark.parametrize("algorithm", ["simplex", "smap"])
+def test_uneven_panels_missing_dt(ctx, panel_weight, algorithm):
+    w = workloads.panel_config(n_panels=48, lo=40, hi=300)
+    theta = [0.0, 1.0, 2.0, 4.0] if algorithm == "smap" else [1.0]
+    kw = dict(panel=w["panel"], E=[3, 4, 5, 6, 7, 8], dt=True, algorithm=algorithm, theta=theta,
+              panelWeight=panel_weight)
+    g = fedm.edm(w["t"], w["x"], ctx=ctx, **kw)
+    o = edm_oracle.oracle_edm(w["t"], w["x"], numThreads=16, **kw)
+    _stats_close(g, o)
+    assert g["kMin"] == o["kMin"] and g["kMax"] == o["kMax"] and g["dtWeight"] == o["dtWeight"]
+
+
+def test_ccm_replicates_reduced(ctx):
+    w = workloads.ccm_config(T=4000, reps=4, n_libs=6, hi=3000)
+    for algorithm, theta in (("simplex", 1.0), ("smap", 2.0)):
+        kw = dict(E=4, library=w["libraries"], numReps=4, seed=w["seed"], algorithm=algorithm, theta=theta)
+        g = fedm.edm(w["t"], w["x"], w["y"], ctx=ctx, **kw)
+        o = edm_oracle.oracle_edm(w["t"], w["x"], w["y"], numThreads=16, **kw)
+        _stats_close(g, o)
+
+
+def test_smap_theta0_is_least_squares_full_size(ctx):
+    """Config 2 size: 10 000 library rows, 10 000 forecasts, k = all."""
+    w = workloads.smap_config(T=20000)
+    a = fedm.normalise(w["t"], w["x"], E=5, theta=[0.0], algorithm="smap", k=float("inf"), savePredictions=True)
+    lib, pred = w["library_rows"].copy(), w["prediction_rows"]
+    lib[:4] = False  # rows without a full lag window are not usable (src/manifold.cpp:314-360)
+    g = ctx.run_task(a, lib, pred, 5, -1)
+    F = fedm.host_manifold(a, 5)
+    x = w["x"]
+    lib_rows = np.nonzero(lib)[0]
+    pred_rows = np.nonzero(pred)[0]
+    A = np.column_stack([np.ones(len(lib_rows)), F[lib_rows]])
+    coef, *_ = np.linalg.lstsq(A, x[lib_rows + 1], rcond=None)
+    want = coef[0] + F[pred_rows] @ coef[1:]
+    got = g["predictions"][0]
+    # every prediction row gets a forecast, also the last one whose target
+    # is not observed (prediction sets keep such rows, src/manifold.h:186-189)
+    assert np.all(got != 1e100) and g["n_lib"] == len(lib_rows)
+    assert np.allclose(got, want, rtol=1e-7, atol=1e-9)
