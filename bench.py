@@ -10,9 +10,12 @@ random-library replicates, simplex (k = E+1) and S-map (theta = 2, k = E+2)
          preparation, splitter, uploads, kernels, downloads)
 
 Also reported: the plain FP64 GPU form and |delta rho| against it on a
-2-replicate sample, the roofline of the dominant kernel against the measured
-FP32 FFMA peak, and the CPU oracle on a bounded sample.  `--impl reference`
-times the CPU restatement of the reference path (all host threads) instead.
+2-replicate sample, the roofline of the dominant kernel (the S-map
+scan + re-rank + solve kernel, FP64-bound: its FP64 operations, counted by
+the kernel, over its CUDA-event time, against this GPU's measured unfused
+FP64 multiply/add rate) with the simplex kernel's FP32 figure beside it, and
+the CPU oracle on a bounded sample.  `--impl reference` times the CPU
+restatement of the reference path (all host threads) instead.
 """
 import argparse
 import json
@@ -30,7 +33,18 @@ import numpy as np
 ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT / "tests"))
 METRIC = "CCM S-map predictions/s: batched FP32+FP64-fix vs plain FP64 GPU @|Δρ|≤1e-6"
-HBM_GBS = 6794.1
+# DRAM bytes per S-map prediction point of knn_mixed_kernel<4,8,1> (ncu
+# dram__bytes_read.sum + dram__bytes_write.sum of one launch over 2 x 20 CCM
+# libraries, divided by its 1,999,880 points; profiles/knn_mixed_smap_ccm.md);
+# the traffic is per-thread solver scratch, so it scales with the points.
+SMAP_DRAM_BYTES_PER_POINT = None
+
+
+def hbm_peak():
+    try:
+        return float(json.loads((ROOT / "MEASURED_PEAKS.json").read_text())["hbm_gbs"]), "MEASURED_PEAKS.json"
+    except (OSError, ValueError, KeyError):
+        return 6800.0, "fallback (no MEASURED_PEAKS.json)"
 
 
 def load_pkg():
@@ -151,22 +165,26 @@ def run_ours(a):
     w["n_pred"] = a.T - (w["E"] - 1)
     ctx = fedm.Context(local, precision=fedm.PRECISION_MIXED)
     fp32_peak = ctx.measure_peak(0)
+    fp64_unfused_peak = ctx.measure_peak(3)
+    fp64_fma_peak = ctx.measure_peak(1)
     calls = [ccm_args(fedm, w, alg, a.reps) for alg in ("simplex", "smap")]
 
     def step():
         tot = dict(device_ms=0.0, knn_kernel_ms=0.0, knn_launches=0, predictions=0, distance_pairs=0,
-                   h2d_bytes=0, d2h_bytes=0, fallback_points=0, kernel_launches=0, wall_ms=0.0)
+                   h2d_bytes=0, d2h_bytes=0, fallback_points=0, kernel_launches=0, fp64_ops=0, wall_ms=0.0)
+        base_keys = [k for k in tot if k != "wall_ms"]
         rhos = []
-        for args in calls:
+        for args, alg in zip(calls, ("simplex", "smap")):
             t0 = time.perf_counter()
             r = ctx.run_command(args)
             tot["wall_ms"] += (time.perf_counter() - t0) * 1e3
             if r["rc"] != 0:
                 raise RuntimeError(f"run_command rc={r['rc']}: {r.get('error')}")
             tm = ctx.timing()
-            for k in tot:
-                if k != "wall_ms":
-                    tot[k] += tm[k]
+            for k in base_keys:
+                tot[k] += tm[k]
+            for k in ("knn_kernel_ms", "knn_launches", "fp64_ops", "distance_pairs", "predictions"):
+                tot[f"{alg}_{k}"] = tm[k]
             rhos.append(r["stats"]["rho"])
         return tot, rhos
 
@@ -192,15 +210,26 @@ def run_ours(a):
     value = preds * world / dev_s_max
     e2e = preds * world / wall_s_max
     pairs, alg_bytes = algorithmic_units(w, a.reps)
-    knn_ms_step = statistics.mean(s["knn_kernel_ms"] for s in per_step)
-    launches_step = statistics.mean(s["knn_launches"] for s in per_step)
-    flops_step = 3.0 * w["E"] * pairs
-    achieved = flops_step / launches_step / (knn_ms_step / launches_step * 1e-3) / 1e12
+    hbm_gbs, hbm_src = hbm_peak()
+
+    def mean_of(key):
+        return statistics.mean(s[key] for s in per_step)
+
+    # dominant kernel: S-map scan + FP64 re-rank + solve (one launch per step
+    # plus the exact kernels of its few uncertified points, timed with it)
+    sm_ms = mean_of("smap_knn_kernel_ms")
+    sm_launches = mean_of("smap_knn_launches")
+    sm_ops = mean_of("smap_fp64_ops")
+    sm_points = mean_of("smap_predictions")
+    sm_fp64 = sm_ops / (sm_ms * 1e-3) / 1e12
+    sm_fp32 = 3.0 * w["E"] * pairs / 2 / (sm_ms * 1e-3) / 1e12
     traffic = None
-    prof = ROOT / "profiles" / "knn_mixed_ccm_traffic.json"
-    if prof.exists():
-        pj = json.loads(prof.read_text())
-        traffic = pj.get("bytes_per_full_launch")
+    if SMAP_DRAM_BYTES_PER_POINT is not None:
+        traffic = SMAP_DRAM_BYTES_PER_POINT * sm_points / sm_launches
+    # simplex kernel: FP32 scan + re-rank + forecast
+    sx_ms = mean_of("simplex_knn_kernel_ms")
+    sx_fp32 = 3.0 * w["E"] * pairs / 2 / (sx_ms * 1e-3) / 1e12
+    knn_ms_step = sm_ms + sx_ms
 
     # plain FP64 GPU form and |delta rho| on a 2-replicate sample
     fp64 = None
@@ -242,12 +271,24 @@ def run_ours(a):
                 "d2h_bytes_per_step": int(s0["d2h_bytes"]), "wall_ms_per_step": wall_s_max / a.steps * 1e3},
         "gpu_launches": int(sum(s["kernel_launches"] for s in per_step)),
         "roofline": {
-            "kernel": "knn_mixed_kernel (FP32 scan + FP64 re-rank + forecast)", "bound": "fp32_simt",
-            "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s", "frac": achieved / fp32_peak,
-            "peak_source": "measured FFMA peak of this GPU (fedm_measure_peak), not in MEASURED_PEAKS.json",
-            "algorithmic_flops_per_step": flops_step, "traffic": traffic,
-            "hbm": {"achieved_gbs": alg_bytes / (knn_ms_step * 1e-3) / 1e9, "peak_gbs": HBM_GBS,
-                    "frac": alg_bytes / (knn_ms_step * 1e-3) / 1e9 / HBM_GBS, "peak_source": "MEASURED_PEAKS.json"},
+            "kernel": "knn_mixed_kernel<E=4,C=8,smap> (FP32 scan + FP64 re-rank + JacobiSVD solve)",
+            "bound": "fp64_simt", "achieved": sm_fp64, "peak": fp64_unfused_peak, "unit": "TFLOP/s",
+            "frac": sm_fp64 / fp64_unfused_peak,
+            "peak_source": "measured FP64 multiply+add rate without fusion on this GPU (fedm_measure_peak kind 3; "
+                           "the bit-exact solve uses no FMA); MEASURED_PEAKS.json has no FP64 figure",
+            "fp64_fma_peak": fp64_fma_peak,
+            "algorithmic_fp64_ops_per_launch": sm_ops / sm_launches,
+            "fp64_ops_per_forecast": sm_ops / max(sm_points, 1),
+            "kernel_ms_per_step": sm_ms, "share_of_device_time": sm_ms / (dev_s_max / a.steps * 1e3),
+            "traffic": traffic,
+            "fp32_scan": {"achieved": sm_fp32, "peak": fp32_peak, "frac": sm_fp32 / fp32_peak,
+                          "flops": "3*E per (prediction, library) pair"},
+            "simplex_kernel": {"kernel": "knn_mixed_kernel<E=4,C=8,simplex>", "bound": "fp32_simt",
+                               "achieved": sx_fp32, "peak": fp32_peak, "frac": sx_fp32 / fp32_peak,
+                               "kernel_ms_per_step": sx_ms,
+                               "peak_source": "measured FFMA rate of this GPU (fedm_measure_peak kind 0)"},
+            "hbm": {"achieved_gbs": alg_bytes / (knn_ms_step * 1e-3) / 1e9, "peak_gbs": hbm_gbs,
+                    "frac": alg_bytes / (knn_ms_step * 1e-3) / 1e9 / hbm_gbs, "peak_source": hbm_src},
         },
         "fp64_plain": fp64,
         "fallback_points_per_step": int(s0["fallback_points"]),

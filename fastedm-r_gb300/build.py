@@ -43,7 +43,7 @@ def _stale(obj, deps):
 
 def build(verbose=False, ptxas_info=False):
     OUT.mkdir(exist_ok=True)
-    headers = list(SRC.glob("*.h")) + [PKG.parent / "include" / "fastedm_gb300.h"]
+    headers = list(SRC.glob("*.h")) + list(SRC.glob("*.cuh")) + [PKG.parent / "include" / "fastedm_gb300.h"]
     jobs, objs = [], []
     for name, extra in CU_FLAGS.items():
         src = SRC / name

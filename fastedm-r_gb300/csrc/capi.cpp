@@ -232,7 +232,7 @@ int fedm_smap_bwd(fedm_ctx* ctx, const double* lib_manifold, const double* lib_t
 
 int fedm_measure_peak(fedm_ctx* ctx, int kind, double* tflops)
 {
-  if (!ctx || !tflops || kind < 0 || kind > 2)
+  if (!ctx || !tflops || kind < 0 || kind > 3)
     return FEDM_UNKNOWN_ERROR;
   return guarded(ctx, [&] {
     *tflops = fedm::measure_peak(kind, ctx->c->num_sms, ctx->c->stream);

@@ -581,9 +581,10 @@ void run_group(Context& ctx, const Options& o, const std::vector<Task>& tasks, c
     m.items = (const int2*)ctx.buf("items", std::max<size_t>(items.size(), 1) * sizeof(int2));
     ctx.upload((void*)m.items, items.data(), items.size() * sizeof(int2));
     m.n_items = (int)items.size();
-    m.counter = (int*)ctx.buf("mix_counter", 8);
+    m.counter = (int*)ctx.buf("mix_counter", 16);
     m.fb_count = m.counter + 1;
-    fill_i32(m.counter, 2, 0, s);
+    m.fp64_ops = (unsigned long long*)(m.counter + 2);
+    fill_i32(m.counter, 4, 0, s);
     m.fb_cap = (int)std::min<long long>(std::max<long long>(P, 1), FB_CAP);
     m.fb_list = (long long*)ctx.buf("fb_list", (size_t)m.fb_cap * 8);
     m.gamma = (Ea + 2) * std::ldexp(1.0, -23);
@@ -628,9 +629,12 @@ void run_group(Context& ctx, const Options& o, const std::vector<Task>& tasks, c
       timed([&] { launch_knn_mixed(g, m, C, ctx.num_sms, s); });
     }
     int nfb = 0;
+    unsigned long long nops = 0;
     ctx.download(&nfb, m.fb_count, 4);
+    ctx.download(&nops, m.fp64_ops, 8);
     ck(cudaStreamSynchronize(s), "sync");
     ctx.timing.fallback_points += nfb;
+    ctx.timing.fp64_ops += (long long)nops;
     if (job.detail) {
       std::vector<int> ku(P), mi((size_t)P * C);
       std::vector<double> md((size_t)P * C);

@@ -127,6 +127,7 @@ struct MixedRun
   int* nn_idx;         // optional [total_points x kslots] final neighbour lists
   double* nn_dist;
   int kslots;
+  unsigned long long* fp64_ops;  // optional: FP64 operations of the re-rank and forecast stage
   int item_begin;      // first item of this launch (the queue head starts here)
   int item_end;        // one past the last item of this launch
   // S-map: when set, the neighbour lists are appended here and solved by

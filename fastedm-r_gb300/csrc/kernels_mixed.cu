@@ -88,8 +88,12 @@ template<int EA>
 __device__ __noinline__ void smap_point(const GroupParams& g, long long p, int prow, bool save, int keff,
                                         const int* rows, const double* cd);
 template<int EA>
-__device__ __noinline__ void smap_point_local(const GroupParams& g, long long p, int prow, bool save, int keff,
-                                              const int* rows, const double* cd);
+__device__ __noinline__ int smap_point_local(const GroupParams& g, long long p, int prow, bool save, int keff,
+                                             const int* rows, const double* cd);
+
+// FP64 operations of exp_rn: one multiply, fifteen fused multiply-adds (two
+// flops each) and the final scaling multiply.
+constexpr int EXP_OPS = 32;
 
 // Candidates of one point, handed to the out-of-line FP64 stage.
 template<int C>
@@ -101,9 +105,10 @@ struct Cand
   int zi[ZCAP];
 };
 
+// Returns the number of FP64 add/sub/mul/div/sqrt operations it performed.
 template<int EA, int C, int ALG>
-__device__ __noinline__ void finalize_point(const GroupParams& g, const MixedRun& m, const DevTask& T, long long p,
-                                            int prow, const Cand<C>& cand)
+__device__ __noinline__ int finalize_point(const GroupParams& g, const MixedRun& m, const DevTask& T, long long p,
+                                           int prow, const Cand<C>& cand)
 {
   const float(&D)[C] = cand.D;
   const int(&I)[C] = cand.I;
@@ -128,7 +133,7 @@ __device__ __noinline__ void finalize_point(const GroupParams& g, const MixedRun
     const int slot = atomicAdd(m.fb_count, 1);
     if (slot < m.fb_cap)
       m.fb_list[slot] = p;
-    return;
+    return 0;
   }
   double y[EA];
 #pragma unroll
@@ -159,6 +164,7 @@ __device__ __noinline__ void finalize_point(const GroupParams& g, const MixedRun
       }
     }
   }
+  int ops = nc * (3 * EA + 1);
   const int numValid = T.n_lib - z + zvalid;
   const int kr = T.k_req < 0 ? numValid : T.k_req;
   const int keff = kr < numValid ? kr : numValid;
@@ -168,7 +174,7 @@ __device__ __noinline__ void finalize_point(const GroupParams& g, const MixedRun
       note_rc_m(g, T.task, 8000);
     if (g.kused)
       g.kused[p] = INT_MIN;
-    return;
+    return ops;
   }
   // (distance, library index) order among the candidates
   for (int a = 1; a < nc; a++) {
@@ -221,7 +227,7 @@ __device__ __noinline__ void finalize_point(const GroupParams& g, const MixedRun
       m.l_rows[(size_t)slot * m.kslots + j] = rows[j];
       m.l_dist[(size_t)slot * m.kslots + j] = cd[j];
     }
-    return;
+    return ops;
   }
 
   if constexpr (ALG == 0) {
@@ -247,10 +253,10 @@ __device__ __noinline__ void finalize_point(const GroupParams& g, const MixedRun
         r = add(r, mul(tg[j], dvd(w[j], sumw)));
       g.pred[(size_t)t * g.total_points + p] = r;
     }
-    return;
+    return ops + keff + g.n_thetas * keff * (EXP_OPS + 5);
   }
   else {
-    smap_point_local<EA>(g, p, prow, T.save_coeffs != 0, keff, rows, cd);
+    return ops + smap_point_local<EA>(g, p, prow, T.save_coeffs != 0, keff, rows, cd);
   }
 }
 
@@ -276,14 +282,23 @@ __global__ void __launch_bounds__(TPB, 2) knn_mixed_kernel(GroupParams g, MixedR
   __shared__ __align__(16) float2 tile[(TILE / 2) * EA];
   __shared__ int s_item;
   const int tid = threadIdx.x;
+  unsigned long long ops = 0;
   for (;;) {
     __syncthreads();
     if (tid == 0)
       s_item = m.item_begin + atomicAdd(m.counter, 1);
     __syncthreads();
     const int item = s_item;
-    if (item >= m.item_end)
+    if (item >= m.item_end) {
+      // every thread of the CTA leaves here together: full warps
+      if (m.fp64_ops) {
+        for (int o = 16; o > 0; o >>= 1)
+          ops += __shfl_xor_sync(0xffffffffu, ops, o);
+        if ((tid & 31) == 0)
+          atomicAdd(m.fp64_ops, ops);
+      }
       return;
+    }
     const int2 it = m.items[item];
     const DevTask T = g.tasks[it.x];
     const int pi0 = it.y + tid, pi1 = it.y + tid + TPB;
@@ -366,7 +381,7 @@ __global__ void __launch_bounds__(TPB, 2) knn_mixed_kernel(GroupParams g, MixedR
 #pragma unroll
       for (int j = 0; j < ZCAP; j++)
         c.zi[j] = zi0[j];
-      finalize_point<EA, C, ALG>(g, m, T, T.point_base + pi0, prow0, c);
+      ops += finalize_point<EA, C, ALG>(g, m, T, T.point_base + pi0, prow0, c);
     }
     if (a1) {
       Cand<C> c;
@@ -379,7 +394,7 @@ __global__ void __launch_bounds__(TPB, 2) knn_mixed_kernel(GroupParams g, MixedR
 #pragma unroll
       for (int j = 0; j < ZCAP; j++)
         c.zi[j] = zi1[j];
-      finalize_point<EA, C, ALG>(g, m, T, T.point_base + pi1, prow1, c);
+      ops += finalize_point<EA, C, ALG>(g, m, T, T.point_base + pi1, prow1, c);
     }
   }
 }
@@ -450,10 +465,13 @@ __device__ __noinline__ void smap_point(const GroupParams& g, long long p, int p
 // used inside the scan kernel, whose register budget (two 256-thread CTAs
 // per SM) leaves no room for them.  Identical operations and bits.
 template<int EA>
-__device__ __noinline__ void smap_point_local(const GroupParams& g, long long p, int prow, bool save, int keff,
-                                              const int* rows, const double* cd)
+__device__ __noinline__ int smap_point_local(const GroupParams& g, long long p, int prow, bool save, int keff,
+                                             const int* rows, const double* cd)
 {
   constexpr int n = EA + 1;
+  // mean; per theta: weights and the normal equations per neighbour, the
+  // forecast (the SVD counts its own)
+  int ops = keff + 1 + g.n_thetas * (keff * (EXP_OPS + 2 + n + n * (n + 1) + 2 * n) + 2 * EA);
   double y[EA];
 #pragma unroll
   for (int j = 0; j < EA; j++)
@@ -489,7 +507,7 @@ __device__ __noinline__ void smap_point_local(const GroupParams& g, long long p,
     for (int a = 0; a < n; a++)
       for (int b = 0; b < a; b++)
         W[a * n + b] = W[b * n + a];
-    svd_solve(W, U, V, sv, tmp, bv, xs, n);
+    svd_solve(W, U, V, sv, tmp, bv, xs, n, ops);
     double r = xs[0];
 #pragma unroll
     for (int j = 0; j < EA; j++)
@@ -500,6 +518,7 @@ __device__ __noinline__ void smap_point_local(const GroupParams& g, long long p,
     }
     g.pred[(size_t)t * g.total_points + p] = r;
   }
+  return ops;
 }
 
 template<int EA>

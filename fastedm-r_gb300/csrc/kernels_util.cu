@@ -114,15 +114,35 @@ __global__ void peak_fp64_kernel(double* out, int iters)
     out[0] = s;
 }
 
+// Separate multiply and add (never contracted): the rate of the FP64 work
+// that must keep the reference's unfused operation order.
+__global__ void peak_fp64_unfused_kernel(double* out, int iters)
+{
+  double a[8];
+  for (int j = 0; j < 8; j++)
+    a[j] = threadIdx.x * 1e-7 + j;
+  const double b = 0.999999, c = 1e-7;
+  for (int i = 0; i < iters; i++) {
+#pragma unroll
+    for (int j = 0; j < 8; j++)
+      a[j] = __dadd_rn(__dmul_rn(a[j], b), c);
+  }
+  double s = 0;
+  for (int j = 0; j < 8; j++)
+    s += a[j];
+  if (s == 12345.0)
+    out[0] = s;
+}
+
 } // namespace
 
-// Returns TFLOP/s (2 flops per multiply-add) of the chosen probe.
+// Returns TFLOP/s (2 flops per multiply-add, fused or not) of the chosen probe.
 double measure_peak(int kind, int num_sms, cudaStream_t s)
 {
   void* buf = nullptr;
   cudaMalloc(&buf, 64);
   const int threads = 256, blocks = num_sms * 8;
-  const int iters = kind == 1 ? 2000 : 40000;
+  const int iters = (kind == 1 || kind == 3) ? 2000 : 40000;
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
@@ -133,6 +153,8 @@ double measure_peak(int kind, int num_sms, cudaStream_t s)
       peak_fp32_kernel<<<blocks, threads, 0, s>>>((float*)buf, iters);
     else if (kind == 2)
       peak_fp32x2_kernel<<<blocks, threads, 0, s>>>((float*)buf, iters);
+    else if (kind == 3)
+      peak_fp64_unfused_kernel<<<blocks, threads, 0, s>>>((double*)buf, iters);
     else
       peak_fp64_kernel<<<blocks, threads, 0, s>>>((double*)buf, iters);
     cudaEventRecord(e1, s);

@@ -45,8 +45,10 @@ __device__ __forceinline__ void rot_cols(double* A, int n, int p, int q, Rot j)
   }
 }
 
-__device__ inline void jacobi_2x2(const double* W, int n, int p, int q, Rot& jl, Rot& jr)
+// ops counts the FP64 add/sub/mul/div/sqrt operations performed.
+__device__ inline void jacobi_2x2(const double* W, int n, int p, int q, Rot& jl, Rot& jr, int& ops)
 {
+  ops += 18;
   const double tiny = DBL_MIN;
   const double m00 = W[p * n + p], m01 = W[p * n + q], m10 = W[q * n + p], m11 = W[q * n + q];
   Rot r1;
@@ -59,6 +61,7 @@ __device__ inline void jacobi_2x2(const double* W, int n, int p, int q, Rot& jl,
     const double tmp = __dsqrt_rn(add(1.0, mul(u, u)));
     r1.s = dvd(1.0, tmp);
     r1.c = dvd(u, tmp);
+    ops += 6;
   }
   const double n00 = add(mul(r1.c, m00), mul(r1.s, m10));
   const double n01 = add(mul(r1.c, m01), mul(r1.s, m11));
@@ -73,8 +76,13 @@ __device__ inline void jacobi_2x2(const double* W, int n, int p, int q, Rot& jl,
     const double tt = tau > 0 ? dvd(1.0, add(tau, w)) : dvd(1.0, sub(tau, w));
     const double sign_t = tt > 0 ? 1.0 : -1.0;
     const double nn = dvd(1.0, __dsqrt_rn(add(mul(tt, tt), 1.0)));
-    jr.s = mul(mul(mul(-sign_t, dvd(n01, fabs(n01))), fabs(tt)), nn);
+    // Eigen forms -sign_t * (n01 / |n01|) * |tt| * nn left to right; the
+    // first two products are exact sign changes (n01 is finite and nonzero
+    // here), so only the last multiply rounds.
+    const bool neg = (sign_t > 0) == (n01 > 0);
+    jr.s = mul(neg ? -fabs(tt) : fabs(tt), nn);
     jr.c = nn;
+    ops += 12;
   }
   const double jtc = jr.c, jts = -jr.s;
   jl.c = sub(mul(r1.c, jtc), mul(r1.s, jts));
@@ -82,9 +90,10 @@ __device__ inline void jacobi_2x2(const double* W, int n, int p, int q, Rot& jl,
 }
 
 // Solves A x = b in the pseudo-inverse sense.  W holds A (n x n, destroyed);
-// U, V: n*n scratch; sv, tmp: n scratch.
+// U, V: n*n scratch; sv, tmp: n scratch.  ops accumulates the number of FP64
+// add/sub/mul/div/sqrt operations performed (the solve's algorithmic work).
 __device__ inline void svd_solve(double* W, double* U, double* V, double* sv, double* tmp, const double* b, double* x,
-                                 int n)
+                                 int n, int& ops)
 {
   const double tiny = DBL_MIN, eps = DBL_EPSILON, precision = 2 * DBL_EPSILON;
   double scale = 0;
@@ -102,6 +111,7 @@ __device__ inline void svd_solve(double* W, double* U, double* V, double* sv, do
     U[i] = 0;
     V[i] = 0;
   }
+  ops += n * n;
   for (int i = 0; i < n; i++)
     U[i * n + i] = V[i * n + i] = 1;
   double maxDiag = 0;
@@ -115,10 +125,12 @@ __device__ inline void svd_solve(double* W, double* U, double* V, double* sv, do
     for (int p = 1; p < n; p++) {
       for (int q = 0; q < p; q++) {
         const double threshold = fmax(tiny, mul(precision, maxDiag));
+        ops += 1;
         if (fabs(W[p * n + q]) > threshold || fabs(W[q * n + p]) > threshold) {
           finished = false;
           Rot jl, jr;
-          jacobi_2x2(W, n, p, q, jl, jr);
+          jacobi_2x2(W, n, p, q, jl, jr, ops);
+          ops += 24 * n;
           rot_rows(W, n, p, q, jl);
           rot_cols(U, n, p, q, Rot{ jl.c, -jl.s });
           rot_cols(W, n, p, q, jr);
@@ -137,6 +149,7 @@ __device__ inline void svd_solve(double* W, double* U, double* V, double* sv, do
   }
   for (int i = 0; i < n; i++)
     sv[i] = mul(sv[i], scale);
+  ops += n + 2;
   int nonzero = n;
   for (int i = 0; i < n; i++) {
     int pos = i;
@@ -181,6 +194,14 @@ __device__ inline void svd_solve(double* W, double* U, double* V, double* sv, do
       s = add(s, mul(V[r * n + cc], tmp[cc]));
     x[r] = s;
   }
+  ops += rank * (2 * n + 2) + 2 * n * rank;
+}
+
+__device__ inline void svd_solve(double* W, double* U, double* V, double* sv, double* tmp, const double* b, double* x,
+                                 int n)
+{
+  int ops = 0;
+  svd_solve(W, U, V, sv, tmp, b, x, n, ops);
 }
 
 // Square-root-free Cholesky (LDL^T) solve of the symmetric normal equations

@@ -80,7 +80,9 @@ __device__ __forceinline__ void svd_solve_n(double (&W)[N][N], const double (&b)
             const double tt = tau > 0 ? dvd(1.0, add(tau, w)) : dvd(1.0, sub(tau, w));
             const double sign_t = tt > 0 ? 1.0 : -1.0;
             const double nn = dvd(1.0, __dsqrt_rn(add(mul(tt, tt), 1.0)));
-            jrs = mul(mul(mul(-sign_t, dvd(n01, fabs(n01))), fabs(tt)), nn);
+            // -sign_t * (n01 / |n01|) * |tt| is an exact sign change
+            const bool neg = (sign_t > 0) == (n01 > 0);
+            jrs = mul(neg ? -fabs(tt) : fabs(tt), nn);
             jrc = nn;
           }
           const double jtc = jrc, jts = -jrs;

@@ -67,7 +67,7 @@ class Timing(C.Structure):
         ("device_ms", C.c_double), ("knn_kernel_ms", C.c_double), ("knn_launches", C.c_int),
         ("host_ms", C.c_double), ("distance_pairs", C.c_longlong), ("predictions", C.c_longlong),
         ("h2d_bytes", C.c_longlong), ("d2h_bytes", C.c_longlong), ("fallback_points", C.c_int),
-        ("kernel_launches", C.c_int),
+        ("kernel_launches", C.c_int), ("fp64_ops", C.c_longlong),
     ]
 
 
@@ -125,6 +125,7 @@ class Context:
     def set_precision(self, precision):
         if self.lib.fedm_set_precision(self.h, precision) != 0:
             raise ValueError("bad precision")
+        self.precision = precision
 
     def close(self):
         if self.h:
@@ -146,7 +147,8 @@ class Context:
         return {f: getattr(t, f) for f, _ in Timing._fields_}
 
     def measure_peak(self, kind):
-        """TFLOP/s of kind 0 FP32 FFMA, 1 FP64 DFMA, 2 packed FP32 FFMA2."""
+        """TFLOP/s of kind 0 FP32 FFMA, 1 FP64 DFMA, 2 packed FP32 FFMA2,
+        3 FP64 DMUL/DADD without fusion (one flop per instruction)."""
         v = C.c_double()
         if self.lib.fedm_measure_peak(self.h, kind, C.byref(v)) != 0:
             raise RuntimeError(self.last_error())

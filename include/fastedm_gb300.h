@@ -184,6 +184,8 @@ typedef struct fedm_timing {
   long long d2h_bytes;
   int fallback_points;       /* mixed path: points re-run in exact FP64      */
   int kernel_launches;       /* kernels this library launched                */
+  long long fp64_ops;        /* mixed path: FP64 add/sub/mul/div/sqrt of the
+                                re-rank and forecast stage (exp = 32)        */
 } fedm_timing;
 
 int fedm_last_timing(const fedm_ctx* ctx, fedm_timing* out);
@@ -265,8 +267,10 @@ int fedm_predict_static(const double* lib_manifold, const double* lib_targets, i
                         const double* thetas, int n_thetas, double* predictions, int* kused, void* stream);
 
 /* Measured arithmetic peak of this GPU in TFLOP/s (2 flops per fused
- * multiply-add): kind 0 FP32 FFMA, 1 FP64 DFMA, 2 packed FP32 FFMA2.  A
- * diagnostic for roofline fractions; it has no counterpart in the reference. */
+ * multiply-add): kind 0 FP32 FFMA, 1 FP64 DFMA, 2 packed FP32 FFMA2, 3 FP64
+ * multiply and add issued separately (1 flop per instruction; the rate of
+ * FP64 work that keeps an unfused operation order).  A diagnostic for
+ * roofline fractions; it has no counterpart in the reference. */
 int fedm_measure_peak(fedm_ctx* ctx, int kind, double* tflops);
 
 #ifdef __cplusplus

@@ -106,3 +106,23 @@ def test_smap_theta0_is_least_squares_full_size(ctx):
     # is not observed (prediction sets keep such rows, src/manifold.h:186-189)
     assert np.all(got != 1e100) and g["n_lib"] == len(lib_rows)
     assert np.allclose(got, want, rtol=1e-7, atol=1e-9)
+
+
+def test_mixed_fp64_operation_count(ctx):
+    """The mixed kernel counts the FP64 arithmetic of its re-rank and forecast
+    stage (the roofline's numerator); the exact FP64 path reports none."""
+    w = workloads.ccm_config(T=3000, reps=2, n_libs=4, hi=2000)
+    per = {}
+    for algorithm, theta in (("simplex", 1.0), ("smap", 2.0)):
+        g = fedm.edm(w["t"], w["x"], w["y"], ctx=ctx, E=4, library=w["libraries"], numReps=2, seed=w["seed"],
+                     algorithm=algorithm, theta=theta)
+        assert g["rc"] == 0
+        tm = ctx.timing()
+        per[algorithm] = tm["fp64_ops"] / tm["predictions"]
+    if ctx.precision == fedm.PRECISION_FP64:
+        assert per["simplex"] == 0 and per["smap"] == 0
+    else:
+        # simplex E=4, k=5: >= 5 rescored distances (13 ops) + 5 * 38 ops
+        assert 250 <= per["simplex"] <= 1000, per
+        # S-map E=4, k=6: ~25 Jacobi rotations of ~170 ops plus the normal equations
+        assert 2000 <= per["smap"] <= 20000, per
