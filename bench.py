@@ -171,7 +171,8 @@ def run_ours(a):
 
     def step():
         tot = dict(device_ms=0.0, knn_kernel_ms=0.0, knn_launches=0, predictions=0, distance_pairs=0,
-                   h2d_bytes=0, d2h_bytes=0, fallback_points=0, kernel_launches=0, fp64_ops=0, wall_ms=0.0)
+                   h2d_bytes=0, d2h_bytes=0, fallback_points=0, kernel_launches=0, fp64_ops=0, host_ms=0.0,
+                   list_wait_ms=0.0, setup_ms=0.0, finish_ms=0.0, wall_ms=0.0)
         base_keys = [k for k in tot if k != "wall_ms"]
         rhos = []
         for args, alg in zip(calls, ("simplex", "smap")):
@@ -268,7 +269,8 @@ def run_ours(a):
             "l2": "flushed between steps (512 MiB write)", "parallelism": f"replicas x{world}",
         },
         "e2e": {"value": e2e, "unit": "predictions/s", "h2d_bytes_per_step": int(s0["h2d_bytes"]),
-                "d2h_bytes_per_step": int(s0["d2h_bytes"]), "wall_ms_per_step": wall_s_max / a.steps * 1e3},
+                "d2h_bytes_per_step": int(s0["d2h_bytes"]), "wall_ms_per_step": wall_s_max / a.steps * 1e3,
+                "host_ms_per_step": {k: mean_of(k) for k in ("host_ms", "list_wait_ms", "setup_ms", "finish_ms")}},
         "gpu_launches": int(sum(s["kernel_launches"] for s in per_step)),
         "roofline": {
             "kernel": "knn_mixed_kernel<E=4,C=8,smap> (FP32 scan + FP64 re-rank + JacobiSVD solve)",

@@ -62,7 +62,7 @@ def build(verbose=False, ptxas_info=False):
         obj = OUT / (name + ".o")
         objs.append(obj)
         if _stale(obj, [src] + headers):
-            jobs.append(["g++", "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall", "-Wno-sign-compare",
+            jobs.append(["g++", "-O3", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall", "-Wno-sign-compare",
                          f"-I{CUDA_HOME / 'include'}", "-c", str(src), "-o", str(obj)])
     with ThreadPoolExecutor(max_workers=max(1, min(8, os.cpu_count() or 1))) as ex:
         logs = list(ex.map(_run, jobs))

@@ -14,6 +14,7 @@
 #include <chrono>
 #include <climits>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <numeric>
 #include <thread>
@@ -48,6 +49,11 @@ Context::Context(int dev) : device(dev)
   ck(cudaSetDevice(dev), "cudaSetDevice");
   ck(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), "cudaStreamCreate");
   ck(cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, dev), "cudaDeviceGetAttribute");
+  if (const char* v = std::getenv("FEDM_SMAP_SOLVER_WARPS")) {
+    const int w = std::atoi(v);
+    if (w == 0 || w == 4 || w == 8)
+      smap_solver_warps = w;
+  }
 }
 
 Context::~Context()
@@ -279,6 +285,8 @@ struct GroupJob
 constexpr int KCAP_MAX = 16384;
 constexpr int MIX_KMAX = 14;        // neighbours the mixed kernel serves (slots C = 16)
 constexpr int MIX_POINTS = 512;     // prediction points per mixed work item
+constexpr size_t LAZY_BATCHES = 8;  // task batches of a group whose CCM lists are produced lazily
+constexpr size_t LAZY_MIN_BATCH = 64;
 constexpr long long FB_CAP = 1 << 24;
 
 // Whether the mixed kernel's preconditions hold for a group (see
@@ -338,6 +346,7 @@ void run_group(Context& ctx, const Options& o, const std::vector<Task>& tasks, c
   const int nT = (int)job.task_ids.size();
   if (nT == 0)
     return;
+  const double t_enter = now_ms();
   const int Ea = job.Ea, n = Ea + 1;
   const int nth = (int)o.thetas.size();
   cudaStream_t s = ctx.stream;
@@ -465,6 +474,7 @@ void run_group(Context& ctx, const Options& o, const std::vector<Task>& tasks, c
   ck(cudaEventCreate(&gs), "event");
   ck(cudaEventCreate(&ge), "event");
   ck(cudaEventRecord(gs, s), "event");
+  ctx.timing.setup_ms += now_ms() - t_enter;
   ctx.timing.kernel_launches += 6;  // fills
 
   // chunking: neighbour lists, statuses and the all-mode Gram buffer
@@ -581,10 +591,13 @@ void run_group(Context& ctx, const Options& o, const std::vector<Task>& tasks, c
     m.items = (const int2*)ctx.buf("items", std::max<size_t>(items.size(), 1) * sizeof(int2));
     ctx.upload((void*)m.items, items.data(), items.size() * sizeof(int2));
     m.n_items = (int)items.size();
-    m.counter = (int*)ctx.buf("mix_counter", 16);
+    // queue head, fallback count, FP64 operation count (8 B), hand-off error
+    m.counter = (int*)ctx.buf("mix_counter", 32);
     m.fb_count = m.counter + 1;
     m.fp64_ops = (unsigned long long*)(m.counter + 2);
-    fill_i32(m.counter, 4, 0, s);
+    m.error = m.counter + 4;
+    fill_i32(m.counter, 8, 0, s);
+    m.solver_warps = o.algorithm == 1 ? ctx.smap_solver_warps : 0;
     m.fb_cap = (int)std::min<long long>(std::max<long long>(P, 1), FB_CAP);
     m.fb_list = (long long*)ctx.buf("fb_list", (size_t)m.fb_cap * 8);
     m.gamma = (Ea + 2) * std::ldexp(1.0, -23);
@@ -628,11 +641,14 @@ void run_group(Context& ctx, const Options& o, const std::vector<Task>& tasks, c
       m.item_end = m.n_items;
       timed([&] { launch_knn_mixed(g, m, C, ctx.num_sms, s); });
     }
-    int nfb = 0;
+    int nfb = 0, herr = 0;
     unsigned long long nops = 0;
     ctx.download(&nfb, m.fb_count, 4);
     ctx.download(&nops, m.fp64_ops, 8);
+    ctx.download(&herr, m.error, 4);
     ck(cudaStreamSynchronize(s), "sync");
+    if (herr)
+      throw Error{ RC_UNKNOWN_ERROR, "mixed S-map kernel: scan/solve hand-off timed out" };
     ctx.timing.fallback_points += nfb;
     ctx.timing.fp64_ops += (long long)nops;
     if (job.detail) {
@@ -723,6 +739,7 @@ void run_group(Context& ctx, const Options& o, const std::vector<Task>& tasks, c
   }
   cudaEventDestroy(gs);
   cudaEventDestroy(ge);
+  const double t_fin = now_ms();
   std::vector<int> rc(nT), kmin(nT), kmax(nT);
   std::vector<double> rho((size_t)nT * nth), mae((size_t)nT * nth);
   int err = 0;
@@ -772,6 +789,7 @@ void run_group(Context& ctx, const Options& o, const std::vector<Task>& tasks, c
     }
   }
   ck(cudaStreamSynchronize(s), "sync");
+  ctx.timing.finish_ms += now_ms() - t_fin;
 }
 
 double na(double v)
@@ -864,22 +882,37 @@ CommandResult run_command(Context& ctx, const fedm_args& a)
   if (copredict_mode)
     cousable = gen.usable(maxE, true, threads);
   RowTables rt = build_row_tables(gen);
+  // CCM library splits are left lazy: a SplitProducer computes their row
+  // lists on background threads while the GPU runs earlier task batches
   TaskPlan plan = configure_tasks(gen, o, P.Es, libraries, a.k, a.num_reps, a.crossfold, P.explore, a.full,
                                   a.shuffle, a.save_predictions, a.save_copredictions, a.save_smap_coeffs,
-                                  copredict_mode, usable, cousable, a.seed, &rt.lib_target, threads);
+                                  copredict_mode, usable, cousable, a.seed, &rt.lib_target, threads, true);
+  std::unique_ptr<SplitProducer> producer;
+  if (plan.lazy.active)
+    producer = std::make_unique<SplitProducer>(plan, rt.lib_target, threads);
   DevRows drows = upload_rows(ctx, gen, rt, o);
 
-  // row lists per mask (shared by every task that uses the mask)
+  // row lists per mask (shared by every task that uses the mask); lazy
+  // library lists are taken when their batch runs
   std::vector<std::vector<int>> lib_lists(plan.masks.size()), pred_lists(plan.masks.size());
   std::vector<uint8_t> lib_done(plan.masks.size(), 0), pred_done(plan.masks.size(), 0);
-  for (const Task& t : plan.tasks) {
-    if (!lib_done[t.lib_mask]) {
-      if (!plan.lists_ready.empty() && plan.lists_ready[t.lib_mask])
-        lib_lists[t.lib_mask].swap(plan.lib_lists[t.lib_mask]);
-      else
-        lib_lists[t.lib_mask] = lib_rows_of(plan.masks[t.lib_mask], rt);
-      lib_done[t.lib_mask] = 1;
+  auto take_lib_list = [&](int mask) {
+    if (lib_done[mask])
+      return;
+    if (producer) {
+      const double tw = now_ms();
+      producer->wait(mask);
+      ctx.timing.list_wait_ms += now_ms() - tw;
     }
+    if (!plan.lists_ready.empty() && plan.lists_ready[mask])
+      lib_lists[mask].swap(plan.lib_lists[mask]);
+    else
+      lib_lists[mask] = lib_rows_of(plan.masks[mask], rt);
+    lib_done[mask] = 1;
+  };
+  for (const Task& t : plan.tasks) {
+    if (!producer)
+      take_lib_list(t.lib_mask);
     if (!pred_done[t.pred_mask]) {
       pred_lists[t.pred_mask] = rows_of(plan.masks[t.pred_mask]);
       pred_done[t.pred_mask] = 1;
@@ -903,15 +936,28 @@ CommandResult run_command(Context& ctx, const fedm_args& a)
     job.dFp = key.second ? device_manifold(ctx, M, gen, rt, key.first, true, threads) : job.dF;
     job.hF = &M.host[std::make_pair(key.first, false)];
     job.hFp = key.second ? &M.host[std::make_pair(key.first, true)] : job.hF;
-    for (int i = 0; i < (int)plan.tasks.size(); i++) {
-      const Task& t = plan.tasks[i];
-      if (t.E == key.first && t.copredict == key.second) {
-        job.task_ids.push_back(i);
+    std::vector<int> ids;
+    for (int i = 0; i < (int)plan.tasks.size(); i++)
+      if (plan.tasks[i].E == key.first && plan.tasks[i].copredict == key.second)
+        ids.push_back(i);
+    // With lazy lists the group runs in about LAZY_BATCHES batches of tasks
+    // in plan order (replicates outermost, so every batch spans all library
+    // sizes); each waits only for its own lists.
+    const size_t per = producer ? std::max<size_t>(LAZY_MIN_BATCH, (ids.size() + LAZY_BATCHES - 1) / LAZY_BATCHES)
+                                : ids.size();
+    for (size_t b0 = 0; b0 < ids.size(); b0 += per) {
+      job.task_ids.clear();
+      job.lib_lists.clear();
+      job.pred_lists.clear();
+      for (size_t q = b0; q < std::min(ids.size(), b0 + per); q++) {
+        const Task& t = plan.tasks[ids[q]];
+        take_lib_list(t.lib_mask);
+        job.task_ids.push_back(ids[q]);
         job.lib_lists.push_back(&lib_lists[t.lib_mask]);
         job.pred_lists.push_back(&pred_lists[t.pred_mask]);
       }
+      run_group(ctx, o, plan.tasks, drows, job, outs);
     }
-    run_group(ctx, o, plan.tasks, drows, job, outs);
   }
 
   // src/r.cpp:348-457 marshalling, in task order
@@ -1101,14 +1147,20 @@ int host_plan(const fedm_args& a, int max_tasks, int* task_E, int* task_k, int* 
   std::vector<uint8_t> cousable;
   if (co)
     cousable = gen.usable(P.Es.back(), true, threads);
-  // every row counts as having a target here, so the parallel splitter's
-  // row lists are exactly the membership masks
+  // every row counts as having a target here, so the splitter's row lists
+  // are exactly the membership masks; the lists come from the same lazy
+  // SplitProducer that run_command uses
   std::vector<double> all_targets(gen.n, 0.0);
   TaskPlan plan = configure_tasks(gen, P.opts, P.Es, libraries, a.k, a.num_reps, a.crossfold, P.explore, a.full,
                                   a.shuffle, a.save_predictions, a.save_copredictions, a.save_smap_coeffs, co,
-                                  usable, cousable, a.seed, &all_targets, threads);
+                                  usable, cousable, a.seed, &all_targets, threads, true);
+  std::unique_ptr<SplitProducer> producer;
+  if (plan.lazy.active && max_tasks > 0)
+    producer = std::make_unique<SplitProducer>(plan, all_targets, threads);
   for (int i = 0; i < (int)plan.tasks.size() && i < max_tasks; i++) {
     const Task& t = plan.tasks[i];
+    if (producer)
+      producer->wait(t.lib_mask);
     task_E[i] = t.E;
     task_k[i] = t.k;
     task_library[i] = t.library;

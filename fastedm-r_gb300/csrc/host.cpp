@@ -329,7 +329,7 @@ void Mt64::skip(long long count)
   }
 }
 
-double Mt64::real2()
+uint64_t Mt64::next53()
 {
   if (left == 0)
     refill();
@@ -339,7 +339,12 @@ double Mt64::real2()
   y ^= (y << 17) & 0x71D67FFFEDA60000ULL;
   y ^= (y << 37) & 0xFFF7EEE000000000ULL;
   y ^= (y >> 43);
-  return (double)(y >> 11) * (1.0 / 9007199254740992.0);
+  return y >> 11;
+}
+
+double Mt64::real2()
+{
+  return (double)next53() * (1.0 / 9007199254740992.0);
 }
 
 // -------------------------------------------------------------- Splitter
@@ -472,12 +477,124 @@ void Splitter::update(int library, int iter)
 }
 
 // ------------------------------------------------------- configure_tasks
+void select_library(Mt64& state, int library, const std::vector<int>& urows, const std::vector<double>& lib_target,
+                    std::vector<int>& out, SplitScratch& sc)
+{
+  const int nu = (int)urows.size();
+  sc.u.resize(nu);
+  sc.hist.assign(4096, 0);
+  for (int o = 0; o < nu; o++)
+    sc.u[o] = state.next53();
+  uint64_t cutoff = 1ULL << 53;  // getReal2() < 1.0 always
+  if (library < nu) {
+    // histogram of the top 12 bits, then nth_element inside the bucket that
+    // holds the order statistic
+    for (int o = 0; o < nu; o++)
+      sc.hist[sc.u[o] >> 41]++;
+    int b = 0, below = 0;
+    while (below + sc.hist[b] <= library)
+      below += sc.hist[b++];
+    sc.c.clear();
+    for (int o = 0; o < nu; o++)
+      if ((int)(sc.u[o] >> 41) == b)
+        sc.c.push_back(sc.u[o]);
+    std::nth_element(sc.c.begin(), sc.c.begin() + (library - below), sc.c.end());
+    cutoff = sc.c[library - below];
+  }
+  out.clear();
+  out.reserve(std::min(library, nu));
+  for (int o = 0; o < nu; o++)
+    if (sc.u[o] < cutoff && lib_target[urows[o]] != MISSING_D)
+      out.push_back(urows[o]);
+}
+
+SplitProducer::SplitProducer(TaskPlan& plan, const std::vector<double>& lib_target, int threads)
+    : plan_(plan), target_(lib_target)
+{
+  const LazySplits& lz = plan.lazy;
+  const int n = (int)lz.library.size();
+  snaps_.resize(n);
+  done_.assign(n, 0);
+  split_of_mask_.assign(plan.masks.size(), -1);
+  for (int j = 0; j < n; j++)
+    split_of_mask_[lz.mask[j]] = j;
+  threads_.emplace_back([this] { sequence(); });
+  const int workers = std::max(1, std::min(threads - 2, n));
+  for (int w = 0; w < workers; w++)
+    threads_.emplace_back([this] { work(); });
+}
+
+SplitProducer::~SplitProducer()
+{
+  stop_ = true;
+  {
+    std::lock_guard<std::mutex> lk(mu_);
+  }
+  cv_snap_.notify_all();
+  cv_done_.notify_all();
+  for (auto& t : threads_)
+    t.join();
+}
+
+void SplitProducer::sequence()
+{
+  const LazySplits& lz = plan_.lazy;
+  Mt64 s = lz.start;
+  const int n = (int)lz.library.size();
+  for (int j = 0; j < n && !stop_; j++) {
+    snaps_[j] = s;
+    {
+      std::lock_guard<std::mutex> lk(mu_);
+      snapped_.store(j + 1);
+    }
+    cv_snap_.notify_all();
+    s.skip(lz.num_usable);
+  }
+}
+
+void SplitProducer::work()
+{
+  const LazySplits& lz = plan_.lazy;
+  const int n = (int)lz.library.size();
+  SplitScratch sc;
+  std::vector<int> out;
+  for (;;) {
+    const int j = next_.fetch_add(1);
+    if (j >= n)
+      return;
+    {
+      std::unique_lock<std::mutex> lk(mu_);
+      cv_snap_.wait(lk, [&] { return stop_.load() || snapped_.load() > j; });
+      if (stop_)
+        return;
+    }
+    Mt64 st = snaps_[j];
+    select_library(st, lz.library[j], lz.urows, target_, out, sc);
+    {
+      std::lock_guard<std::mutex> lk(mu_);
+      plan_.lib_lists[lz.mask[j]].swap(out);
+      plan_.lists_ready[lz.mask[j]] = 1;
+      done_[j] = 1;
+    }
+    cv_done_.notify_all();
+  }
+}
+
+void SplitProducer::wait(int mask)
+{
+  const int j = mask < (int)split_of_mask_.size() ? split_of_mask_[mask] : -1;
+  if (j < 0)
+    return;
+  std::unique_lock<std::mutex> lk(mu_);
+  cv_done_.wait(lk, [&] { return stop_.load() || done_[j] != 0; });
+}
+
 TaskPlan configure_tasks(const Generator& g, const Options& opts, const std::vector<int>& Es,
                          const std::vector<int>& libraries, int k, int num_reps, int crossfold, bool explore,
                          bool full, bool shuffle, bool save_predictions, bool save_copredictions,
                          bool save_smap_coeffs, bool copredict_mode, const std::vector<uint8_t>& usable,
                          const std::vector<uint8_t>& cousable, int seed, const std::vector<double>* lib_target,
-                         int threads)
+                         int threads, bool lazy_lists)
 {
   TaskPlan plan;
   Splitter sp(explore, full, shuffle, crossfold, usable, seed);
@@ -526,7 +643,24 @@ TaskPlan configure_tasks(const Generator& g, const Options& opts, const std::vec
         t.save_coeffs = save_smap_coeffs;
         if (new_split) {
           new_split = false;
-          if (deferred) {
+          if (deferred && lazy_lists) {
+            // src/library_prediction_split.h:231-270 (shuffle branch), left
+            // to a SplitProducer: only the first split's stream state is kept
+            if (!plan.lazy.active) {
+              plan.lazy.active = true;
+              plan.lazy.start = sp.stream();
+              plan.lazy.num_usable = sp.num_usable();
+            }
+            plan.masks.emplace_back();
+            lib_mask = (int)plan.masks.size() - 1;
+            plan.lazy.library.push_back(library);
+            plan.lazy.mask.push_back(lib_mask);
+            if (usable_mask < 0) {
+              plan.masks.push_back(usable);
+              usable_mask = (int)plan.masks.size() - 1;
+            }
+            pred_mask = usable_mask;
+          } else if (deferred) {
             // src/library_prediction_split.h:231-270 (shuffle branch), run
             // later from a snapshot of the stream
             Deferred d;
@@ -567,6 +701,13 @@ TaskPlan configure_tasks(const Generator& g, const Options& opts, const std::vec
       }
     }
   }
+  if (plan.lazy.active) {
+    plan.lib_lists.resize(plan.masks.size());
+    plan.lists_ready.assign(plan.masks.size(), 0);
+    for (int i = 0; i < (int)usable.size(); i++)
+      if (usable[i])
+        plan.lazy.urows.push_back(i);
+  }
   if (!splits.empty()) {
     plan.lib_lists.resize(plan.masks.size());
     plan.lists_ready.assign(plan.masks.size(), 0);
@@ -574,29 +715,15 @@ TaskPlan configure_tasks(const Generator& g, const Options& opts, const std::vec
     for (int i = 0; i < (int)usable.size(); i++)
       if (usable[i])
         urows.push_back(i);
-    const int nu = (int)urows.size();
     std::atomic<size_t> next{ 0 };
     auto worker = [&] {
-      std::vector<double> u(nu), c(nu);
+      SplitScratch sc;
       for (;;) {
         const size_t j = next.fetch_add(1);
         if (j >= splits.size())
           break;
         Deferred& d = splits[j];
-        for (int o = 0; o < nu; o++)
-          u[o] = d.state.real2();
-        double cutoff = 1.0;
-        if (d.library < nu) {
-          c = u;
-          std::nth_element(c.begin(), c.begin() + d.library, c.end());
-          cutoff = c[d.library];
-        }
-        std::vector<int>& out = plan.lib_lists[d.mask];
-        out.clear();
-        out.reserve(std::min(d.library, nu));
-        for (int o = 0; o < nu; o++)
-          if (u[o] < cutoff && (*lib_target)[urows[o]] != MISSING_D)
-            out.push_back(urows[o]);
+        select_library(d.state, d.library, urows, *lib_target, plan.lib_lists[d.mask], sc);
         plan.lists_ready[d.mask] = 1;
       }
     };

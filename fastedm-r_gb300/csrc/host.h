@@ -5,11 +5,15 @@
 // dimension E over all rows, tasks are row-index lists into it.
 #pragma once
 
+#include <atomic>
 #include <climits>
+#include <condition_variable>
 #include <cstdint>
 #include <map>
 #include <memory>
+#include <mutex>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/fastedm_gb300.h"
@@ -96,6 +100,8 @@ struct Mt64
   void init(uint64_t seed);
   void refill();
   double real2();
+  // The 53-bit integer behind real2(): real2() == next53() * 2^-53 exactly.
+  uint64_t next53();
   // Advances the stream by `count` draws without producing them (refills
   // only); the next real2() returns the value it would have returned after
   // `count` calls.
@@ -110,6 +116,7 @@ public:
   int next_library_size(int iter) const;
   void update(int library, int iter);
   void defer_fixed_size(Mt64& snapshot);
+  const Mt64& stream() const { return rng_; }
   int num_usable() const { return num_usable_; }
   const std::vector<uint8_t>& lib() const { return lib_; }
   const std::vector<uint8_t>& pred() const { return pred_; }
@@ -154,6 +161,20 @@ struct Task
   bool save_coeffs = false;
 };
 
+// Shuffled fixed-size CCM splits whose row lists are left to a SplitProducer:
+// the MT19937-64 state at the first split (each split then consumes
+// num_usable draws), and per split, in stream order, its library size and
+// mask id.
+struct LazySplits
+{
+  bool active = false;
+  Mt64 start{};
+  int num_usable = 0;
+  std::vector<int> library;
+  std::vector<int> mask;
+  std::vector<int> urows;  // the usable rows, in order
+};
+
 struct TaskPlan
 {
   std::vector<Task> tasks;
@@ -162,6 +183,50 @@ struct TaskPlan
   // parallel CCM splitter; lists_ready[id] marks the mask ids they replace.
   std::vector<std::vector<int>> lib_lists;
   std::vector<uint8_t> lists_ready;
+  LazySplits lazy;
+};
+
+// One shuffled fixed-size split (src/library_prediction_split.h:231-270):
+// draws num_usable uniforms from `state`, takes the library-th order
+// statistic as the cutoff and returns, in `out`, the usable rows under it
+// whose target is observed.  The uniforms are compared as the 53-bit
+// integers behind getReal2 (same order, same cutoff test).
+struct SplitScratch
+{
+  std::vector<uint64_t> u, c;
+  std::vector<int> hist;
+};
+void select_library(Mt64& state, int library, const std::vector<int>& urows, const std::vector<double>& lib_target,
+                    std::vector<int>& out, SplitScratch& scratch);
+
+// Produces the row lists of plan.lazy on background threads while the
+// caller runs the GPU work of earlier tasks: one thread walks the stream and
+// snapshots it at each split, the others select each split's library from
+// its snapshot.  wait(mask) blocks until that mask's list is in
+// plan.lib_lists; the destructor stops and joins the threads.
+class SplitProducer
+{
+public:
+  SplitProducer(TaskPlan& plan, const std::vector<double>& lib_target, int threads);
+  ~SplitProducer();
+  SplitProducer(const SplitProducer&) = delete;
+  SplitProducer& operator=(const SplitProducer&) = delete;
+  void wait(int mask);
+
+private:
+  TaskPlan& plan_;
+  const std::vector<double>& target_;
+  std::vector<Mt64> snaps_;
+  std::vector<int> split_of_mask_;
+  std::vector<uint8_t> done_;
+  std::atomic<int> snapped_{ 0 };
+  std::atomic<int> next_{ 0 };
+  std::atomic<bool> stop_{ false };
+  std::mutex mu_;
+  std::condition_variable cv_snap_, cv_done_;
+  std::vector<std::thread> threads_;
+  void sequence();
+  void work();
 };
 
 // src/edm.cpp:90-212 configure_tasks
@@ -175,7 +240,8 @@ TaskPlan configure_tasks(const Generator& g, const Options& opts, const std::vec
                          bool full, bool shuffle, bool save_predictions, bool save_copredictions,
                          bool save_smap_coeffs, bool copredict_mode, const std::vector<uint8_t>& usable,
                          const std::vector<uint8_t>& cousable, int seed,
-                         const std::vector<double>* lib_target = nullptr, int threads = 1);
+                         const std::vector<double>* lib_target = nullptr, int threads = 1,
+                         bool lazy_lists = false);
 
 // Cleans one input vector: every non-normal value becomes MISSING_D
 // (src/r.cpp:64-71).

@@ -128,6 +128,8 @@ struct MixedRun
   double* nn_dist;
   int kslots;
   unsigned long long* fp64_ops;  // optional: FP64 operations of the re-rank and forecast stage
+  int* error;          // set when a bounded wait of the warp-specialised kernel ran out
+  int solver_warps;    // S-map: 0 = knn_mixed_kernel, 4 / 8 = knn_smap_ws_kernel
   int item_begin;      // first item of this launch (the queue head starts here)
   int item_end;        // one past the last item of this launch
   // S-map: when set, the neighbour lists are appended here and solved by

@@ -90,6 +90,9 @@ __device__ __noinline__ void smap_point(const GroupParams& g, long long p, int p
 template<int EA>
 __device__ __noinline__ int smap_point_local(const GroupParams& g, long long p, int prow, bool save, int keff,
                                              const int* rows, const double* cd);
+template<int EA>
+__device__ __noinline__ int smap_point_sm(const GroupParams& g, long long p, int prow, bool save, int keff,
+                                          const int* rows, const double* cd, double* uv, int uv_stride);
 
 // FP64 operations of exp_rn: one multiply, fifteen fused multiply-adds (two
 // flops each) and the final scaling multiply.
@@ -106,9 +109,12 @@ struct Cand
 };
 
 // Returns the number of FP64 add/sub/mul/div/sqrt operations it performed.
-template<int EA, int C, int ALG>
+// uv, when given, is this thread's shared-memory slice for the S-map solver's
+// rotation accumulators (2 (EA+1)^2 doubles, interleaved with stride
+// uv_stride).
+template<int EA, int C, int ALG, bool UVS = false>
 __device__ __noinline__ int finalize_point(const GroupParams& g, const MixedRun& m, const DevTask& T, long long p,
-                                           int prow, const Cand<C>& cand)
+                                           int prow, const Cand<C>& cand, double* uv = nullptr, int uv_stride = 0)
 {
   const float(&D)[C] = cand.D;
   const int(&I)[C] = cand.I;
@@ -256,7 +262,10 @@ __device__ __noinline__ int finalize_point(const GroupParams& g, const MixedRun&
     return ops + keff + g.n_thetas * keff * (EXP_OPS + 5);
   }
   else {
-    return ops + smap_point_local<EA>(g, p, prow, T.save_coeffs != 0, keff, rows, cd);
+    if constexpr (UVS)
+      return ops + smap_point_sm<EA>(g, p, prow, T.save_coeffs != 0, keff, rows, cd, uv, uv_stride);
+    else
+      return ops + smap_point_local<EA>(g, p, prow, T.save_coeffs != 0, keff, rows, cd);
   }
 }
 
@@ -274,10 +283,129 @@ __device__ __forceinline__ void offer(float (&D)[C], int (&I)[C], int& z, int (&
   }
 }
 
+// Barrier of the 256 scanning threads: the whole CTA in knn_mixed_kernel,
+// named barrier 1 in the warp-specialised kernel (whose solver warps never
+// take part in it).
+template<bool NAMED>
+__device__ __forceinline__ void scan_sync()
+{
+  if constexpr (NAMED)
+    asm volatile("bar.sync 1, %0;" ::"n"(TPB) : "memory");
+  else
+    __syncthreads();
+}
+
+// FP32 scan of one work item: thread tid scores the task's library against
+// prediction points first + tid and first + tid + 256 and copies their
+// candidate lists to c0 / c1 at the end (the lists live in private arrays
+// during the scan, so they stay in registers whatever the caller does with
+// c0 / c1).
+template<int EA, int C, bool NAMED>
+__device__ __forceinline__ void scan_item(const GroupParams& g, const MixedRun& m, const DevTask& T, int first,
+                                          int tid, float2* tile, Cand<C>& c0, Cand<C>& c1, int& prow0, int& prow1,
+                                          bool& a0, bool& a1)
+{
+  constexpr int S = EA <= 4 ? 4 : 8;  // row stride of the float manifold
+  const int pi0 = first + tid, pi1 = first + tid + TPB;
+  a0 = pi0 < T.n_pred;
+  a1 = pi1 < T.n_pred;
+  prow0 = a0 ? g.pred_rows[T.pred_off + pi0] : 0;
+  prow1 = a1 ? g.pred_rows[T.pred_off + pi1] : 0;
+  // negated prediction coordinates, duplicated in both halves; an idle slot
+  // sits at 1e30 so its squared distances overflow to +inf and never enter
+  float2 na[EA], nb[EA];
+#pragma unroll
+  for (int j = 0; j < EA; j++) {
+    const float va = a0 ? -m.Fp32[(size_t)prow0 * S + j] : -1e30f;
+    const float vb = a1 ? -m.Fp32[(size_t)prow1 * S + j] : -1e30f;
+    na[j] = make_float2(va, va);
+    nb[j] = make_float2(vb, vb);
+  }
+  float D0[C], D1[C];
+  int I0[C], I1[C];
+#pragma unroll
+  for (int j = 0; j < C; j++) {
+    D0[j] = D1[j] = INFINITY;
+    I0[j] = I1[j] = -1;
+  }
+  int z0 = 0, z1 = 0;
+  int zi0[ZCAP], zi1[ZCAP];
+#pragma unroll
+  for (int j = 0; j < ZCAP; j++)
+    zi0[j] = zi1[j] = -1;
+  for (int t0 = 0; t0 < T.n_lib; t0 += TILE) {
+    const int cnt = min(TILE, T.n_lib - t0);
+    const int npairs = (cnt + 1) >> 1;
+    scan_sync<NAMED>();
+    for (int i = tid; i < 2 * npairs; i += TPB) {
+      float* dst = reinterpret_cast<float*>(tile + (i >> 1) * EA) + (i & 1);
+      if (i < cnt) {
+        const float* src = m.F32 + (size_t)g.lib_rows[T.lib_off + t0 + i] * S;
+#pragma unroll
+        for (int j = 0; j < EA; j++)
+          dst[2 * j] = src[j];
+      } else {
+#pragma unroll
+        for (int j = 0; j < EA; j++)
+          dst[2 * j] = 1e30f;  // padding row: never a candidate
+      }
+    }
+    scan_sync<NAMED>();
+#pragma unroll 2
+    for (int ip = 0; ip < npairs; ip++) {
+      const float2* xr = tile + ip * EA;
+      float2 x = xr[0];
+      float2 da = __fadd2_rn(x, na[0]);
+      float2 db = __fadd2_rn(x, nb[0]);
+      float2 sa = __fmul2_rn(da, da);
+      float2 sb = __fmul2_rn(db, db);
+#pragma unroll
+      for (int j = 1; j < EA; j++) {
+        x = xr[j];
+        da = __fadd2_rn(x, na[j]);
+        db = __fadd2_rn(x, nb[j]);
+        sa = __ffma2_rn(da, da, sa);
+        sb = __ffma2_rn(db, db, sb);
+      }
+      if (fminf(sa.x, sa.y) < D0[C - 1] || fminf(sb.x, sb.y) < D1[C - 1]) {
+        const int li = t0 + 2 * ip;
+        offer<C>(D0, I0, z0, zi0, sa.x, li);
+        offer<C>(D0, I0, z0, zi0, sa.y, li + 1);
+        offer<C>(D1, I1, z1, zi1, sb.x, li);
+        offer<C>(D1, I1, z1, zi1, sb.y, li + 1);
+      }
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < C; j++) {
+    c0.D[j] = D0[j];
+    c0.I[j] = I0[j];
+    c1.D[j] = D1[j];
+    c1.I[j] = I1[j];
+  }
+  c0.z = z0;
+  c1.z = z1;
+#pragma unroll
+  for (int j = 0; j < ZCAP; j++) {
+    c0.zi[j] = zi0[j];
+    c1.zi[j] = zi1[j];
+  }
+}
+
+__device__ __forceinline__ void add_ops(const MixedRun& m, unsigned long long ops)
+{
+  // called by whole warps
+  if (m.fp64_ops) {
+    for (int o = 16; o > 0; o >>= 1)
+      ops += __shfl_xor_sync(0xffffffffu, ops, o);
+    if ((threadIdx.x & 31) == 0)
+      atomicAdd(m.fp64_ops, ops);
+  }
+}
+
 template<int EA, int C, int ALG>
 __global__ void __launch_bounds__(TPB, 2) knn_mixed_kernel(GroupParams g, MixedRun m)
 {
-  constexpr int S = EA <= 4 ? 4 : 8;  // row stride of the float manifold
   // library rows staged as interleaved pairs: tile[pair][dim] = (row 2i, row 2i+1)
   __shared__ __align__(16) float2 tile[(TILE / 2) * EA];
   __shared__ int s_item;
@@ -290,113 +418,215 @@ __global__ void __launch_bounds__(TPB, 2) knn_mixed_kernel(GroupParams g, MixedR
     __syncthreads();
     const int item = s_item;
     if (item >= m.item_end) {
-      // every thread of the CTA leaves here together: full warps
-      if (m.fp64_ops) {
-        for (int o = 16; o > 0; o >>= 1)
-          ops += __shfl_xor_sync(0xffffffffu, ops, o);
-        if ((tid & 31) == 0)
-          atomicAdd(m.fp64_ops, ops);
-      }
+      add_ops(m, ops);  // every thread of the CTA leaves here together
       return;
     }
     const int2 it = m.items[item];
     const DevTask T = g.tasks[it.x];
-    const int pi0 = it.y + tid, pi1 = it.y + tid + TPB;
-    const bool a0 = pi0 < T.n_pred, a1 = pi1 < T.n_pred;
-    const int prow0 = a0 ? g.pred_rows[T.pred_off + pi0] : 0;
-    const int prow1 = a1 ? g.pred_rows[T.pred_off + pi1] : 0;
-    // negated prediction coordinates, duplicated in both halves; an idle slot
-    // sits at 1e30 so its squared distances overflow to +inf and never enter
-    float2 na[EA], nb[EA];
-#pragma unroll
-    for (int j = 0; j < EA; j++) {
-      const float va = a0 ? -m.Fp32[(size_t)prow0 * S + j] : -1e30f;
-      const float vb = a1 ? -m.Fp32[(size_t)prow1 * S + j] : -1e30f;
-      na[j] = make_float2(va, va);
-      nb[j] = make_float2(vb, vb);
-    }
-    float D0[C], D1[C];
-    int I0[C], I1[C];
-#pragma unroll
-    for (int j = 0; j < C; j++) {
-      D0[j] = D1[j] = INFINITY;
-      I0[j] = I1[j] = -1;
-    }
-    int z0 = 0, z1 = 0;
-    int zi0[ZCAP], zi1[ZCAP];
-#pragma unroll
-    for (int j = 0; j < ZCAP; j++)
-      zi0[j] = zi1[j] = -1;
-    for (int t0 = 0; t0 < T.n_lib; t0 += TILE) {
-      const int cnt = min(TILE, T.n_lib - t0);
-      const int npairs = (cnt + 1) >> 1;
-      __syncthreads();
-      for (int i = tid; i < 2 * npairs; i += TPB) {
-        float* dst = reinterpret_cast<float*>(tile + (i >> 1) * EA) + (i & 1);
-        if (i < cnt) {
-          const float* src = m.F32 + (size_t)g.lib_rows[T.lib_off + t0 + i] * S;
-#pragma unroll
-          for (int j = 0; j < EA; j++)
-            dst[2 * j] = src[j];
-        } else {
-#pragma unroll
-          for (int j = 0; j < EA; j++)
-            dst[2 * j] = 1e30f;  // padding row: never a candidate
-        }
-      }
-      __syncthreads();
-#pragma unroll 2
-      for (int ip = 0; ip < npairs; ip++) {
-        const float2* xr = tile + ip * EA;
-        float2 x = xr[0];
-        float2 da = __fadd2_rn(x, na[0]);
-        float2 db = __fadd2_rn(x, nb[0]);
-        float2 sa = __fmul2_rn(da, da);
-        float2 sb = __fmul2_rn(db, db);
-#pragma unroll
-        for (int j = 1; j < EA; j++) {
-          x = xr[j];
-          da = __fadd2_rn(x, na[j]);
-          db = __fadd2_rn(x, nb[j]);
-          sa = __ffma2_rn(da, da, sa);
-          sb = __ffma2_rn(db, db, sb);
-        }
-        if (fminf(sa.x, sa.y) < D0[C - 1] || fminf(sb.x, sb.y) < D1[C - 1]) {
-          const int li = t0 + 2 * ip;
-          offer<C>(D0, I0, z0, zi0, sa.x, li);
-          offer<C>(D0, I0, z0, zi0, sa.y, li + 1);
-          offer<C>(D1, I1, z1, zi1, sb.x, li);
-          offer<C>(D1, I1, z1, zi1, sb.y, li + 1);
-        }
-      }
-    }
+    Cand<C> c0, c1;
+    int prow0, prow1;
+    bool a0, a1;
+    scan_item<EA, C, false>(g, m, T, it.y, tid, tile, c0, c1, prow0, prow1, a0, a1);
     if (a0) {
-      Cand<C> c;
-#pragma unroll
-      for (int j = 0; j < C; j++) {
-        c.D[j] = D0[j];
-        c.I[j] = I0[j];
-      }
-      c.z = z0;
-#pragma unroll
-      for (int j = 0; j < ZCAP; j++)
-        c.zi[j] = zi0[j];
-      ops += finalize_point<EA, C, ALG>(g, m, T, T.point_base + pi0, prow0, c);
+      const Cand<C> c = c0;
+      ops += finalize_point<EA, C, ALG>(g, m, T, T.point_base + it.y + tid, prow0, c);
     }
     if (a1) {
-      Cand<C> c;
-#pragma unroll
-      for (int j = 0; j < C; j++) {
-        c.D[j] = D1[j];
-        c.I[j] = I1[j];
-      }
-      c.z = z1;
-#pragma unroll
-      for (int j = 0; j < ZCAP; j++)
-        c.zi[j] = zi1[j];
-      ops += finalize_point<EA, C, ALG>(g, m, T, T.point_base + pi1, prow1, c);
+      const Cand<C> c = c1;
+      ops += finalize_point<EA, C, ALG>(g, m, T, T.point_base + it.y + tid + TPB, prow1, c);
     }
   }
+}
+
+// ---------------------------------------------------------------------------
+// Warp-specialised S-map kernel.  Warps 0-7 scan (FP32 pipe) and warps 8.. run
+// the FP64 re-rank and JacobiSVD solve (FP64 pipe) of the previous item, so the
+// two pipes work at the same time.  The scan warps hand each item's 512
+// candidate lists over through two shared-memory job buffers guarded by
+// mbarriers ("full": 256 scanner arrivals; "empty": one arrival per solver
+// thread).  Every wait is bounded: past WAIT_NS the waiter sets m.error and
+// leaves, so a broken hand-off ends the kernel with an error instead of a hang.
+
+template<int C>
+struct Job
+{
+  Cand<C> c;
+  long long p;  // global point id, -1 for an idle slot
+  int prow;
+};
+
+constexpr unsigned long long WAIT_NS = 5000000000ULL;
+
+__device__ __forceinline__ unsigned long long globaltimer_ns()
+{
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+__device__ __forceinline__ void mbar_init(unsigned long long* bar, int count)
+{
+  const unsigned a = (unsigned)__cvta_generic_to_shared(bar);
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(a), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(unsigned long long* bar)
+{
+  const unsigned a = (unsigned)__cvta_generic_to_shared(bar);
+  asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.shared::cta.b64 st, [%0];\n\t}" ::"r"(a) : "memory");
+}
+
+// Waits for the completion of the phase with the given parity; false after
+// WAIT_NS nanoseconds (or 2^30 polls) without it.
+__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, int parity)
+{
+  const unsigned a = (unsigned)__cvta_generic_to_shared(bar);
+  unsigned long long t0 = 0;
+  for (unsigned n = 0; n < (1u << 30); n++) {
+    unsigned ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(a), "r"(parity)
+        : "memory");
+    if (ok)
+      return true;
+    if ((n & 31) == 0) {
+      const unsigned long long t = globaltimer_ns();
+      if (t0 == 0)
+        t0 = t;
+      else if (t - t0 > WAIT_NS)
+        return false;
+    }
+  }
+  return false;
+}
+
+// AND of v over the N threads of named barrier ID (a barrier as well), so a
+// role takes the same branch on every thread even if one thread's wait ran out.
+template<int ID, int N>
+__device__ __forceinline__ bool group_and(bool v)
+{
+  unsigned r;
+  asm volatile(
+      "{\n\t.reg .pred p, q;\n\tsetp.ne.u32 q, %1, 0;\n\tbar.red.and.pred p, %2, %3, q;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(r)
+      : "r"((unsigned)v), "n"(ID), "n"(N)
+      : "memory");
+  return r != 0;
+}
+
+constexpr size_t SMEM_LIMIT = 227 * 1024;
+
+template<int EA, int C>
+__host__ __device__ constexpr size_t ws_base_bytes()
+{
+  return (size_t)(TILE / 2) * EA * sizeof(float2) + 2 * (size_t)(2 * TPB) * sizeof(Job<C>);
+}
+
+// The solver threads' U and V (2 (EA+1)^2 doubles each) go to shared memory
+// when they fit beside the tile and the job buffers (E_a = 4: 100 KB for 256
+// solver threads); otherwise the solver keeps them in local memory.
+template<int EA, int C, int SW>
+__host__ __device__ constexpr bool ws_uv_in_smem()
+{
+  return ws_base_bytes<EA, C>() + (size_t)2 * (EA + 1) * (EA + 1) * 32 * SW * sizeof(double) + 1024 <= SMEM_LIMIT;
+}
+
+template<int EA, int C, int SW>
+__host__ __device__ constexpr size_t ws_smem_bytes()
+{
+  return ws_base_bytes<EA, C>() +
+         (ws_uv_in_smem<EA, C, SW>() ? (size_t)2 * (EA + 1) * (EA + 1) * 32 * SW * sizeof(double) : 0);
+}
+
+template<int EA, int C, int SW>
+__global__ void __launch_bounds__(TPB + 32 * SW, 1) knn_smap_ws_kernel(GroupParams g, MixedRun m)
+{
+  constexpr int NS = 32 * SW;  // solver threads
+  constexpr int JOBS = 2 * TPB;
+  extern __shared__ __align__(16) unsigned char smem[];
+  float2* tile = reinterpret_cast<float2*>(smem);
+  Job<C>* jobs = reinterpret_cast<Job<C>*>(smem + (size_t)(TILE / 2) * EA * sizeof(float2));
+  double* uv_all = reinterpret_cast<double*>(smem + ws_base_bytes<EA, C>());
+  __shared__ unsigned long long full_bar[2], empty_bar[2];
+  __shared__ DevTask s_task[2];
+  __shared__ int s_end[2];
+  __shared__ int s_item;
+  const int tid = threadIdx.x;
+  if (tid == 0) {
+    mbar_init(&full_bar[0], TPB);
+    mbar_init(&full_bar[1], TPB);
+    mbar_init(&empty_bar[0], NS);
+    mbar_init(&empty_bar[1], NS);
+  }
+  __syncthreads();
+  unsigned long long ops = 0;
+  if (tid < TPB) {
+    for (int it = 0;; it++) {
+      const int b = it & 1, k = it >> 1;
+      scan_sync<true>();  // everyone has read the previous s_item
+      if (tid == 0)
+        s_item = m.item_begin + atomicAdd(m.counter, 1);
+      scan_sync<true>();
+      const int item = s_item;
+      // buffer b is free once the solvers finished its previous use (the
+      // first use waits on the phase before the barrier's first one, which
+      // counts as complete)
+      if (!group_and<1, TPB>(mbar_wait(&empty_bar[b], (k & 1) ^ 1))) {
+        if (tid == 0)
+          atomicExch(m.error, 1);
+        break;
+      }
+      if (item >= m.item_end) {
+        if (tid == 0)
+          s_end[b] = 1;
+        mbar_arrive(&full_bar[b]);
+        break;
+      }
+      const int2 iv = m.items[item];
+      const DevTask T = g.tasks[iv.x];
+      if (tid == 0) {
+        s_task[b] = T;
+        s_end[b] = 0;
+      }
+      Job<C>& j0 = jobs[b * JOBS + tid];
+      Job<C>& j1 = jobs[b * JOBS + tid + TPB];
+      int prow0, prow1;
+      bool a0, a1;
+      Cand<C> c0, c1;
+      scan_item<EA, C, true>(g, m, T, iv.y, tid, tile, c0, c1, prow0, prow1, a0, a1);
+      j0.c = c0;
+      j0.p = a0 ? T.point_base + iv.y + tid : -1;
+      j0.prow = prow0;
+      j1.c = c1;
+      j1.p = a1 ? T.point_base + iv.y + tid + TPB : -1;
+      j1.prow = prow1;
+      mbar_arrive(&full_bar[b]);
+    }
+  } else {
+    const int st = tid - TPB;
+    constexpr bool UVS = ws_uv_in_smem<EA, C, SW>();
+    double* uv = UVS ? uv_all + st : nullptr;
+    for (int it = 0;; it++) {
+      const int b = it & 1, k = it >> 1;
+      if (!group_and<2, NS>(mbar_wait(&full_bar[b], k & 1))) {
+        if (st == 0)
+          atomicExch(m.error, 1);
+        break;
+      }
+      if (s_end[b])
+        break;
+      const DevTask T = s_task[b];
+      for (int j = st; j < JOBS; j += NS) {
+        const Job<C>& jb = jobs[b * JOBS + j];
+        if (jb.p >= 0)
+          ops += finalize_point<EA, C, 1, UVS>(g, m, T, jb.p, jb.prow, jb.c, uv, NS);
+      }
+      mbar_arrive(&empty_bar[b]);
+    }
+  }
+  add_ops(m, ops);  // both roles leave their loops as whole warps
 }
 
 // S-map forecast of one point from its neighbour rows and FP64 distances,
@@ -521,6 +751,71 @@ __device__ __noinline__ int smap_point_local(const GroupParams& g, long long p, 
   return ops;
 }
 
+// The same forecast with the normal matrix in registers and the solver's
+// rotation accumulators in the caller's shared-memory slice (the
+// warp-specialised kernel's solver threads).  Identical operations and bits.
+template<int EA>
+__device__ __noinline__ int smap_point_sm(const GroupParams& g, long long p, int prow, bool save, int keff,
+                                          const int* rows, const double* cd, double* uv, int uv_stride)
+{
+  constexpr int n = EA + 1;
+  int ops = keff + 1 + g.n_thetas * (keff * (EXP_OPS + 2 + n + n * (n + 1) + 2 * n) + 2 * EA);
+  double y[EA];
+#pragma unroll
+  for (int j = 0; j < EA; j++)
+    y[j] = g.Fp[(size_t)prow * EA + j];
+  double mean = 0;
+  for (int j = 0; j < keff; j++)
+    mean = add(mean, cd[j]);
+  mean = dvd(mean, (double)keff);
+  const StridedMat<n> U{ uv, uv_stride }, V{ uv + n * n * uv_stride, uv_stride };
+  for (int t = 0; t < g.n_thetas; t++) {
+    const double theta = g.thetas[t];
+    double W[n][n], bv[n], xs[n];
+#pragma unroll
+    for (int a = 0; a < n; a++) {
+      bv[a] = 0;
+#pragma unroll
+      for (int b = 0; b < n; b++)
+        W[a][b] = 0;
+    }
+    for (int i = 0; i < keff; i++) {
+      const double w = exp_rn(mul(-theta, dvd(cd[i], mean)));
+      const int row = rows[i];
+      double xr[n];
+      xr[0] = w;
+#pragma unroll
+      for (int j = 1; j < n; j++)
+        xr[j] = mul(w, g.F[(size_t)row * EA + j - 1]);
+      const double yl = mul(w, g.lib_target[row]);
+#pragma unroll
+      for (int a = 0; a < n; a++) {
+#pragma unroll
+        for (int b = a; b < n; b++)
+          W[a][b] = add(W[a][b], mul(xr[a], xr[b]));
+        bv[a] = add(bv[a], mul(xr[a], yl));
+      }
+    }
+#pragma unroll
+    for (int a = 0; a < n; a++)
+#pragma unroll
+      for (int b = 0; b < a; b++)
+        W[a][b] = W[b][a];
+    svd_solve_nm<n>(W, bv, xs, U, V, ops);
+    double r = xs[0];
+#pragma unroll
+    for (int j = 0; j < EA; j++)
+      r = add(r, mul(y[j], xs[j + 1]));
+    if (g.coeffs && save && t == g.n_thetas - 1) {
+#pragma unroll
+      for (int j = 0; j < n; j++)
+        g.coeffs[(size_t)p * n + j] = fabs(xs[j]) < 1.0e-11 ? MISS : xs[j];
+    }
+    g.pred[(size_t)t * g.total_points + p] = r;
+  }
+  return ops;
+}
+
 template<int EA>
 __global__ void __launch_bounds__(128) smap_lists_kernel(GroupParams g, MixedRun m)
 {
@@ -607,18 +902,47 @@ void launch_one(const GroupParams& g, const MixedRun& m, int num_sms, cudaStream
   knn_mixed_kernel<EA, C, ALG><<<(int)blocks, TPB, 0, s>>>(g, m);
 }
 
+template<int EA, int C, int SW>
+void launch_ws(const GroupParams& g, const MixedRun& m, int num_sms, cudaStream_t s)
+{
+  const size_t smem = ws_smem_bytes<EA, C, SW>();
+  cudaFuncSetAttribute(knn_smap_ws_kernel<EA, C, SW>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  int per_sm = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, knn_smap_ws_kernel<EA, C, SW>, TPB + 32 * SW, smem);
+  if (per_sm < 1)
+    per_sm = 1;
+  long long blocks = (long long)num_sms * per_sm;
+  if (blocks > m.item_end - m.item_begin)
+    blocks = m.item_end - m.item_begin;
+  if (blocks < 1)
+    blocks = 1;
+  knn_smap_ws_kernel<EA, C, SW><<<(int)blocks, TPB + 32 * SW, smem, s>>>(g, m);
+}
+
+template<int EA, int C, int ALG>
+void launch_ea(const GroupParams& g, const MixedRun& m, int num_sms, cudaStream_t s)
+{
+  if constexpr (ALG == 1) {
+    if (m.solver_warps == 4)
+      return launch_ws<EA, C, 4>(g, m, num_sms, s);
+    if (m.solver_warps == 8)
+      return launch_ws<EA, C, 8>(g, m, num_sms, s);
+  }
+  launch_one<EA, C, ALG>(g, m, num_sms, s);
+}
+
 template<int C, int ALG>
 void launch_c(const GroupParams& g, const MixedRun& m, int num_sms, cudaStream_t s)
 {
   switch (g.Ea) {
-    case 1: launch_one<1, C, ALG>(g, m, num_sms, s); break;
-    case 2: launch_one<2, C, ALG>(g, m, num_sms, s); break;
-    case 3: launch_one<3, C, ALG>(g, m, num_sms, s); break;
-    case 4: launch_one<4, C, ALG>(g, m, num_sms, s); break;
-    case 5: launch_one<5, C, ALG>(g, m, num_sms, s); break;
-    case 6: launch_one<6, C, ALG>(g, m, num_sms, s); break;
-    case 7: launch_one<7, C, ALG>(g, m, num_sms, s); break;
-    case 8: launch_one<8, C, ALG>(g, m, num_sms, s); break;
+    case 1: launch_ea<1, C, ALG>(g, m, num_sms, s); break;
+    case 2: launch_ea<2, C, ALG>(g, m, num_sms, s); break;
+    case 3: launch_ea<3, C, ALG>(g, m, num_sms, s); break;
+    case 4: launch_ea<4, C, ALG>(g, m, num_sms, s); break;
+    case 5: launch_ea<5, C, ALG>(g, m, num_sms, s); break;
+    case 6: launch_ea<6, C, ALG>(g, m, num_sms, s); break;
+    case 7: launch_ea<7, C, ALG>(g, m, num_sms, s); break;
+    case 8: launch_ea<8, C, ALG>(g, m, num_sms, s); break;
     default: break;
   }
 }

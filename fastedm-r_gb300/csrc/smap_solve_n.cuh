@@ -1,7 +1,9 @@
 // The JacobiSVD restatement of smap_solve.cuh for a compile-time size N,
-// fully unrolled so the work matrix and both rotation accumulators live in
-// registers.  Every floating-point operation and its order are those of
-// svd_solve(): the results are the same bits.
+// fully unrolled so the work matrix lives in registers.  The two rotation
+// accumulators U and V are reached through an accessor: registers
+// (svd_solve_n) or a per-thread slice of shared memory interleaved across
+// threads (svd_solve_nm with StridedMat).  Every floating-point operation and
+// its order are those of svd_solve(): the results are the same bits.
 #pragma once
 
 #include <cfloat>
@@ -10,8 +12,29 @@
 
 namespace fedm {
 
+// N x N matrix of one thread stored element-major across `stride` threads:
+// element (i, j) at base[(i * N + j) * stride], so a warp touching the same
+// element reads consecutive doubles.
 template<int N>
-__device__ __forceinline__ void svd_solve_n(double (&W)[N][N], const double (&b)[N], double (&x)[N])
+struct StridedMat
+{
+  double* base;
+  int stride;
+  __device__ __forceinline__ double& operator()(int i, int j) const { return base[(i * N + j) * stride]; }
+};
+
+template<int N>
+struct RegMat
+{
+  double (&m)[N][N];
+  __device__ __forceinline__ double& operator()(int i, int j) const { return m[i][j]; }
+};
+
+// ops accumulates the FP64 add/sub/mul/div/sqrt operations performed, with
+// the same rules as svd_solve.
+template<int N, class M>
+__device__ __forceinline__ void svd_solve_nm(double (&W)[N][N], const double (&b)[N], double (&x)[N], const M& U,
+                                             const M& V, int& ops)
 {
   const double tiny = DBL_MIN, eps = DBL_EPSILON, precision = 2 * DBL_EPSILON;
   double scale = 0;
@@ -28,15 +51,15 @@ __device__ __forceinline__ void svd_solve_n(double (&W)[N][N], const double (&b)
   }
   if (scale == 0)
     scale = 1;
-  double U[N][N], V[N][N];
 #pragma unroll
   for (int i = 0; i < N; i++)
 #pragma unroll
     for (int j = 0; j < N; j++) {
       W[i][j] = dvd(W[i][j], scale);
-      U[i][j] = i == j ? 1.0 : 0.0;
-      V[i][j] = i == j ? 1.0 : 0.0;
+      U(i, j) = i == j ? 1.0 : 0.0;
+      V(i, j) = i == j ? 1.0 : 0.0;
     }
+  ops += N * N;
   double maxDiag = 0;
 #pragma unroll
   for (int i = 0; i < N; i++)
@@ -51,8 +74,10 @@ __device__ __forceinline__ void svd_solve_n(double (&W)[N][N], const double (&b)
 #pragma unroll
       for (int q = 0; q < p; q++) {
         const double threshold = fmax(tiny, mul(precision, maxDiag));
+        ops += 1;
         if (fabs(W[p][q]) > threshold || fabs(W[q][p]) > threshold) {
           finished = false;
+          ops += 18 + 24 * N;
           // real_2x2_jacobi_svd on rows/cols p, q
           const double m00 = W[p][p], m01 = W[p][q], m10 = W[q][p], m11 = W[q][q];
           double r1c, r1s;
@@ -65,6 +90,7 @@ __device__ __forceinline__ void svd_solve_n(double (&W)[N][N], const double (&b)
             const double tmp = __dsqrt_rn(add(1.0, mul(u, u)));
             r1s = dvd(1.0, tmp);
             r1c = dvd(u, tmp);
+            ops += 6;
           }
           const double n00 = add(mul(r1c, m00), mul(r1s, m10));
           const double n01 = add(mul(r1c, m01), mul(r1s, m11));
@@ -84,6 +110,7 @@ __device__ __forceinline__ void svd_solve_n(double (&W)[N][N], const double (&b)
             const bool neg = (sign_t > 0) == (n01 > 0);
             jrs = mul(neg ? -fabs(tt) : fabs(tt), nn);
             jrc = nn;
+            ops += 12;
           }
           const double jtc = jrc, jts = -jrs;
           const double jlc = sub(mul(r1c, jtc), mul(r1s, jts));
@@ -100,9 +127,9 @@ __device__ __forceinline__ void svd_solve_n(double (&W)[N][N], const double (&b)
             const double c = jlc, s = jls;  // transpose of (jlc, -jls)
 #pragma unroll
             for (int i = 0; i < N; i++) {
-              const double xv = U[i][p], yv = U[i][q];
-              U[i][p] = add(mul(c, xv), mul(s, yv));
-              U[i][q] = add(mul(-s, xv), mul(c, yv));
+              const double xv = U(i, p), yv = U(i, q);
+              U(i, p) = add(mul(c, xv), mul(s, yv));
+              U(i, q) = add(mul(-s, xv), mul(c, yv));
             }
           }
           // W.applyOnTheRight(p, q, jr) and V.applyOnTheRight(p, q, jr)
@@ -116,9 +143,9 @@ __device__ __forceinline__ void svd_solve_n(double (&W)[N][N], const double (&b)
             }
 #pragma unroll
             for (int i = 0; i < N; i++) {
-              const double xv = V[i][p], yv = V[i][q];
-              V[i][p] = add(mul(c, xv), mul(s, yv));
-              V[i][q] = add(mul(-s, xv), mul(c, yv));
+              const double xv = V(i, p), yv = V(i, q);
+              V(i, p) = add(mul(c, xv), mul(s, yv));
+              V(i, q) = add(mul(-s, xv), mul(c, yv));
             }
           }
           maxDiag = fmax(maxDiag, fmax(fabs(W[p][p]), fabs(W[q][q])));
@@ -134,12 +161,13 @@ __device__ __forceinline__ void svd_solve_n(double (&W)[N][N], const double (&b)
     if (a < 0) {
 #pragma unroll
       for (int r = 0; r < N; r++)
-        U[r][i] = -U[r][i];
+        U(r, i) = -U(r, i);
     }
   }
 #pragma unroll
   for (int i = 0; i < N; i++)
     sv[i] = mul(sv[i], scale);
+  ops += N + 2;
   int nonzero = N;
   bool stop = false;
 #pragma unroll
@@ -165,12 +193,12 @@ __device__ __forceinline__ void svd_solve_n(double (&W)[N][N], const double (&b)
             sv[j] = s0;
 #pragma unroll
             for (int r = 0; r < N; r++) {
-              const double u0 = U[r][i];
-              U[r][i] = U[r][j];
-              U[r][j] = u0;
-              const double v0 = V[r][i];
-              V[r][i] = V[r][j];
-              V[r][j] = v0;
+              const double u0 = U(r, i);
+              U(r, i) = U(r, j);
+              U(r, j) = u0;
+              const double v0 = V(r, i);
+              V(r, i) = V(r, j);
+              V(r, j) = v0;
             }
           }
         }
@@ -192,7 +220,7 @@ __device__ __forceinline__ void svd_solve_n(double (&W)[N][N], const double (&b)
       double s = 0;
 #pragma unroll
       for (int r = 0; r < N; r++)
-        s = add(s, mul(U[r][cc], b[r]));
+        s = add(s, mul(U(r, cc), b[r]));
       tmp[cc] = mul(dvd(1.0, sv[cc]), s);
     }
   }
@@ -202,9 +230,18 @@ __device__ __forceinline__ void svd_solve_n(double (&W)[N][N], const double (&b)
 #pragma unroll
     for (int cc = 0; cc < N; cc++)
       if (cc < rank)
-        s = add(s, mul(V[r][cc], tmp[cc]));
+        s = add(s, mul(V(r, cc), tmp[cc]));
     x[r] = s;
   }
+  ops += rank * (2 * N + 2) + 2 * N * rank;
+}
+
+template<int N>
+__device__ __forceinline__ void svd_solve_n(double (&W)[N][N], const double (&b)[N], double (&x)[N])
+{
+  double Ur[N][N], Vr[N][N];
+  int ops = 0;
+  svd_solve_nm<N>(W, b, x, RegMat<N>{ Ur }, RegMat<N>{ Vr }, ops);
 }
 
 } // namespace fedm

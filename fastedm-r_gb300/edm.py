@@ -67,7 +67,8 @@ class Timing(C.Structure):
         ("device_ms", C.c_double), ("knn_kernel_ms", C.c_double), ("knn_launches", C.c_int),
         ("host_ms", C.c_double), ("distance_pairs", C.c_longlong), ("predictions", C.c_longlong),
         ("h2d_bytes", C.c_longlong), ("d2h_bytes", C.c_longlong), ("fallback_points", C.c_int),
-        ("kernel_launches", C.c_int), ("fp64_ops", C.c_longlong),
+        ("kernel_launches", C.c_int), ("fp64_ops", C.c_longlong), ("list_wait_ms", C.c_double),
+        ("setup_ms", C.c_double), ("finish_ms", C.c_double),
     ]
 
 

@@ -186,6 +186,12 @@ typedef struct fedm_timing {
   int kernel_launches;       /* kernels this library launched                */
   long long fp64_ops;        /* mixed path: FP64 add/sub/mul/div/sqrt of the
                                 re-rank and forecast stage (exp = 32)        */
+  double list_wait_ms;       /* host time blocked on CCM library lists that
+                                the background splitter had not finished     */
+  double setup_ms;           /* host time preparing task batches before their
+                                first kernel (row pools, uploads)            */
+  double finish_ms;          /* host time after each batch's statistics
+                                (downloads, per-task results)                */
 } fedm_timing;
 
 int fedm_last_timing(const fedm_ctx* ctx, fedm_timing* out);

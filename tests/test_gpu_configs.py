@@ -126,3 +126,26 @@ def test_mixed_fp64_operation_count(ctx):
         assert 250 <= per["simplex"] <= 1000, per
         # S-map E=4, k=6: ~25 Jacobi rotations of ~170 ops plus the normal equations
         assert 2000 <= per["smap"] <= 20000, per
+
+
+@pytest.mark.parametrize("solver_warps", ["0", "4", "8"])
+def test_smap_kernel_forms_agree(solver_warps, monkeypatch):
+    """The mixed S-map runs in one of three kernel forms: every warp scans
+    then solves (0), or 8 scan warps hand candidate lists to 4 or 8 FP64
+    solver warps through shared memory.  All give the FP64 path's bits."""
+    monkeypatch.setenv("FEDM_SMAP_SOLVER_WARPS", solver_warps)
+    w = workloads.ccm_config(T=6000, reps=3, n_libs=5, hi=5000)
+    kw = dict(E=4, library=w["libraries"], numReps=3, seed=w["seed"], algorithm="smap", theta=2.0,
+              savePredictions=True, saveSMAPCoeffs=True)
+    cm = fedm.Context(0, precision=fedm.PRECISION_MIXED)
+    c64 = fedm.Context(0, precision=fedm.PRECISION_FP64)
+    try:
+        g = fedm.edm(w["t"], w["x"], w["y"], ctx=cm, **kw)
+        f = fedm.edm(w["t"], w["x"], w["y"], ctx=c64, **kw)
+    finally:
+        cm.close()
+        c64.close()
+    assert g["rc"] == f["rc"] == 0
+    assert np.array_equal(g["stats"]["rho"], f["stats"]["rho"], equal_nan=True)
+    assert np.array_equal(g["predictions"], f["predictions"], equal_nan=True)
+    assert np.array_equal(g["coeffs"], f["coeffs"], equal_nan=True)
