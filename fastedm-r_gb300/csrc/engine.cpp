@@ -280,6 +280,10 @@ struct GroupJob
   std::vector<const std::vector<int>*> lib_lists, pred_lists;
   bool detail = false;          // keep per-point outputs and neighbour lists
   bool knn_for_all = false;     // route all-neighbour tasks through the list path
+  // optional: rows containing every library list of the job (the usable rows
+  // for lazily produced CCM lists); the mixed path's bounding box is then
+  // taken over it once instead of over each list
+  const std::vector<int>* lib_superset = nullptr;
 };
 
 constexpr int KCAP_MAX = 16384;
@@ -315,8 +319,10 @@ bool mixed_eligible(const Context& ctx, const Options& o, const GroupJob& job, s
     return true;
   };
   std::vector<const std::vector<int>*> seen_l, seen_p;
+  if (job.lib_superset && !scan(*job.hF, *job.lib_superset))
+    return false;
   for (size_t i = 0; i < job.lib_lists.size(); i++) {
-    if (std::find(seen_l.begin(), seen_l.end(), job.lib_lists[i]) == seen_l.end()) {
+    if (!job.lib_superset && std::find(seen_l.begin(), seen_l.end(), job.lib_lists[i]) == seen_l.end()) {
       seen_l.push_back(job.lib_lists[i]);
       if (!scan(*job.hF, *job.lib_lists[i]))
         return false;
@@ -940,6 +946,8 @@ CommandResult run_command(Context& ctx, const fedm_args& a)
     for (int i = 0; i < (int)plan.tasks.size(); i++)
       if (plan.tasks[i].E == key.first && plan.tasks[i].copredict == key.second)
         ids.push_back(i);
+    if (producer)
+      job.lib_superset = &plan.lazy.urows;
     // With lazy lists the group runs in about LAZY_BATCHES batches of tasks
     // in plan order (replicates outermost, so every batch spans all library
     // sizes); each waits only for its own lists.
