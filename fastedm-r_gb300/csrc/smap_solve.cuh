@@ -18,14 +18,48 @@ __device__ __forceinline__ double mul(double a, double b) { return __dmul_rn(a, 
 __device__ __forceinline__ double add(double a, double b) { return __dadd_rn(a, b); }
 __device__ __forceinline__ double sub(double a, double b) { return __dsub_rn(a, b); }
 __device__ __forceinline__ double dvd(double a, double b) { return __ddiv_rn(a, b); }
+// 1.0 / a, correctly rounded (IEEE round-to-nearest): the same bits as
+// dvd(1.0, a).
+__device__ __forceinline__ double rcp(double a) { return __drcp_rn(a); }
+
+// The Jacobi sweep's magnitude tests run on integers, off the FP64 pipe.
+// mag_bits(x) is |x| as its bit pattern, whose integer order is the order of
+// the magnitudes; NaN maps to -1 so, like a floating-point comparison with
+// NaN, it never exceeds a threshold and never wins a maximum.
+__device__ __forceinline__ long long mag_bits(double x)
+{
+  const long long b = __double_as_longlong(x) & 0x7fffffffffffffffLL;
+  return b > 0x7ff0000000000000LL ? -1 : b;
+}
+
+// Bits of fmax(DBL_MIN, 2 DBL_EPSILON * m) for m = mag_bits of a finite
+// m >= 0: the product is a power-of-two scaling, exact (exponent field less
+// 51) unless it falls below DBL_MIN, where the maximum is DBL_MIN.
+__device__ __forceinline__ long long jacobi_threshold_bits(long long m)
+{
+  constexpr long long TINY = 1LL << 52;  // bits of DBL_MIN
+  return m >= (52LL << 52) ? m - (51LL << 52) : TINY;
+}
 
 struct Rot
 {
   double c, s;
 };
 
+// A matrix element e of one thread stored at base[e * stride] (shared
+// memory interleaved across threads); indexes like a double*.
+struct LaneMat
+{
+  double* base;
+  int stride;
+  __device__ __forceinline__ double& operator[](int e) const { return base[e * stride]; }
+};
+
+// The helpers below take the matrix as a double* or a LaneMat.
+
 // rows p, q <- J [row p; row q], J = [c s; -s c]
-__device__ __forceinline__ void rot_rows(double* A, int n, int p, int q, Rot j)
+template<class Mat>
+__device__ __forceinline__ void rot_rows(Mat A, int n, int p, int q, Rot j)
 {
   for (int i = 0; i < n; i++) {
     const double x = A[p * n + i], y = A[q * n + i];
@@ -35,7 +69,8 @@ __device__ __forceinline__ void rot_rows(double* A, int n, int p, int q, Rot j)
 }
 
 // cols p, q <- [col p, col q] J^T  (Eigen's applyOnTheRight)
-__device__ __forceinline__ void rot_cols(double* A, int n, int p, int q, Rot j)
+template<class Mat>
+__device__ __forceinline__ void rot_cols(Mat A, int n, int p, int q, Rot j)
 {
   const double c = j.c, s = -j.s;
   for (int i = 0; i < n; i++) {
@@ -46,7 +81,8 @@ __device__ __forceinline__ void rot_cols(double* A, int n, int p, int q, Rot j)
 }
 
 // ops counts the FP64 add/sub/mul/div/sqrt operations performed.
-__device__ inline void jacobi_2x2(const double* W, int n, int p, int q, Rot& jl, Rot& jr, int& ops)
+template<class Mat>
+__device__ inline void jacobi_2x2(const Mat W, int n, int p, int q, Rot& jl, Rot& jr, int& ops)
 {
   ops += 18;
   const double tiny = DBL_MIN;
@@ -59,7 +95,7 @@ __device__ inline void jacobi_2x2(const double* W, int n, int p, int q, Rot& jl,
   } else {
     const double u = dvd(t, d);
     const double tmp = __dsqrt_rn(add(1.0, mul(u, u)));
-    r1.s = dvd(1.0, tmp);
+    r1.s = rcp(tmp);
     r1.c = dvd(u, tmp);
     ops += 6;
   }
@@ -73,9 +109,9 @@ __device__ inline void jacobi_2x2(const double* W, int n, int p, int q, Rot& jl,
   } else {
     const double tau = dvd(sub(n00, n11), deno);
     const double w = __dsqrt_rn(add(mul(tau, tau), 1.0));
-    const double tt = tau > 0 ? dvd(1.0, add(tau, w)) : dvd(1.0, sub(tau, w));
+    const double tt = rcp(tau > 0 ? add(tau, w) : sub(tau, w));
     const double sign_t = tt > 0 ? 1.0 : -1.0;
-    const double nn = dvd(1.0, __dsqrt_rn(add(mul(tt, tt), 1.0)));
+    const double nn = rcp(__dsqrt_rn(add(mul(tt, tt), 1.0)));
     // Eigen forms -sign_t * (n01 / |n01|) * |tt| * nn left to right; the
     // first two products are exact sign changes (n01 is finite and nonzero
     // here), so only the last multiply rounds.
@@ -95,7 +131,7 @@ __device__ inline void jacobi_2x2(const double* W, int n, int p, int q, Rot& jl,
 __device__ inline void svd_solve(double* W, double* U, double* V, double* sv, double* tmp, const double* b, double* x,
                                  int n, int& ops)
 {
-  const double tiny = DBL_MIN, eps = DBL_EPSILON, precision = 2 * DBL_EPSILON;
+  const double tiny = DBL_MIN, eps = DBL_EPSILON;
   double scale = 0;
   for (int i = 0; i < n * n; i++)
     scale = fmax(scale, fabs(W[i]));
@@ -114,9 +150,9 @@ __device__ inline void svd_solve(double* W, double* U, double* V, double* sv, do
   ops += n * n;
   for (int i = 0; i < n; i++)
     U[i * n + i] = V[i * n + i] = 1;
-  double maxDiag = 0;
+  long long maxDiag = 0;  // as mag_bits
   for (int i = 0; i < n; i++)
-    maxDiag = fmax(maxDiag, fabs(W[i * n + i]));
+    maxDiag = max(maxDiag, mag_bits(W[i * n + i]));
   bool finished = false;
   int sweeps = 0;
   while (!finished && sweeps < 100) {
@@ -124,9 +160,9 @@ __device__ inline void svd_solve(double* W, double* U, double* V, double* sv, do
     sweeps++;
     for (int p = 1; p < n; p++) {
       for (int q = 0; q < p; q++) {
-        const double threshold = fmax(tiny, mul(precision, maxDiag));
-        ops += 1;
-        if (fabs(W[p * n + q]) > threshold || fabs(W[q * n + p]) > threshold) {
+        // fmax(tiny, precision * maxDiag), precision = 2 DBL_EPSILON
+        const long long threshold = jacobi_threshold_bits(maxDiag);
+        if (mag_bits(W[p * n + q]) > threshold || mag_bits(W[q * n + p]) > threshold) {
           finished = false;
           Rot jl, jr;
           jacobi_2x2(W, n, p, q, jl, jr, ops);
@@ -135,7 +171,7 @@ __device__ inline void svd_solve(double* W, double* U, double* V, double* sv, do
           rot_cols(U, n, p, q, Rot{ jl.c, -jl.s });
           rot_cols(W, n, p, q, jr);
           rot_cols(V, n, p, q, jr);
-          maxDiag = fmax(maxDiag, fmax(fabs(W[p * n + p]), fabs(W[q * n + q])));
+          maxDiag = max(maxDiag, max(mag_bits(W[p * n + p]), mag_bits(W[q * n + q])));
         }
       }
     }
@@ -186,7 +222,7 @@ __device__ inline void svd_solve(double* W, double* U, double* V, double* sv, do
     double s = 0;
     for (int r = 0; r < n; r++)
       s = add(s, mul(U[r * n + cc], b[r]));
-    tmp[cc] = mul(dvd(1.0, sv[cc]), s);
+    tmp[cc] = mul(rcp(sv[cc]), s);
   }
   for (int r = 0; r < n; r++) {
     double s = 0;

@@ -36,7 +36,7 @@ template<int N, class M>
 __device__ __forceinline__ void svd_solve_nm(double (&W)[N][N], const double (&b)[N], double (&x)[N], const M& U,
                                              const M& V, int& ops)
 {
-  const double tiny = DBL_MIN, eps = DBL_EPSILON, precision = 2 * DBL_EPSILON;
+  const double tiny = DBL_MIN, eps = DBL_EPSILON;
   double scale = 0;
 #pragma unroll
   for (int i = 0; i < N; i++)
@@ -60,10 +60,10 @@ __device__ __forceinline__ void svd_solve_nm(double (&W)[N][N], const double (&b
       V(i, j) = i == j ? 1.0 : 0.0;
     }
   ops += N * N;
-  double maxDiag = 0;
+  long long maxDiag = 0;  // as mag_bits
 #pragma unroll
   for (int i = 0; i < N; i++)
-    maxDiag = fmax(maxDiag, fabs(W[i][i]));
+    maxDiag = max(maxDiag, mag_bits(W[i][i]));
   bool finished = false;
   int sweeps = 0;
   while (!finished && sweeps < 100) {
@@ -73,9 +73,9 @@ __device__ __forceinline__ void svd_solve_nm(double (&W)[N][N], const double (&b
     for (int p = 1; p < N; p++) {
 #pragma unroll
       for (int q = 0; q < p; q++) {
-        const double threshold = fmax(tiny, mul(precision, maxDiag));
-        ops += 1;
-        if (fabs(W[p][q]) > threshold || fabs(W[q][p]) > threshold) {
+        // fmax(tiny, precision * maxDiag), precision = 2 DBL_EPSILON
+        const long long threshold = jacobi_threshold_bits(maxDiag);
+        if (mag_bits(W[p][q]) > threshold || mag_bits(W[q][p]) > threshold) {
           finished = false;
           ops += 18 + 24 * N;
           // real_2x2_jacobi_svd on rows/cols p, q
@@ -88,7 +88,7 @@ __device__ __forceinline__ void svd_solve_nm(double (&W)[N][N], const double (&b
           } else {
             const double u = dvd(t, d);
             const double tmp = __dsqrt_rn(add(1.0, mul(u, u)));
-            r1s = dvd(1.0, tmp);
+            r1s = rcp(tmp);
             r1c = dvd(u, tmp);
             ops += 6;
           }
@@ -103,9 +103,9 @@ __device__ __forceinline__ void svd_solve_nm(double (&W)[N][N], const double (&b
           } else {
             const double tau = dvd(sub(n00, n11), deno);
             const double w = __dsqrt_rn(add(mul(tau, tau), 1.0));
-            const double tt = tau > 0 ? dvd(1.0, add(tau, w)) : dvd(1.0, sub(tau, w));
+            const double tt = rcp(tau > 0 ? add(tau, w) : sub(tau, w));
             const double sign_t = tt > 0 ? 1.0 : -1.0;
-            const double nn = dvd(1.0, __dsqrt_rn(add(mul(tt, tt), 1.0)));
+            const double nn = rcp(__dsqrt_rn(add(mul(tt, tt), 1.0)));
             // -sign_t * (n01 / |n01|) * |tt| is an exact sign change
             const bool neg = (sign_t > 0) == (n01 > 0);
             jrs = mul(neg ? -fabs(tt) : fabs(tt), nn);
@@ -148,7 +148,7 @@ __device__ __forceinline__ void svd_solve_nm(double (&W)[N][N], const double (&b
               V(i, q) = add(mul(-s, xv), mul(c, yv));
             }
           }
-          maxDiag = fmax(maxDiag, fmax(fabs(W[p][p]), fabs(W[q][q])));
+          maxDiag = max(maxDiag, max(mag_bits(W[p][p]), mag_bits(W[q][q])));
         }
       }
     }
@@ -221,7 +221,7 @@ __device__ __forceinline__ void svd_solve_nm(double (&W)[N][N], const double (&b
 #pragma unroll
       for (int r = 0; r < N; r++)
         s = add(s, mul(U(r, cc), b[r]));
-      tmp[cc] = mul(dvd(1.0, sv[cc]), s);
+      tmp[cc] = mul(rcp(sv[cc]), s);
     }
   }
 #pragma unroll
