@@ -332,6 +332,106 @@ def cpu_baseline(fedm, w, a, reps=1, n_libs=None, stride=8):
                       f"row ({preds} forecasts, {dt:.1f} s)"}
 
 
+# Other benchmark configurations at full size (--workload).  Each step runs
+# the configuration through the library's C ABI from host buffers; `value`
+# is forecasts per second of device time, `e2e` per second of wall time.
+# They are measurements of the parity-test configurations, not the headline.
+def config_steps(fedm, workloads, ctx, name):
+    """Returns (description, step function -> list of (timing dict, wall s))."""
+    if name == "simplex_explore":
+        w = workloads.simplex_config()
+        args = {E: fedm.normalise(w["t"], w["x"], E=E, theta=1.0) for E in w["Es"]}
+
+        def step():
+            out = []
+            for E in w["Es"]:
+                t0 = time.perf_counter()
+                ctx.run_task(args[E], w["library_rows"], w["prediction_rows"], E, E + 1)
+                out.append((ctx.timing(), time.perf_counter() - t0))
+            return out
+        return {"workload": "simplex_T500_lib250_pred250_E1-10_k=E+1", "T": 500}, step
+    if name == "smap_sweep":
+        # edm()'s explore split of 20 000 rows: the first 9 998 usable rows
+        # are the library, the other 9 998 the prediction set
+        w = workloads.smap_config()
+        a_ = fedm.normalise(w["t"], w["x"], E=w["E"], theta=w["thetas"], algorithm="smap", k=float("inf"))
+
+        def step():
+            t0 = time.perf_counter()
+            ctx.run_command(a_)
+            return [(ctx.timing(), time.perf_counter() - t0)]
+        return {"workload": "smap_kall_lib9998_pred9998_E5_theta0-8x81", "T": 20000}, step
+    if name == "panels":
+        w = workloads.panel_config()
+        kws = [dict(panel=w["panel"], E=[3, 4, 5, 6, 7, 8], dt=True, algorithm="simplex"),
+               dict(panel=w["panel"], E=[3, 4, 5, 6, 7, 8], dt=True, algorithm="smap", theta=[0.0, 1.0, 2.0, 4.0])]
+
+        def step():
+            out = []
+            for kw in kws:
+                t0 = time.perf_counter()
+                fedm.edm(w["t"], w["x"], ctx=ctx, **kw)
+                out.append((ctx.timing(), time.perf_counter() - t0))
+            return out
+        return {"workload": f"panels{512}_rows{len(w['t'])}_E3-8_dt_simplex+smap4theta_mixed_library",
+                "rows": len(w["t"])}, step
+    if name == "adjoint":
+        w = workloads.lorenz_config()
+        a_ = fedm.normalise(w["t"], w["x"], E=6, tau=5)
+        F = fedm.host_manifold(a_, 6)
+        first = 5 * 5
+        lib_rows = np.arange(first, first + 50000)
+        pred_rows = np.arange(first + 50000, first + 70000)
+        lib, lib_t = F[lib_rows], w["x"][lib_rows + 1]
+        pred, pred_t = F[pred_rows], w["x"][pred_rows + 1]
+
+        def step():
+            t0 = time.perf_counter()
+            ctx.smap_grad(lib, lib_t, pred, pred_t, 1.0, np.ones(6))
+            tm = ctx.timing()
+            tm = dict(tm, predictions=len(pred_rows))
+            return [(tm, time.perf_counter() - t0)]
+        return {"workload": "lorenz_smap_grad_kall_lib50000_pred20000_E6_tau5", "T": 100000}, step
+    raise ValueError(name)
+
+
+def run_config(a):
+    fedm, workloads = load_pkg()
+    world, rank, local = dist_setup()
+    ctx = fedm.Context(local, precision=fedm.PRECISION_MIXED)
+    cfg, step = config_steps(fedm, workloads, ctx, a.workload)
+    for _ in range(max(3, a.warmup)):
+        step()
+        flush_l2(local)
+    barrier(world)
+    dev = wall = 0.0
+    preds = launches = 0
+    with Clocks(local) as clk:
+        for _ in range(a.steps):
+            for tm, ws in step():
+                dev += tm["device_ms"] / 1e3
+                wall += ws
+                preds += tm["predictions"]
+                launches += tm["kernel_launches"]
+            flush_l2(local)
+    dev = allreduce_max(world, dev)
+    wall = allreduce_max(world, wall)
+    if rank != 0:
+        return
+    cfg["l2"] = "flushed between steps (512 MiB write)"
+    cfg["parallelism"] = f"replicas x{world}"
+    out = {
+        "metric": f"{a.workload} predictions/s (full-size configuration, mixed precision path)", "value":
+        preds * world / dev, "unit": "predictions/s", "n_gpus": world, "steps": a.steps, "warmup": max(3, a.warmup),
+        "ms_per_step": dev / a.steps * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "fp32+fp64", "data": "synthetic (seeded generators)", "config": cfg,
+        "e2e": {"value": preds * world / wall, "unit": "predictions/s", "wall_ms_per_step": wall / a.steps * 1e3},
+        "gpu_launches": launches, "predictions_per_step": preds // a.steps, "roofline": None, "cpu_baseline": None,
+        "clocks": clk.summary(),
+    }
+    print(json.dumps(out), flush=True)
+
+
 def run_reference(a):
     world, rank, local = dist_setup()
     if rank != 0:
@@ -376,9 +476,15 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fp64", dest="no_fp64", action="store_true",
                     help="skip the plain FP64 sample (profiling runs)")
+    ap.add_argument("--workload", default="ccm",
+                    choices=["ccm", "simplex_explore", "smap_sweep", "panels", "adjoint"],
+                    help="ccm (default): the headline CCM benchmark; the others time the other benchmark "
+                         "configurations at full size")
     a = ap.parse_args()
     if a.impl == "reference":
         run_reference(a)
+    elif a.workload != "ccm":
+        run_config(a)
     else:
         run_ours(a)
 

@@ -289,8 +289,7 @@ struct GroupJob
 constexpr int KCAP_MAX = 16384;
 constexpr int MIX_KMAX = 14;        // neighbours the mixed kernel serves (slots C = 16)
 constexpr int MIX_POINTS = 512;     // prediction points per mixed work item
-constexpr size_t LAZY_BATCHES = 8;  // task batches of a group whose CCM lists are produced lazily
-constexpr size_t LAZY_MIN_BATCH = 64;
+constexpr size_t LAZY_FIRST_BATCH = 64;  // first task batch of a group with lazily produced CCM lists
 constexpr long long FB_CAP = 1 << 24;
 
 // Whether the mixed kernel's preconditions hold for a group (see
@@ -948,12 +947,13 @@ CommandResult run_command(Context& ctx, const fedm_args& a)
         ids.push_back(i);
     if (producer)
       job.lib_superset = &plan.lazy.urows;
-    // With lazy lists the group runs in about LAZY_BATCHES batches of tasks
-    // in plan order (replicates outermost, so every batch spans all library
-    // sizes); each waits only for its own lists.
-    const size_t per = producer ? std::max<size_t>(LAZY_MIN_BATCH, (ids.size() + LAZY_BATCHES - 1) / LAZY_BATCHES)
-                                : ids.size();
-    for (size_t b0 = 0; b0 < ids.size(); b0 += per) {
+    // With lazy lists the group runs in task batches in plan order
+    // (replicates outermost, so every batch spans all library sizes), each
+    // waiting only for its own lists.  Batches double from LAZY_FIRST_BATCH
+    // tasks: the GPU starts after a few splits, and the splitter, far faster
+    // per task than the GPU, stays ahead.
+    size_t per = producer ? LAZY_FIRST_BATCH : ids.size();
+    for (size_t b0 = 0; b0 < ids.size(); b0 += per, per *= 2) {
       job.task_ids.clear();
       job.lib_lists.clear();
       job.pred_lists.clear();
@@ -1239,6 +1239,8 @@ int run_task(Context& ctx, const fedm_args& a, fedm_task_io& io)
   io.e_actual = Ea;
   io.total_nn = to.nn_offsets.empty() ? 0 : to.nn_offsets.back();
   ctx.timing.host_ms = now_ms() - t0;
+  ctx.timing.predictions = (long long)Pl.size() * nth;
+  ctx.timing.distance_pairs = (long long)Pl.size() * (long long)L.size();
   if (sizes_only)
     return RC_SUCCESS;
   const int np = io.n_pred;

@@ -432,14 +432,16 @@ __global__ void all_dist_kernel(GroupParams g, ChunkBuffers c, long long max_nli
   }
 }
 
+// One thread per (point, theta), theta fastest: the threads of a warp read
+// the same point's distance row and library rows (broadcast loads).
 __global__ void all_forecast_kernel(GroupParams g, ChunkBuffers c, long long max_nlib, long long slab)
 {
   const long long chunk = c.p_end - c.p_begin;
   const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (idx >= chunk * g.n_thetas)
     return;
-  const int t = (int)(idx / chunk);
-  const long long q = idx - (long long)t * chunk;
+  const long long q = idx / g.n_thetas;
+  const int t = (int)(idx - q * g.n_thetas);
   const long long p = point_of(c, q);
   const DevTask T = g.tasks[find_task(g, p)];
   if (!T.all_mode)
@@ -509,6 +511,76 @@ __global__ void all_forecast_kernel(GroupParams g, ChunkBuffers c, long long max
     for (int b = 0; b < a; b++)
       W[a * n + b] = W[b * n + a];
   svd_solve(W, U, V, sv, tmp, bv, xs, n);
+  const int prow = g.pred_rows[T.pred_off + (int)(p - T.point_base)];
+  smap_finish(g, T, p, prow, t, xs, n);
+}
+
+// S-map over every valid neighbour for E_a <= 8 (src/edm.cpp:737-814): the
+// all_forecast_kernel computation with the normal equations accumulated in
+// registers (the same operations in the same order, so the same bits).
+template<int EA>
+__global__ void __launch_bounds__(128) all_smap_kernel(GroupParams g, ChunkBuffers c, long long max_nlib)
+{
+  constexpr int n = EA + 1;
+  const long long chunk = c.p_end - c.p_begin;
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= chunk * g.n_thetas)
+    return;
+  const long long q = idx / g.n_thetas;
+  const int t = (int)(idx - q * g.n_thetas);
+  const long long p = point_of(c, q);
+  const DevTask T = g.tasks[find_task(g, p)];
+  if (!T.all_mode)
+    return;
+  const int st = c.status[q];
+  if (st != PT_OK) {
+    early_rc(g, T.task, st, t);
+    return;
+  }
+  const double* dq = c.scratch + q * max_nlib;
+  const double theta = g.thetas[t];
+  const int ke = c.nn_count[q];
+  double mean = 0;
+  for (int i = 0; i < T.n_lib; i++)
+    if (dq[i] >= 0)
+      mean += dq[i];
+  mean /= (double)ke;
+  double W[n][n], bv[n];
+#pragma unroll
+  for (int a = 0; a < n; a++) {
+    bv[a] = 0;
+#pragma unroll
+    for (int b = 0; b < n; b++)
+      W[a][b] = 0;
+  }
+  for (int i = 0; i < T.n_lib; i++) {
+    const double d = dq[i];
+    if (d < 0)
+      continue;
+    const double w = exp_rn(-theta * (d / mean));
+    const int row = g.lib_rows[T.lib_off + i];
+    const double* fr = g.F + (size_t)row * EA;
+    const double yl = w * g.lib_target[row];
+    double xr[n];
+    xr[0] = w;
+#pragma unroll
+    for (int j = 1; j < n; j++)
+      xr[j] = w * fr[j - 1];
+#pragma unroll
+    for (int a = 0; a < n; a++) {
+#pragma unroll
+      for (int b = a; b < n; b++)
+        W[a][b] += xr[a] * xr[b];
+      bv[a] += xr[a] * yl;
+    }
+  }
+  double Wl[n * n], U[n * n], V[n * n], sv[n], tmp[n], xs[n];
+#pragma unroll
+  for (int a = 0; a < n; a++)
+#pragma unroll
+    for (int b = 0; b < n; b++)
+      Wl[a * n + b] = b >= a ? W[a][b] : W[b][a];
+  svd_solve(Wl, U, V, sv, tmp, bv, xs, n);
   const int prow = g.pred_rows[T.pred_off + (int)(p - T.point_base)];
   smap_finish(g, T, p, prow, t, xs, n);
 }
@@ -668,8 +740,23 @@ void launch_all_mode(const GroupParams& g, const ChunkBuffers& c, int num_sms, l
     blocks = 1;
   all_dist_kernel<<<(int)blocks, 32 * w, (size_t)w * per_warp, s>>>(g, c, max_nlib, per_warp);
   const long long total = chunk * g.n_thetas;
-  if (total > 0)
-    all_forecast_kernel<<<(int)((total + 127) / 128), 128, 0, s>>>(g, c, max_nlib, all_mode_slab(g.Ea));
+  if (total <= 0)
+    return;
+  const int fb = (int)((total + 127) / 128);
+  if (g.algorithm == 1 && g.Ea <= 8) {
+    switch (g.Ea) {
+      case 1: all_smap_kernel<1><<<fb, 128, 0, s>>>(g, c, max_nlib); return;
+      case 2: all_smap_kernel<2><<<fb, 128, 0, s>>>(g, c, max_nlib); return;
+      case 3: all_smap_kernel<3><<<fb, 128, 0, s>>>(g, c, max_nlib); return;
+      case 4: all_smap_kernel<4><<<fb, 128, 0, s>>>(g, c, max_nlib); return;
+      case 5: all_smap_kernel<5><<<fb, 128, 0, s>>>(g, c, max_nlib); return;
+      case 6: all_smap_kernel<6><<<fb, 128, 0, s>>>(g, c, max_nlib); return;
+      case 7: all_smap_kernel<7><<<fb, 128, 0, s>>>(g, c, max_nlib); return;
+      case 8: all_smap_kernel<8><<<fb, 128, 0, s>>>(g, c, max_nlib); return;
+      default: break;
+    }
+  }
+  all_forecast_kernel<<<fb, 128, 0, s>>>(g, c, max_nlib, all_mode_slab(g.Ea));
 }
 
 void launch_stats(const GroupParams& g, const DevTask*, int n_tasks, double* rho, double* mae, cudaStream_t s)
