@@ -24,6 +24,7 @@ CU_FLAGS = {
     "kernels_exact.cu": ["--fmad=false"],
     "kernels_util.cu": [],
     "kernels_mixed.cu": [],
+    "kernels_wide.cu": [],
     "static_entry.cu": [],
     "kernels_adjoint.cu": [],
 }

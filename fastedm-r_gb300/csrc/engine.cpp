@@ -51,7 +51,7 @@ Context::Context(int dev) : device(dev)
   ck(cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, dev), "cudaDeviceGetAttribute");
   if (const char* v = std::getenv("FEDM_SMAP_SOLVER_WARPS")) {
     const int w = std::atoi(v);
-    if (w == 0 || w == 4 || w == 8)
+    if (w == 0 || w == 3 || w == 4 || w == 8)
       smap_solver_warps = w;
   }
 }
@@ -289,6 +289,9 @@ struct GroupJob
 constexpr int KCAP_MAX = 16384;
 constexpr int MIX_KMAX = 14;        // neighbours the mixed kernel serves (slots C = 16)
 constexpr int MIX_POINTS = 512;     // prediction points per mixed work item
+constexpr int WIDE_EA = 16;         // widest embedding of the mixed path (knn_wide_kernel above 8)
+constexpr int WIDE_KMAX = 30;       // neighbours the wide kernel serves (slots C = 32)
+constexpr int WIDE_POINTS = 256;    // prediction points per wide work item
 constexpr size_t LAZY_FIRST_BATCH = 64;  // first task batch of a group with lazily produced CCM lists
 constexpr long long FB_CAP = 1 << 24;
 
@@ -300,7 +303,7 @@ bool mixed_eligible(const Context& ctx, const Options& o, const GroupJob& job, s
                     double& R)
 {
   if (ctx.precision != FEDM_PRECISION_MIXED || o.distance != 1 || o.has_missing || o.low_memory || o.past_only ||
-      !o.force_compute || job.Ea > 8 || job.Ea < 1 || !job.hF || !job.hFp)
+      !o.force_compute || job.Ea > WIDE_EA || job.Ea < 1 || !job.hF || !job.hFp)
     return false;
   if (o.panel_mode && (o.idw != 0 || o.has_id_weights))
     return false;
@@ -398,7 +401,7 @@ void run_group(Context& ctx, const Options& o, const std::vector<Task>& tasks, c
     }
     if (!d.all_mode && d.k > KCAP_MAX)
       throw Error{ RC_NOT_IMPLEMENTED, "k above the supported maximum of 16384 neighbours" };
-    d.mixed = (mixed_group && !d.all_mode && d.k >= 1 && d.k <= MIX_KMAX) ? 1 : 0;
+    d.mixed = (mixed_group && !d.all_mode && d.k >= 1 && d.k <= (Ea > 8 ? WIDE_KMAX : MIX_KMAX)) ? 1 : 0;
     if (d.all_mode) {
       any_all = true;
       max_nlib_all = std::max<long long>(max_nlib_all, d.n_lib);
@@ -570,7 +573,9 @@ void run_group(Context& ctx, const Options& o, const std::vector<Task>& tasks, c
 
   // 1. mixed-precision kernel for the tasks it serves
   if (any_mixed) {
-    const int S = Ea <= 4 ? 4 : 8;
+    const bool wide = Ea > 8;
+    const int S = Ea <= 4 ? 4 : (Ea <= 8 ? 8 : 16);
+    const int item_points = wide ? WIDE_POINTS : MIX_POINTS;
     const long long nrows = (long long)rows.n_rows;
     double* d_center = (double*)ctx.buf("center", Ea * 8);
     ctx.upload(d_center, center.data(), Ea * 8);
@@ -588,7 +593,7 @@ void run_group(Context& ctx, const Options& o, const std::vector<Task>& tasks, c
     std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return dt[a].n_lib > dt[b].n_lib; });
     std::vector<int2> items;
     for (int j : order)
-      for (int b = 0; b < dt[j].n_pred; b += MIX_POINTS)
+      for (int b = 0; b < dt[j].n_pred; b += item_points)
         items.push_back(make_int2(j, b));
     MixedRun m{};
     m.F32 = F32;
@@ -607,14 +612,14 @@ void run_group(Context& ctx, const Options& o, const std::vector<Task>& tasks, c
     m.fb_list = (long long*)ctx.buf("fb_list", (size_t)m.fb_cap * 8);
     m.gamma = (Ea + 2) * std::ldexp(1.0, -23);
     m.err_abs = std::ldexp(R, -21) + 1e-21;
-    const int C = kmix <= 6 ? 8 : 16;
+    const int C = wide ? 32 : (kmix <= 6 ? 8 : 16);
     if (job.detail) {
       m.nn_idx = (int*)ctx.buf("mix_nn_idx", (size_t)std::max<long long>(P, 1) * C * 4);
       m.nn_dist = (double*)ctx.buf("mix_nn_dist", (size_t)std::max<long long>(P, 1) * C * 8);
     }
     ctx.timing.kernel_launches += (job.dFp != job.dF ? 2 : 1) + 1;  // centring, counter fill
     m.kslots = C;
-    if (o.algorithm == 1 && ctx.smap_deferred) {
+    if (o.algorithm == 1 && ctx.smap_deferred && !wide) {
       // S-map alternative: scan + re-rank in batches of items; each batch's
       // neighbour lists go to a separate register-resident SVD kernel
       const long long batch_points = 8LL << 20;
@@ -644,7 +649,10 @@ void run_group(Context& ctx, const Options& o, const std::vector<Task>& tasks, c
     } else {
       m.item_begin = 0;
       m.item_end = m.n_items;
-      timed([&] { launch_knn_mixed(g, m, C, ctx.num_sms, s); });
+      if (wide)
+        timed([&] { launch_knn_wide(g, m, ctx.num_sms, s); });
+      else
+        timed([&] { launch_knn_mixed(g, m, C, ctx.num_sms, s); });
     }
     int nfb = 0, herr = 0;
     unsigned long long nops = 0;

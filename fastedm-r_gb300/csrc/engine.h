@@ -30,11 +30,12 @@ public:
   // kernel over batched neighbour lists (true)
   bool smap_deferred = false;
   // S-map in the mixed path, in-kernel form: 0 = every warp scans then
-  // solves (knn_mixed_kernel, two CTAs per SM; the fastest on GB300 for
-  // E_a = 4); 4 or 8 = warp-specialised kernel with that many FP64 solver
-  // warps beside 8 scan warps.  FEDM_SMAP_SOLVER_WARPS overrides it when the
-  // context is created.
-  int smap_solver_warps = 0;
+  // solves (knn_mixed_kernel, two CTAs per SM); 3 = the same kernel at three
+  // CTAs per SM (85 registers; used for k <= 6, else the two-CTA form; the
+  // fastest on GB300 for the CCM workload); 4 or 8 = warp-specialised kernel
+  // with that many FP64 solver warps beside 8 scan warps.
+  // FEDM_SMAP_SOLVER_WARPS overrides it when the context is created.
+  int smap_solver_warps = 3;
   std::string last_error;
   fedm_timing timing{};
 

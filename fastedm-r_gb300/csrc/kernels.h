@@ -129,7 +129,8 @@ struct MixedRun
   int kslots;
   unsigned long long* fp64_ops;  // optional: FP64 operations of the re-rank and forecast stage
   int* error;          // set when a bounded wait of the warp-specialised kernel ran out
-  int solver_warps;    // S-map: 0 = knn_mixed_kernel, 4 / 8 = knn_smap_ws_kernel
+  int solver_warps;    // S-map: 0 = knn_mixed_kernel, 3 = the same at 3 CTAs per SM (C = 8),
+                       // 4 / 8 = knn_smap_ws_kernel
   int item_begin;      // first item of this launch (the queue head starts here)
   int item_end;        // one past the last item of this launch
   // S-map: when set, the neighbour lists are appended here and solved by
@@ -150,6 +151,11 @@ struct MixedRun
 void launch_smap_lists(const GroupParams& g, const MixedRun& m, int num_sms, cudaStream_t s);
 
 void launch_knn_mixed(const GroupParams& g, const MixedRun& m, int C, int num_sms, cudaStream_t s);
+
+// The mixed path for E_a = 9..16 and up to 30 neighbours (knn_wide_kernel:
+// one point per thread, 32 candidate slots, work items of 256 points, float
+// manifold row stride 16).
+void launch_knn_wide(const GroupParams& g, const MixedRun& m, int num_sms, cudaStream_t s);
 
 // Differentiable S-map over every library neighbour (kernels_adjoint.cu).
 struct AdjointParams

@@ -29,61 +29,10 @@ namespace {
 template<int EA>
 __device__ __noinline__ void smap_point(const GroupParams& g, long long p, int prow, bool save, int keff,
                                         const int* rows, const double* cd);
-template<int EA>
-__device__ __noinline__ int smap_point_local(const GroupParams& g, long long p, int prow, bool save, int keff,
-                                             const int* rows, const double* cd);
-template<int EA>
-__device__ __noinline__ int smap_point_sm(const GroupParams& g, long long p, int prow, bool save, int keff,
-                                          const int* rows, const double* cd, double* uv, int uv_stride);
 
-// Returns the number of FP64 add/sub/mul/div/sqrt operations it performed.
-// uv, when given, is this thread's shared-memory slice for the S-map solver's
-// rotation accumulators (2 (EA+1)^2 doubles, interleaved with stride
-// uv_stride).
-template<int EA, int C, int ALG, bool UVS = false>
-__device__ __noinline__ int finalize_point(const GroupParams& g, const MixedRun& m, const DevTask& T, long long p,
-                                           int prow, const Cand<C>& cand, double* uv = nullptr, int uv_stride = 0)
-{
-  int keff = 0, ops = 0;
-  int rows[C + ZCAP];
-  double cd[C + ZCAP];
-  if (!prepare_point<EA, C>(g, m, T, p, prow, cand, keff, rows, cd, ops))
-    return ops;
-  if constexpr (ALG == 0) {
-    // simplex (src/edm.cpp:707-735)
-    double minD = cd[0];
-    for (int j = 1; j < keff; j++)
-      minD = cd[j] < minD ? cd[j] : minD;
-    double rel[C + ZCAP], tg[C + ZCAP];
-    for (int j = 0; j < keff; j++) {
-      rel[j] = dvd(cd[j], minD);
-      tg[j] = g.lib_target[rows[j]];
-    }
-    for (int t = 0; t < g.n_thetas; t++) {
-      const double theta = g.thetas[t];
-      double w[C + ZCAP];
-      double sumw = 0.0;
-      for (int j = 0; j < keff; j++) {
-        w[j] = exp_rn(mul(-theta, rel[j]));
-        sumw = add(sumw, w[j]);
-      }
-      double r = 0.0;
-      for (int j = 0; j < keff; j++)
-        r = add(r, mul(tg[j], dvd(w[j], sumw)));
-      g.pred[(size_t)t * g.total_points + p] = r;
-    }
-    return ops + keff + g.n_thetas * keff * (EXP_OPS + 5);
-  }
-  else {
-    if constexpr (UVS)
-      return ops + smap_point_sm<EA>(g, p, prow, T.save_coeffs != 0, keff, rows, cd, uv, uv_stride);
-    else
-      return ops + smap_point_local<EA>(g, p, prow, T.save_coeffs != 0, keff, rows, cd);
-  }
-}
-
-template<int EA, int C, int ALG>
-__global__ void __launch_bounds__(TPB, 2) knn_mixed_kernel(GroupParams g, MixedRun m)
+// OCC: CTAs per SM the register budget is set for (2: 128 registers, 3: 85).
+template<int EA, int C, int ALG, int OCC = 2>
+__global__ void __launch_bounds__(TPB, OCC) knn_mixed_kernel(GroupParams g, MixedRun m)
 {
   // library rows staged as interleaved pairs: tile[pair][dim] = (row 2i, row 2i+1)
   __shared__ __align__(16) float2 tile[(TILE / 2) * EA];
@@ -300,66 +249,6 @@ __device__ __noinline__ void smap_point(const GroupParams& g, long long p, int p
   }
 }
 
-// The same forecast with the solver's matrices in per-thread local memory;
-// used inside the scan kernel, whose register budget (two 256-thread CTAs
-// per SM) leaves no room for them.  Identical operations and bits.
-template<int EA>
-__device__ __noinline__ int smap_point_local(const GroupParams& g, long long p, int prow, bool save, int keff,
-                                             const int* rows, const double* cd)
-{
-  constexpr int n = EA + 1;
-  // mean; per theta: weights and the normal equations per neighbour, the
-  // forecast (the SVD counts its own)
-  int ops = keff + 1 + g.n_thetas * (keff * (EXP_OPS + 2 + n + n * (n + 1) + 2 * n) + 2 * EA);
-  double y[EA];
-#pragma unroll
-  for (int j = 0; j < EA; j++)
-    y[j] = g.Fp[(size_t)prow * EA + j];
-  double mean = 0;
-  for (int j = 0; j < keff; j++)
-    mean = add(mean, cd[j]);
-  mean = dvd(mean, (double)keff);
-  for (int t = 0; t < g.n_thetas; t++) {
-    const double theta = g.thetas[t];
-    double W[n * n], bv[n], xs[n], U[n * n], V[n * n], sv[n], tmp[n];
-    for (int e = 0; e < n * n; e++)
-      W[e] = 0;
-    for (int a = 0; a < n; a++)
-      bv[a] = 0;
-    for (int i = 0; i < keff; i++) {
-      const double w = exp_rn(mul(-theta, dvd(cd[i], mean)));
-      const int row = rows[i];
-      double xr[n];
-      xr[0] = w;
-#pragma unroll
-      for (int j = 1; j < n; j++)
-        xr[j] = mul(w, g.F[(size_t)row * EA + j - 1]);
-      const double yl = mul(w, g.lib_target[row]);
-#pragma unroll
-      for (int a = 0; a < n; a++) {
-#pragma unroll
-        for (int b = a; b < n; b++)
-          W[a * n + b] = add(W[a * n + b], mul(xr[a], xr[b]));
-        bv[a] = add(bv[a], mul(xr[a], yl));
-      }
-    }
-    for (int a = 0; a < n; a++)
-      for (int b = 0; b < a; b++)
-        W[a * n + b] = W[b * n + a];
-    svd_solve(W, U, V, sv, tmp, bv, xs, n, ops);
-    double r = xs[0];
-#pragma unroll
-    for (int j = 0; j < EA; j++)
-      r = add(r, mul(y[j], xs[j + 1]));
-    if (g.coeffs && save && t == g.n_thetas - 1) {
-      for (int j = 0; j < n; j++)
-        g.coeffs[(size_t)p * n + j] = fabs(xs[j]) < 1.0e-11 ? MISS : xs[j];
-    }
-    g.pred[(size_t)t * g.total_points + p] = r;
-  }
-  return ops;
-}
-
 // The same forecast with the normal matrix in registers and the solver's
 // rotation accumulators in the caller's shared-memory slice (the
 // warp-specialised kernel's solver threads).  Identical operations and bits.
@@ -496,11 +385,11 @@ __global__ void __launch_bounds__(128) smap_lists_kernel(GroupParams g, MixedRun
   }
 }
 
-template<int EA, int C, int ALG>
+template<int EA, int C, int ALG, int OCC = 2>
 void launch_one(const GroupParams& g, const MixedRun& m, int num_sms, cudaStream_t s)
 {
   int per_sm = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, knn_mixed_kernel<EA, C, ALG>, TPB, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, knn_mixed_kernel<EA, C, ALG, OCC>, TPB, 0);
   if (per_sm < 1)
     per_sm = 1;
   long long blocks = (long long)num_sms * per_sm;
@@ -508,7 +397,7 @@ void launch_one(const GroupParams& g, const MixedRun& m, int num_sms, cudaStream
     blocks = m.item_end - m.item_begin;
   if (blocks < 1)
     blocks = 1;
-  knn_mixed_kernel<EA, C, ALG><<<(int)blocks, TPB, 0, s>>>(g, m);
+  knn_mixed_kernel<EA, C, ALG, OCC><<<(int)blocks, TPB, 0, s>>>(g, m);
 }
 
 template<int EA, int C, int SW>
@@ -536,6 +425,9 @@ void launch_ea(const GroupParams& g, const MixedRun& m, int num_sms, cudaStream_
       return launch_ws<EA, C, 4>(g, m, num_sms, s);
     if (m.solver_warps == 8)
       return launch_ws<EA, C, 8>(g, m, num_sms, s);
+    if constexpr (C == 8)
+      if (m.solver_warps == 3)
+        return launch_one<EA, C, ALG, 3>(g, m, num_sms, s);
   }
   launch_one<EA, C, ALG>(g, m, num_sms, s);
 }

@@ -422,6 +422,120 @@ __device__ __forceinline__ bool group_and(bool v)
 
 constexpr size_t SMEM_LIMIT = 227 * 1024;
 
+
+template<int EA>
+__device__ __noinline__ int smap_point_local(const GroupParams& g, long long p, int prow, bool save, int keff,
+                                             const int* rows, const double* cd);
+template<int EA>
+__device__ __noinline__ int smap_point_sm(const GroupParams& g, long long p, int prow, bool save, int keff,
+                                          const int* rows, const double* cd, double* uv, int uv_stride);
+
+// Returns the number of FP64 add/sub/mul/div/sqrt operations it performed.
+// uv, when given, is this thread's shared-memory slice for the S-map solver's
+// rotation accumulators (2 (EA+1)^2 doubles, interleaved with stride
+// uv_stride).
+template<int EA, int C, int ALG, bool UVS = false>
+__device__ __noinline__ int finalize_point(const GroupParams& g, const MixedRun& m, const DevTask& T, long long p,
+                                           int prow, const Cand<C>& cand, double* uv = nullptr, int uv_stride = 0)
+{
+  int keff = 0, ops = 0;
+  int rows[C + ZCAP];
+  double cd[C + ZCAP];
+  if (!prepare_point<EA, C>(g, m, T, p, prow, cand, keff, rows, cd, ops))
+    return ops;
+  if constexpr (ALG == 0) {
+    // simplex (src/edm.cpp:707-735)
+    double minD = cd[0];
+    for (int j = 1; j < keff; j++)
+      minD = cd[j] < minD ? cd[j] : minD;
+    double rel[C + ZCAP], tg[C + ZCAP];
+    for (int j = 0; j < keff; j++) {
+      rel[j] = dvd(cd[j], minD);
+      tg[j] = g.lib_target[rows[j]];
+    }
+    for (int t = 0; t < g.n_thetas; t++) {
+      const double theta = g.thetas[t];
+      double w[C + ZCAP];
+      double sumw = 0.0;
+      for (int j = 0; j < keff; j++) {
+        w[j] = exp_rn(mul(-theta, rel[j]));
+        sumw = add(sumw, w[j]);
+      }
+      double r = 0.0;
+      for (int j = 0; j < keff; j++)
+        r = add(r, mul(tg[j], dvd(w[j], sumw)));
+      g.pred[(size_t)t * g.total_points + p] = r;
+    }
+    return ops + keff + g.n_thetas * keff * (EXP_OPS + 5);
+  }
+  else {
+    if constexpr (UVS)
+      return ops + smap_point_sm<EA>(g, p, prow, T.save_coeffs != 0, keff, rows, cd, uv, uv_stride);
+    else
+      return ops + smap_point_local<EA>(g, p, prow, T.save_coeffs != 0, keff, rows, cd);
+  }
+}
+
+// The same forecast with the solver's matrices in per-thread local memory;
+// used inside the scan kernel, whose register budget (two 256-thread CTAs
+// per SM) leaves no room for them.  Identical operations and bits.
+template<int EA>
+__device__ __noinline__ int smap_point_local(const GroupParams& g, long long p, int prow, bool save, int keff,
+                                             const int* rows, const double* cd)
+{
+  constexpr int n = EA + 1;
+  // mean; per theta: weights and the normal equations per neighbour, the
+  // forecast (the SVD counts its own)
+  int ops = keff + 1 + g.n_thetas * (keff * (EXP_OPS + 2 + n + n * (n + 1) + 2 * n) + 2 * EA);
+  double y[EA];
+#pragma unroll
+  for (int j = 0; j < EA; j++)
+    y[j] = g.Fp[(size_t)prow * EA + j];
+  double mean = 0;
+  for (int j = 0; j < keff; j++)
+    mean = add(mean, cd[j]);
+  mean = dvd(mean, (double)keff);
+  for (int t = 0; t < g.n_thetas; t++) {
+    const double theta = g.thetas[t];
+    double W[n * n], bv[n], xs[n], U[n * n], V[n * n], sv[n], tmp[n];
+    for (int e = 0; e < n * n; e++)
+      W[e] = 0;
+    for (int a = 0; a < n; a++)
+      bv[a] = 0;
+    for (int i = 0; i < keff; i++) {
+      const double w = exp_rn(mul(-theta, dvd(cd[i], mean)));
+      const int row = rows[i];
+      double xr[n];
+      xr[0] = w;
+#pragma unroll
+      for (int j = 1; j < n; j++)
+        xr[j] = mul(w, g.F[(size_t)row * EA + j - 1]);
+      const double yl = mul(w, g.lib_target[row]);
+#pragma unroll
+      for (int a = 0; a < n; a++) {
+#pragma unroll
+        for (int b = a; b < n; b++)
+          W[a * n + b] = add(W[a * n + b], mul(xr[a], xr[b]));
+        bv[a] = add(bv[a], mul(xr[a], yl));
+      }
+    }
+    for (int a = 0; a < n; a++)
+      for (int b = 0; b < a; b++)
+        W[a * n + b] = W[b * n + a];
+    svd_solve(W, U, V, sv, tmp, bv, xs, n, ops);
+    double r = xs[0];
+#pragma unroll
+    for (int j = 0; j < EA; j++)
+      r = add(r, mul(y[j], xs[j + 1]));
+    if (g.coeffs && save && t == g.n_thetas - 1) {
+      for (int j = 0; j < n; j++)
+        g.coeffs[(size_t)p * n + j] = fabs(xs[j]) < 1.0e-11 ? MISS : xs[j];
+    }
+    g.pred[(size_t)t * g.total_points + p] = r;
+  }
+  return ops;
+}
+
 } // namespace
 
 } // namespace fedm

@@ -128,7 +128,7 @@ def test_mixed_fp64_operation_count(ctx):
         assert 2000 <= per["smap"] <= 20000, per
 
 
-@pytest.mark.parametrize("solver_warps", ["0", "4", "8"])
+@pytest.mark.parametrize("solver_warps", ["0", "3", "4", "8"])
 def test_smap_kernel_forms_agree(solver_warps, monkeypatch):
     """The mixed S-map runs in one of three kernel forms: every warp scans
     then solves (0), or 8 scan warps hand candidate lists to 4 or 8 FP64
@@ -149,3 +149,27 @@ def test_smap_kernel_forms_agree(solver_warps, monkeypatch):
     assert np.array_equal(g["stats"]["rho"], f["stats"]["rho"], equal_nan=True)
     assert np.array_equal(g["predictions"], f["predictions"], equal_nan=True)
     assert np.array_equal(g["coeffs"], f["coeffs"], equal_nan=True)
+
+
+@pytest.mark.parametrize("E", [5, 8])
+@pytest.mark.parametrize("algorithm", ["simplex", "smap"])
+def test_wide_embedding_task_bit_exact(ctx, E, algorithm):
+    """Panels with dt double the embedding (E_a = 2E = 10, 16): the mixed
+    path's wide kernel (one point per thread, 32 candidate slots) must give
+    the oracle's neighbour lists, distances and forecasts bit for bit."""
+    w = workloads.panel_config(n_panels=24, lo=80, hi=400)
+    n = len(w["t"])
+    rng = np.random.default_rng(E)
+    lib = rng.uniform(size=n) < 0.5
+    pred = ~lib
+    kw = dict(panel=w["panel"], E=E, dt=True, algorithm=algorithm, theta=[0.5, 2.0])
+    a = fedm.normalise(w["t"], w["x"], **kw)
+    Ea = fedm.host_manifold(a, E).shape[1]
+    assert Ea == 2 * E
+    k = Ea + 1 + (algorithm == "smap")
+    g = ctx.run_task(a, lib, pred, E, k)
+    o = edm_oracle.oracle_task(edm_oracle.normalise(w["t"], w["x"], **kw), lib, pred, E, k)
+    assert g["n_pred"] > 1000
+    assert np.array_equal(g["nn_idx"], o["nn_idx"])
+    assert np.array_equal(g["nn_dist"].view(np.int64), o["nn_dist"].view(np.int64))
+    assert np.array_equal(g["predictions"], o["predictions"], equal_nan=True)
