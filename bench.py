@@ -33,12 +33,12 @@ import numpy as np
 ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT / "tests"))
 METRIC = "CCM S-map predictions/s: batched FP32+FP64-fix vs plain FP64 GPU @|Δρ|≤1e-6"
-# DRAM bytes per S-map prediction point of knn_mixed_kernel<4,8,1>: ncu
-# dram__bytes_read.sum + dram__bytes_write.sum of one launch over the
-# 2-replicate x 20-library workload (42.5 MB + 2122.2 MB) divided by its
-# 1 999 880 points.  The traffic is the solver's per-thread scratch leaving
-# L1, so it scales with the points of a launch.
-SMAP_DRAM_BYTES_PER_POINT = 1082.5
+# DRAM bytes per S-map prediction point of the S-map kernel
+# (knn_mixed_kernel<4,8,1,3>): ncu dram__bytes_read.sum + dram__bytes_write.sum
+# of one launch over the 2-replicate x 20-library workload (457.4 MB +
+# 5243.6 MB) divided by its 1 999 880 points.  The traffic is the solver's
+# per-thread scratch and spills leaving L1, so it scales with the points.
+SMAP_DRAM_BYTES_PER_POINT = 2850.7
 
 
 def hbm_peak():

@@ -962,6 +962,9 @@ CommandResult run_command(Context& ctx, const fedm_args& a)
     // per task than the GPU, stays ahead.
     size_t per = producer ? LAZY_FIRST_BATCH : ids.size();
     for (size_t b0 = 0; b0 < ids.size(); b0 += per, per *= 2) {
+      // src/edm.cpp:572-591: the caller may stop the run between batches
+      if (ctx.keep_going && !ctx.keep_going())
+        throw Error{ RC_BREAK_HIT, "cancelled" };
       job.task_ids.clear();
       job.lib_lists.clear();
       job.pred_lists.clear();

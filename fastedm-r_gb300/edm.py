@@ -94,6 +94,7 @@ def load():
         lib.fedm_last_error.argtypes = [C.c_void_p]
         lib.fedm_last_error.restype = C.c_char_p
         lib.fedm_set_precision.argtypes = [C.c_void_p, C.c_int]
+        lib.fedm_set_keep_going.argtypes = [C.c_void_p, C.CFUNCTYPE(C.c_int)]
         lib.fedm_run_command.argtypes = [C.c_void_p, C.POINTER(Args), C.POINTER(C.POINTER(Result))]
         lib.fedm_free_result.argtypes = [C.POINTER(Result)]
         lib.fedm_run_task.argtypes = [C.c_void_p, C.POINTER(Args), C.POINTER(TaskIO)]
@@ -122,6 +123,14 @@ class Context:
             raise RuntimeError(f"fedm_create failed (rc={rc}): no usable CUDA device {device}")
         self.h = h
         self.set_precision(precision)
+
+    def set_keep_going(self, fn):
+        """fn() -> bool is polled between GPU batches; returning False stops
+        the run with rc 1 (BREAK_HIT), like the reference's keep_going()."""
+        proto = C.CFUNCTYPE(C.c_int)
+        # a NULL function pointer clears the callback
+        self._keep_going = proto() if fn is None else proto(lambda: 1 if fn() else 0)
+        self.lib.fedm_set_keep_going(self.h, self._keep_going)
 
     def set_precision(self, precision):
         if self.lib.fedm_set_precision(self.h, precision) != 0:

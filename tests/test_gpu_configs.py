@@ -173,3 +173,53 @@ def test_wide_embedding_task_bit_exact(ctx, E, algorithm):
     assert np.array_equal(g["nn_idx"], o["nn_idx"])
     assert np.array_equal(g["nn_dist"].view(np.int64), o["nn_dist"].view(np.int64))
     assert np.array_equal(g["predictions"], o["predictions"], equal_nan=True)
+
+
+def test_keep_going_stops_between_batches():
+    """keep_going() (src/edm.cpp:572-591) is polled before every task batch:
+    returning false stops the run with rc 1 (BREAK_HIT).  The context (its
+    stream, pool and the background splitter) is usable again afterwards."""
+    c = fedm.Context(0, precision=fedm.PRECISION_MIXED)
+    try:
+        w = workloads.ccm_config(T=6000, reps=40, n_libs=5, hi=5000)
+        kw = dict(E=4, library=w["libraries"], numReps=40, seed=w["seed"], algorithm="simplex")
+        polls = []
+
+        def keep_going():
+            polls.append(1)
+            return len(polls) < 2  # let the first batch run, stop before the second
+
+        c.set_keep_going(keep_going)
+        r = fedm.edm(w["t"], w["x"], w["y"], ctx=c, **kw)
+        assert r["rc"] == 1 and len(polls) == 2
+        c.set_keep_going(None)
+        r2 = fedm.edm(w["t"], w["x"], w["y"], ctx=c, **kw)
+        assert r2["rc"] == 0 and len(r2["stats"]["rho"]) == 40 * 5
+        o = edm_oracle.oracle_edm(w["t"], w["x"], w["y"], numThreads=16, **kw)
+        _stats_close(r2, o)
+    finally:
+        c.close()
+
+
+@pytest.mark.parametrize("levels", [6, 40])
+@pytest.mark.parametrize("algorithm", ["simplex", "smap"])
+def test_ties_and_duplicate_rows_bit_exact(ctx, levels, algorithm):
+    """A series quantised to a few levels has many identical manifold rows:
+    exact-zero distances (excluded, src/distances.cpp:218), more zeros than
+    the mixed kernel keeps slots for (those points fall back to the exact
+    kernels), and many equal distances ordered by library index
+    (src/edm.cpp:652-681).  Neighbours, distances and forecasts must be the
+    oracle's bits."""
+    t, x, _ = workloads.coupled_logistic(3000, seed=11)
+    xq = np.round(x * levels) / levels
+    lib = np.zeros(3000, bool)
+    lib[:1800] = True
+    kw = dict(E=3, theta=[0.0, 1.5], algorithm=algorithm)
+    a = fedm.normalise(t, xq, **kw)
+    k = 4 + (algorithm == "smap")
+    g = ctx.run_task(a, lib, ~lib, 3, k)
+    o = edm_oracle.oracle_task(edm_oracle.normalise(t, xq, **kw), lib, ~lib, 3, k)
+    assert np.array_equal(g["nn_idx"], o["nn_idx"])
+    assert np.array_equal(g["nn_dist"].view(np.int64), o["nn_dist"].view(np.int64))
+    assert np.array_equal(g["predictions"], o["predictions"], equal_nan=True)
+    assert np.array_equal(g["kused"], o["kused"])
