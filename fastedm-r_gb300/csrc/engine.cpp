@@ -619,41 +619,12 @@ void run_group(Context& ctx, const Options& o, const std::vector<Task>& tasks, c
     }
     ctx.timing.kernel_launches += (job.dFp != job.dF ? 2 : 1) + 1;  // centring, counter fill
     m.kslots = C;
-    if (o.algorithm == 1 && ctx.smap_deferred && !wide) {
-      // S-map alternative: scan + re-rank in batches of items; each batch's
-      // neighbour lists go to a separate register-resident SVD kernel
-      const long long batch_points = 8LL << 20;
-      const int batch_items = (int)std::max<long long>(1, batch_points / MIX_POINTS);
-      const long long cap = std::min<long long>((long long)batch_items * MIX_POINTS, std::max<long long>(P, 1));
-      m.defer = 1;
-      m.l_cap = (int)cap;
-      m.l_point = (long long*)ctx.buf("l_point", (size_t)cap * 8);
-      m.l_prow = (int*)ctx.buf("l_prow", (size_t)cap * 4);
-      m.l_task = (int*)ctx.buf("l_task", (size_t)cap * 4);
-      m.l_k = (int*)ctx.buf("l_k", (size_t)cap * 4);
-      m.l_rows = (int*)ctx.buf("l_rows", (size_t)cap * C * 4);
-      m.l_dist = (double*)ctx.buf("l_dist", (size_t)cap * C * 8);
-      m.l_count = (int*)ctx.buf("l_count", 4);
-      for (int b0 = 0; b0 < m.n_items; b0 += batch_items) {
-        if (ctx.keep_going && !ctx.keep_going())
-          throw Error{ RC_BREAK_HIT, "cancelled" };
-        m.item_begin = b0;
-        m.item_end = std::min(m.n_items, b0 + batch_items);
-        fill_i32(m.counter, 1, 0, s);
-        fill_i32(m.l_count, 1, 0, s);
-        timed([&] { launch_knn_mixed(g, m, C, ctx.num_sms, s); });
-        launch_smap_lists(g, m, ctx.num_sms, s);
-        ctx.check("smap lists");
-        ctx.timing.kernel_launches += 4;
-      }
-    } else {
-      m.item_begin = 0;
-      m.item_end = m.n_items;
-      if (wide)
-        timed([&] { launch_knn_wide(g, m, ctx.num_sms, s); });
-      else
-        timed([&] { launch_knn_mixed(g, m, C, ctx.num_sms, s); });
-    }
+    m.item_begin = 0;
+    m.item_end = m.n_items;
+    if (wide)
+      timed([&] { launch_knn_wide(g, m, ctx.num_sms, s); });
+    else
+      timed([&] { launch_knn_mixed(g, m, C, ctx.num_sms, s); });
     int nfb = 0, herr = 0;
     unsigned long long nops = 0;
     ctx.download(&nfb, m.fb_count, 4);

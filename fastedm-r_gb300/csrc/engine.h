@@ -25,10 +25,6 @@ public:
   cudaStream_t stream = nullptr;
   int precision = FEDM_PRECISION_MIXED;
   int (*keep_going)(void) = nullptr;
-  // S-map in the mixed path: solve inside the scan kernel (false, default:
-  // the FP64 solve overlaps the FP32 scan of other warps) or in a separate
-  // kernel over batched neighbour lists (true)
-  bool smap_deferred = false;
   // S-map in the mixed path, in-kernel form: 0 = every warp scans then
   // solves (knn_mixed_kernel, two CTAs per SM); 3 = the same kernel at three
   // CTAs per SM (85 registers; used for k <= 6, else the two-CTA form; the

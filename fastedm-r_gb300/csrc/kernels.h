@@ -133,22 +133,7 @@ struct MixedRun
                        // 4 / 8 = knn_smap_ws_kernel
   int item_begin;      // first item of this launch (the queue head starts here)
   int item_end;        // one past the last item of this launch
-  // S-map: when set, the neighbour lists are appended here and solved by
-  // launch_smap_lists instead of in the scan kernel
-  int defer;
-  long long* l_point;  // [cap] global point id
-  int* l_prow;         // [cap] prediction row
-  int* l_task;         // [cap] task slot
-  int* l_k;            // [cap] neighbours used
-  int* l_rows;         // [cap x kslots] library rows of the neighbours
-  double* l_dist;      // [cap x kslots] their FP64 distances
-  int* l_count;
-  int l_cap;
 };
-
-// Solves the deferred S-map systems of launch_knn_mixed (one thread per
-// point, all thetas; the SVD is unrolled for the compile-time size).
-void launch_smap_lists(const GroupParams& g, const MixedRun& m, int num_sms, cudaStream_t s);
 
 void launch_knn_mixed(const GroupParams& g, const MixedRun& m, int C, int num_sms, cudaStream_t s);
 

@@ -26,9 +26,6 @@ namespace fedm {
 
 namespace {
 
-template<int EA>
-__device__ __noinline__ void smap_point(const GroupParams& g, long long p, int prow, bool save, int keff,
-                                        const int* rows, const double* cd);
 
 // OCC: CTAs per SM the register budget is set for (2: 128 registers, 3: 85).
 template<int EA, int C, int ALG, int OCC = 2>
@@ -187,68 +184,6 @@ __global__ void __launch_bounds__(TPB + 32 * SW, 1) knn_smap_ws_kernel(GroupPara
   add_ops(m, ops);  // both roles leave their loops as whole warps
 }
 
-// S-map forecast of one point from its neighbour rows and FP64 distances,
-// all thetas (src/edm.cpp:737-814); the normal matrix, the rotation
-// accumulators and the right-hand side stay in registers.
-template<int EA>
-__device__ __noinline__ void smap_point(const GroupParams& g, long long p, int prow, bool save, int keff,
-                                        const int* rows, const double* cd)
-{
-  constexpr int n = EA + 1;
-  double y[EA];
-#pragma unroll
-  for (int j = 0; j < EA; j++)
-    y[j] = g.Fp[(size_t)prow * EA + j];
-  double mean = 0;
-  for (int j = 0; j < keff; j++)
-    mean = add(mean, cd[j]);
-  mean = dvd(mean, (double)keff);
-  for (int t = 0; t < g.n_thetas; t++) {
-    const double theta = g.thetas[t];
-    double W[n][n], bv[n], xs[n];
-#pragma unroll
-    for (int a = 0; a < n; a++) {
-      bv[a] = 0;
-#pragma unroll
-      for (int b = 0; b < n; b++)
-        W[a][b] = 0;
-    }
-    for (int i = 0; i < keff; i++) {
-      const double w = exp_rn(mul(-theta, dvd(cd[i], mean)));
-      const int row = rows[i];
-      double xr[n];
-      xr[0] = w;
-#pragma unroll
-      for (int j = 1; j < n; j++)
-        xr[j] = mul(w, g.F[(size_t)row * EA + j - 1]);
-      const double yl = mul(w, g.lib_target[row]);
-#pragma unroll
-      for (int a = 0; a < n; a++) {
-#pragma unroll
-        for (int b = a; b < n; b++)
-          W[a][b] = add(W[a][b], mul(xr[a], xr[b]));
-        bv[a] = add(bv[a], mul(xr[a], yl));
-      }
-    }
-#pragma unroll
-    for (int a = 0; a < n; a++)
-#pragma unroll
-      for (int b = 0; b < a; b++)
-        W[a][b] = W[b][a];
-    svd_solve_n<n>(W, bv, xs);
-    double r = xs[0];
-#pragma unroll
-    for (int j = 0; j < EA; j++)
-      r = add(r, mul(y[j], xs[j + 1]));
-    if (g.coeffs && save && t == g.n_thetas - 1) {
-#pragma unroll
-      for (int j = 0; j < n; j++)
-        g.coeffs[(size_t)p * n + j] = fabs(xs[j]) < 1.0e-11 ? MISS : xs[j];
-    }
-    g.pred[(size_t)t * g.total_points + p] = r;
-  }
-}
-
 // The same forecast with the normal matrix in registers and the solver's
 // rotation accumulators in the caller's shared-memory slice (the
 // warp-specialised kernel's solver threads).  Identical operations and bits.
@@ -312,77 +247,6 @@ __device__ __noinline__ int smap_point_sm(const GroupParams& g, long long p, int
     g.pred[(size_t)t * g.total_points + p] = r;
   }
   return ops;
-}
-
-template<int EA>
-__global__ void __launch_bounds__(128) smap_lists_kernel(GroupParams g, MixedRun m)
-{
-  constexpr int n = EA + 1;
-  const int q = blockIdx.x * blockDim.x + threadIdx.x;
-  if (q >= *m.l_count)
-    return;
-  const long long p = m.l_point[q];
-  const int prow = m.l_prow[q];
-  const int tk = m.l_task[q];
-  const bool save = (tk >> 30) & 1;
-  const int keff = m.l_k[q];
-  const int* rows = m.l_rows + (size_t)q * m.kslots;
-  const double* cd = m.l_dist + (size_t)q * m.kslots;
-  double y[EA];
-#pragma unroll
-  for (int j = 0; j < EA; j++)
-    y[j] = g.Fp[(size_t)prow * EA + j];
-  // src/edm.cpp:744-745: w = exp(-theta * d / mean(d))
-  double mean = 0;
-  for (int j = 0; j < keff; j++)
-    mean = add(mean, cd[j]);
-  mean = dvd(mean, (double)keff);
-  for (int t = 0; t < g.n_thetas; t++) {
-    const double theta = g.thetas[t];
-    double W[n][n], bv[n], xs[n];
-#pragma unroll
-    for (int a = 0; a < n; a++) {
-      bv[a] = 0;
-#pragma unroll
-      for (int b = 0; b < n; b++)
-        W[a][b] = 0;
-    }
-    // X^T X and X^T y summed over the neighbours in order: each entry sees the
-    // same additions as the reference's products (src/edm.cpp:749-782)
-    for (int i = 0; i < keff; i++) {
-      const double w = exp_rn(mul(-theta, dvd(cd[i], mean)));
-      const int row = rows[i];
-      double xr[n];
-      xr[0] = w;
-#pragma unroll
-      for (int j = 1; j < n; j++)
-        xr[j] = mul(w, g.F[(size_t)row * EA + j - 1]);
-      const double yl = mul(w, g.lib_target[row]);
-#pragma unroll
-      for (int a = 0; a < n; a++) {
-#pragma unroll
-        for (int b = a; b < n; b++)
-          W[a][b] = add(W[a][b], mul(xr[a], xr[b]));
-        bv[a] = add(bv[a], mul(xr[a], yl));
-      }
-    }
-#pragma unroll
-    for (int a = 0; a < n; a++)
-#pragma unroll
-      for (int b = 0; b < a; b++)
-        W[a][b] = W[b][a];
-    svd_solve_n<n>(W, bv, xs);
-    double r = xs[0];
-#pragma unroll
-    for (int j = 0; j < EA; j++)
-      r = add(r, mul(y[j], xs[j + 1]));
-    if (g.coeffs && save && t == g.n_thetas - 1) {
-#pragma unroll
-      for (int j = 0; j < n; j++)
-        g.coeffs[(size_t)p * n + j] = fabs(xs[j]) < 1.0e-11 ? MISS : xs[j];
-    }
-    g.pred[(size_t)t * g.total_points + p] = r;
-  }
 }
 
 template<int EA, int C, int ALG, int OCC = 2>
@@ -459,25 +323,6 @@ __global__ void center_kernel(const double* F, long long n, int Ea, const double
 }
 
 } // namespace
-
-void launch_smap_lists(const GroupParams& g, const MixedRun& m, int num_sms, cudaStream_t s)
-{
-  (void)num_sms;
-  const int blocks = (m.l_cap + 127) / 128;
-  if (blocks <= 0)
-    return;
-  switch (g.Ea) {
-    case 1: smap_lists_kernel<1><<<blocks, 128, 0, s>>>(g, m); break;
-    case 2: smap_lists_kernel<2><<<blocks, 128, 0, s>>>(g, m); break;
-    case 3: smap_lists_kernel<3><<<blocks, 128, 0, s>>>(g, m); break;
-    case 4: smap_lists_kernel<4><<<blocks, 128, 0, s>>>(g, m); break;
-    case 5: smap_lists_kernel<5><<<blocks, 128, 0, s>>>(g, m); break;
-    case 6: smap_lists_kernel<6><<<blocks, 128, 0, s>>>(g, m); break;
-    case 7: smap_lists_kernel<7><<<blocks, 128, 0, s>>>(g, m); break;
-    case 8: smap_lists_kernel<8><<<blocks, 128, 0, s>>>(g, m); break;
-    default: break;
-  }
-}
 
 void launch_knn_mixed(const GroupParams& g, const MixedRun& m, int C, int num_sms, cudaStream_t s)
 {

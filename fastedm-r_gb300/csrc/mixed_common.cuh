@@ -90,8 +90,8 @@ struct Cand
 // every valid neighbour is used -- and applies the k rules of
 // src/edm.cpp:565-639.  Returns true with keff, rows (library manifold rows)
 // and cd (their FP64 distances) set when a forecast follows; false when the
-// point was handed to the exact kernels, has no valid neighbour, or its list
-// went to the deferred S-map batch.  ops accumulates the FP64 operations.
+// point was handed to the exact kernels or has no valid neighbour.  ops
+// accumulates the FP64 operations.
 template<int EA, int C>
 __device__ __forceinline__ bool prepare_point(const GroupParams& g, const MixedRun& m, const DevTask& T, long long p,
                                               int prow, const Cand<C>& cand, int& keff, int (&rows)[C + ZCAP],
@@ -202,18 +202,6 @@ __device__ __forceinline__ bool prepare_point(const GroupParams& g, const MixedR
   }
   for (int j = 0; j < keff; j++)
     rows[j] = g.lib_rows[T.lib_off + ci[j]];
-  if (m.defer) {
-    const int slot = atomicAdd(m.l_count, 1);
-    m.l_point[slot] = p;
-    m.l_prow[slot] = prow;
-    m.l_task[slot] = T.task | (T.save_coeffs ? (1 << 30) : 0);
-    m.l_k[slot] = keff;
-    for (int j = 0; j < keff; j++) {
-      m.l_rows[(size_t)slot * m.kslots + j] = rows[j];
-      m.l_dist[(size_t)slot * m.kslots + j] = cd[j];
-    }
-    return false;
-  }
   return true;
 }
 

@@ -1,8 +1,7 @@
 // The JacobiSVD restatement of smap_solve.cuh for a compile-time size N,
 // fully unrolled so the work matrix lives in registers.  The two rotation
-// accumulators U and V are reached through an accessor: registers
-// (svd_solve_n) or a per-thread slice of shared memory interleaved across
-// threads (svd_solve_nm with StridedMat).  Every floating-point operation and
+// accumulators U and V are reached through an accessor (StridedMat: a
+// per-thread slice of shared memory interleaved across threads).  Every floating-point operation and
 // its order are those of svd_solve(): the results are the same bits.
 #pragma once
 
@@ -21,13 +20,6 @@ struct StridedMat
   double* base;
   int stride;
   __device__ __forceinline__ double& operator()(int i, int j) const { return base[(i * N + j) * stride]; }
-};
-
-template<int N>
-struct RegMat
-{
-  double (&m)[N][N];
-  __device__ __forceinline__ double& operator()(int i, int j) const { return m[i][j]; }
 };
 
 // ops accumulates the FP64 add/sub/mul/div/sqrt operations performed, with
@@ -234,14 +226,6 @@ __device__ __forceinline__ void svd_solve_nm(double (&W)[N][N], const double (&b
     x[r] = s;
   }
   ops += rank * (2 * N + 2) + 2 * N * rank;
-}
-
-template<int N>
-__device__ __forceinline__ void svd_solve_n(double (&W)[N][N], const double (&b)[N], double (&x)[N])
-{
-  double Ur[N][N], Vr[N][N];
-  int ops = 0;
-  svd_solve_nm<N>(W, b, x, RegMat<N>{ Ur }, RegMat<N>{ Vr }, ops);
 }
 
 } // namespace fedm
