@@ -34,11 +34,12 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT / "tests"))
 METRIC = "CCM S-map predictions/s: batched FP32+FP64-fix vs plain FP64 GPU @|Δρ|≤1e-6"
 # DRAM bytes per S-map prediction point of the S-map kernel
-# (knn_mixed_kernel<4,8,1,3>): ncu dram__bytes_read.sum + dram__bytes_write.sum
-# of one launch over the 2-replicate x 20-library workload (457.4 MB +
-# 5243.6 MB) divided by its 1 999 880 points.  The traffic is the solver's
-# per-thread scratch and spills leaving L1, so it scales with the points.
-SMAP_DRAM_BYTES_PER_POINT = 2850.7
+# (knn_one_kernel<4,8,4,1024,1,6>): ncu dram__bytes_read.sum +
+# dram__bytes_write.sum of one launch over the 2-replicate x 20-library
+# workload (2734.6 MB + 10037.9 MB) divided by its 1 999 880 points.  The
+# traffic is the solver's per-thread scratch and spills leaving L1, so it
+# scales with the points of a launch.
+SMAP_DRAM_BYTES_PER_POINT = 6386.6
 
 
 def hbm_peak():
@@ -274,7 +275,7 @@ def run_ours(a):
                 "host_ms_per_step": {k: mean_of(k) for k in ("host_ms", "list_wait_ms", "setup_ms", "finish_ms")}},
         "gpu_launches": int(sum(s["kernel_launches"] for s in per_step)),
         "roofline": {
-            "kernel": "knn_mixed_kernel<E=4,C=8,smap> (FP32 scan + FP64 re-rank + JacobiSVD solve)",
+            "kernel": "knn_one_kernel<E=4,C=8,smap,6 CTAs/SM> (FP32 scan + FP64 re-rank + JacobiSVD solve)",
             "bound": "fp64_simt", "achieved": sm_fp64, "peak": fp64_unfused_peak, "unit": "TFLOP/s",
             "frac": sm_fp64 / fp64_unfused_peak,
             "peak_source": "measured FP64 multiply+add rate without fusion on this GPU (fedm_measure_peak kind 3; "

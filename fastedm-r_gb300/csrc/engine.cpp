@@ -49,10 +49,13 @@ Context::Context(int dev) : device(dev)
   ck(cudaSetDevice(dev), "cudaSetDevice");
   ck(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), "cudaStreamCreate");
   ck(cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, dev), "cudaDeviceGetAttribute");
-  if (const char* v = std::getenv("FEDM_SMAP_SOLVER_WARPS")) {
-    const int w = std::atoi(v);
-    if (w == 0 || w == 3 || w == 4 || w == 8)
-      smap_solver_warps = w;
+  if (const char* v = std::getenv("FEDM_SMAP_KERNEL")) {
+    static const std::pair<const char*, int> forms[] = {
+      { "one6", SMAP_ONE6 }, { "fused2", SMAP_FUSED2 }, { "ws4", SMAP_WS4 }, { "ws8", SMAP_WS8 }
+    };
+    for (const auto& f : forms)
+      if (std::strcmp(v, f.first) == 0)
+        smap_form = f.second;
   }
 }
 
@@ -289,7 +292,7 @@ struct GroupJob
 constexpr int KCAP_MAX = 16384;
 constexpr int MIX_KMAX = 14;        // neighbours the mixed kernel serves (slots C = 16)
 constexpr int MIX_POINTS = 512;     // prediction points per mixed work item
-constexpr int WIDE_EA = 16;         // widest embedding of the mixed path (knn_wide_kernel above 8)
+constexpr int WIDE_EA = 16;         // widest embedding of the mixed path (knn_one_kernel's wide form above 8)
 constexpr int WIDE_KMAX = 30;       // neighbours the wide kernel serves (slots C = 32)
 constexpr int WIDE_POINTS = 256;    // prediction points per wide work item
 constexpr size_t LAZY_FIRST_BATCH = 64;  // first task batch of a group with lazily produced CCM lists
@@ -575,7 +578,9 @@ void run_group(Context& ctx, const Options& o, const std::vector<Task>& tasks, c
   if (any_mixed) {
     const bool wide = Ea > 8;
     const int S = Ea <= 4 ? 4 : (Ea <= 8 ? 8 : 16);
-    const int item_points = wide ? WIDE_POINTS : MIX_POINTS;
+    const int C = wide ? 32 : (kmix <= 6 ? 8 : 16);
+    const bool one = !wide && o.algorithm == 1 && C == 8 && ctx.smap_form == SMAP_ONE6;
+    const int item_points = (wide || one) ? WIDE_POINTS : MIX_POINTS;
     const long long nrows = (long long)rows.n_rows;
     double* d_center = (double*)ctx.buf("center", Ea * 8);
     ctx.upload(d_center, center.data(), Ea * 8);
@@ -607,12 +612,11 @@ void run_group(Context& ctx, const Options& o, const std::vector<Task>& tasks, c
     m.fp64_ops = (unsigned long long*)(m.counter + 2);
     m.error = m.counter + 4;
     fill_i32(m.counter, 8, 0, s);
-    m.solver_warps = o.algorithm == 1 ? ctx.smap_solver_warps : 0;
+    m.smap_form = o.algorithm == 1 ? ctx.smap_form : SMAP_FUSED2;
     m.fb_cap = (int)std::min<long long>(std::max<long long>(P, 1), FB_CAP);
     m.fb_list = (long long*)ctx.buf("fb_list", (size_t)m.fb_cap * 8);
     m.gamma = (Ea + 2) * std::ldexp(1.0, -23);
     m.err_abs = std::ldexp(R, -21) + 1e-21;
-    const int C = wide ? 32 : (kmix <= 6 ? 8 : 16);
     if (job.detail) {
       m.nn_idx = (int*)ctx.buf("mix_nn_idx", (size_t)std::max<long long>(P, 1) * C * 4);
       m.nn_dist = (double*)ctx.buf("mix_nn_dist", (size_t)std::max<long long>(P, 1) * C * 8);
@@ -623,6 +627,8 @@ void run_group(Context& ctx, const Options& o, const std::vector<Task>& tasks, c
     m.item_end = m.n_items;
     if (wide)
       timed([&] { launch_knn_wide(g, m, ctx.num_sms, s); });
+    else if (one)
+      timed([&] { launch_smap_one(g, m, ctx.num_sms, s); });
     else
       timed([&] { launch_knn_mixed(g, m, C, ctx.num_sms, s); });
     int nfb = 0, herr = 0;

@@ -25,13 +25,10 @@ public:
   cudaStream_t stream = nullptr;
   int precision = FEDM_PRECISION_MIXED;
   int (*keep_going)(void) = nullptr;
-  // S-map in the mixed path, in-kernel form: 0 = every warp scans then
-  // solves (knn_mixed_kernel, two CTAs per SM); 3 = the same kernel at three
-  // CTAs per SM (85 registers; used for k <= 6, else the two-CTA form; the
-  // fastest on GB300 for the CCM workload); 4 or 8 = warp-specialised kernel
-  // with that many FP64 solver warps beside 8 scan warps.
-  // FEDM_SMAP_SOLVER_WARPS overrides it when the context is created.
-  int smap_solver_warps = 3;
+  // In-kernel form of the mixed S-map (SmapForm in kernels.h); the
+  // environment variable FEDM_SMAP_KERNEL (one6, fused2, ws4, ws8)
+  // overrides it when the context is created.
+  int smap_form = SMAP_ONE6;
   std::string last_error;
   fedm_timing timing{};
 

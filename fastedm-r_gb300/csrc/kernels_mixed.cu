@@ -27,9 +27,8 @@ namespace fedm {
 namespace {
 
 
-// OCC: CTAs per SM the register budget is set for (2: 128 registers, 3: 85).
-template<int EA, int C, int ALG, int OCC = 2>
-__global__ void __launch_bounds__(TPB, OCC) knn_mixed_kernel(GroupParams g, MixedRun m)
+template<int EA, int C, int ALG>
+__global__ void __launch_bounds__(TPB, 2) knn_mixed_kernel(GroupParams g, MixedRun m)
 {
   // library rows staged as interleaved pairs: tile[pair][dim] = (row 2i, row 2i+1)
   __shared__ __align__(16) float2 tile[(TILE / 2) * EA];
@@ -249,11 +248,11 @@ __device__ __noinline__ int smap_point_sm(const GroupParams& g, long long p, int
   return ops;
 }
 
-template<int EA, int C, int ALG, int OCC = 2>
+template<int EA, int C, int ALG>
 void launch_one(const GroupParams& g, const MixedRun& m, int num_sms, cudaStream_t s)
 {
   int per_sm = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, knn_mixed_kernel<EA, C, ALG, OCC>, TPB, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, knn_mixed_kernel<EA, C, ALG>, TPB, 0);
   if (per_sm < 1)
     per_sm = 1;
   long long blocks = (long long)num_sms * per_sm;
@@ -261,7 +260,7 @@ void launch_one(const GroupParams& g, const MixedRun& m, int num_sms, cudaStream
     blocks = m.item_end - m.item_begin;
   if (blocks < 1)
     blocks = 1;
-  knn_mixed_kernel<EA, C, ALG, OCC><<<(int)blocks, TPB, 0, s>>>(g, m);
+  knn_mixed_kernel<EA, C, ALG><<<(int)blocks, TPB, 0, s>>>(g, m);
 }
 
 template<int EA, int C, int SW>
@@ -285,13 +284,10 @@ template<int EA, int C, int ALG>
 void launch_ea(const GroupParams& g, const MixedRun& m, int num_sms, cudaStream_t s)
 {
   if constexpr (ALG == 1) {
-    if (m.solver_warps == 4)
+    if (m.smap_form == SMAP_WS4)
       return launch_ws<EA, C, 4>(g, m, num_sms, s);
-    if (m.solver_warps == 8)
+    if (m.smap_form == SMAP_WS8)
       return launch_ws<EA, C, 8>(g, m, num_sms, s);
-    if constexpr (C == 8)
-      if (m.solver_warps == 3)
-        return launch_one<EA, C, ALG, 3>(g, m, num_sms, s);
   }
   launch_one<EA, C, ALG>(g, m, num_sms, s);
 }

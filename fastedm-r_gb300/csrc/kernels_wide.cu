@@ -1,26 +1,30 @@
-// Mixed-precision neighbour search and forecast for wide embeddings:
-// E_a = 9..16 (dt columns double E_a, so E = 5..8 with dt lands here) and up
-// to 30 neighbours.  The kernel is knn_mixed_kernel's with one prediction
-// point per thread and 32 candidate slots, so the lists still fit in
-// registers: a 256-thread CTA takes a work item of 256 points, stages 512
-// library rows of the centred FP32 manifold (row stride 16 floats) per tile
-// as interleaved pairs, and every thread scores two rows against its point
-// per packed step.  Certification, the FP64 re-rank in the reference's
-// operation order and the forecast are finalize_point's, so neighbours and
-// forecasts are the FP64 path's bits.
+// Mixed-precision neighbour search and forecast with one prediction point
+// per thread (knn_mixed_kernel has two):
+//   * wide embeddings, E_a = 9..16 (dt columns double E_a, so E = 5..8 with
+//     dt lands here), up to 30 neighbours: 32 candidate slots, 512-row tiles
+//     of a float manifold with row stride 16;
+//   * the S-map at E_a <= 8, k <= 6 with six CTAs per SM (40 registers):
+//     more warps to hide the FP64 solve's latency (the default form).
+// A 256-thread CTA takes a work item of 256 points, stages library rows of
+// the centred FP32 manifold per tile as interleaved pairs, and every thread
+// scores two rows against its point per packed step.  Certification, the
+// FP64 re-rank in the reference's operation order and the forecast are
+// finalize_point's, so neighbours and forecasts are the FP64 path's bits.
 #include "mixed_common.cuh"
 
 namespace fedm {
 
 namespace {
 
-constexpr int WTILE = 512;  // library rows per tile: 32 KB of shared memory at E_a = 16
-constexpr int WC = 32;      // candidate slots per point
-constexpr int WS = 16;      // row stride of the float manifold
+constexpr int WTILE = 512;  // wide form: library rows per tile, 32 KB of shared memory at E_a = 16
+constexpr int WC = 32;      // wide form: candidate slots per point
+constexpr int WS = 16;      // wide form: row stride of the float manifold
 
-template<int EA>
-__device__ __forceinline__ void scan_item_wide(const GroupParams& g, const MixedRun& m, const DevTask& T, int first,
-                                               int tid, float2* tile, Cand<WC>& c0, int& prow0, bool& a0)
+// One point per thread: C candidate slots, float manifold row stride RS,
+// TR library rows per shared-memory tile.
+template<int EA, int C, int RS, int TR>
+__device__ __forceinline__ void scan_item_one(const GroupParams& g, const MixedRun& m, const DevTask& T, int first,
+                                              int tid, float2* tile, Cand<C>& c0, int& prow0, bool& a0)
 {
   const int pi0 = first + tid;
   a0 = pi0 < T.n_pred;
@@ -30,13 +34,13 @@ __device__ __forceinline__ void scan_item_wide(const GroupParams& g, const Mixed
   float2 na[EA];
 #pragma unroll
   for (int j = 0; j < EA; j++) {
-    const float va = a0 ? -m.Fp32[(size_t)prow0 * WS + j] : -1e30f;
+    const float va = a0 ? -m.Fp32[(size_t)prow0 * RS + j] : -1e30f;
     na[j] = make_float2(va, va);
   }
-  float D0[WC];
-  int I0[WC];
+  float D0[C];
+  int I0[C];
 #pragma unroll
-  for (int j = 0; j < WC; j++) {
+  for (int j = 0; j < C; j++) {
     D0[j] = INFINITY;
     I0[j] = -1;
   }
@@ -45,14 +49,14 @@ __device__ __forceinline__ void scan_item_wide(const GroupParams& g, const Mixed
 #pragma unroll
   for (int j = 0; j < ZCAP; j++)
     zi0[j] = -1;
-  for (int t0 = 0; t0 < T.n_lib; t0 += WTILE) {
-    const int cnt = min(WTILE, T.n_lib - t0);
+  for (int t0 = 0; t0 < T.n_lib; t0 += TR) {
+    const int cnt = min(TR, T.n_lib - t0);
     const int npairs = (cnt + 1) >> 1;
     __syncthreads();
     for (int i = tid; i < 2 * npairs; i += TPB) {
       float* dst = reinterpret_cast<float*>(tile + (i >> 1) * EA) + (i & 1);
       if (i < cnt) {
-        const float* src = m.F32 + (size_t)g.lib_rows[T.lib_off + t0 + i] * WS;
+        const float* src = m.F32 + (size_t)g.lib_rows[T.lib_off + t0 + i] * RS;
 #pragma unroll
         for (int j = 0; j < EA; j++)
           dst[2 * j] = src[j];
@@ -73,15 +77,15 @@ __device__ __forceinline__ void scan_item_wide(const GroupParams& g, const Mixed
         d = __fadd2_rn(xr[j], na[j]);
         sa = __ffma2_rn(d, d, sa);
       }
-      if (fminf(sa.x, sa.y) < D0[WC - 1]) {
+      if (fminf(sa.x, sa.y) < D0[C - 1]) {
         const int li = t0 + 2 * ip;
-        offer<WC>(D0, I0, z0, zi0, sa.x, li);
-        offer<WC>(D0, I0, z0, zi0, sa.y, li + 1);
+        offer<C>(D0, I0, z0, zi0, sa.x, li);
+        offer<C>(D0, I0, z0, zi0, sa.y, li + 1);
       }
     }
   }
 #pragma unroll
-  for (int j = 0; j < WC; j++) {
+  for (int j = 0; j < C; j++) {
     c0.D[j] = D0[j];
     c0.I[j] = I0[j];
   }
@@ -91,10 +95,10 @@ __device__ __forceinline__ void scan_item_wide(const GroupParams& g, const Mixed
     c0.zi[j] = zi0[j];
 }
 
-template<int EA, int ALG>
-__global__ void __launch_bounds__(TPB, 2) knn_wide_kernel(GroupParams g, MixedRun m)
+template<int EA, int C, int RS, int TR, int ALG, int OCC>
+__global__ void __launch_bounds__(TPB, OCC) knn_one_kernel(GroupParams g, MixedRun m)
 {
-  __shared__ __align__(16) float2 tile[(WTILE / 2) * EA];
+  __shared__ __align__(16) float2 tile[(TR / 2) * EA];
   __shared__ int s_item;
   const int tid = threadIdx.x;
   unsigned long long ops = 0;
@@ -110,22 +114,22 @@ __global__ void __launch_bounds__(TPB, 2) knn_wide_kernel(GroupParams g, MixedRu
     }
     const int2 it = m.items[item];
     const DevTask T = g.tasks[it.x];
-    Cand<WC> c0;
+    Cand<C> c0;
     int prow0;
     bool a0;
-    scan_item_wide<EA>(g, m, T, it.y, tid, tile, c0, prow0, a0);
+    scan_item_one<EA, C, RS, TR>(g, m, T, it.y, tid, tile, c0, prow0, a0);
     if (a0) {
-      const Cand<WC> c = c0;
-      ops += finalize_point<EA, WC, ALG>(g, m, T, T.point_base + it.y + tid, prow0, c);
+      const Cand<C> c = c0;
+      ops += finalize_point<EA, C, ALG>(g, m, T, T.point_base + it.y + tid, prow0, c);
     }
   }
 }
 
-template<int EA, int ALG>
-void launch_wide(const GroupParams& g, const MixedRun& m, int num_sms, cudaStream_t s)
+template<int EA, int C, int RS, int TR, int ALG, int OCC>
+void launch_one(const GroupParams& g, const MixedRun& m, int num_sms, cudaStream_t s)
 {
   int per_sm = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, knn_wide_kernel<EA, ALG>, TPB, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, knn_one_kernel<EA, C, RS, TR, ALG, OCC>, TPB, 0);
   if (per_sm < 1)
     per_sm = 1;
   long long blocks = (long long)num_sms * per_sm;
@@ -133,7 +137,13 @@ void launch_wide(const GroupParams& g, const MixedRun& m, int num_sms, cudaStrea
     blocks = m.item_end - m.item_begin;
   if (blocks < 1)
     blocks = 1;
-  knn_wide_kernel<EA, ALG><<<(int)blocks, TPB, 0, s>>>(g, m);
+  knn_one_kernel<EA, C, RS, TR, ALG, OCC><<<(int)blocks, TPB, 0, s>>>(g, m);
+}
+
+template<int EA, int ALG>
+void launch_wide(const GroupParams& g, const MixedRun& m, int num_sms, cudaStream_t s)
+{
+  launch_one<EA, WC, WS, WTILE, ALG, 2>(g, m, num_sms, s);
 }
 
 template<int ALG>
@@ -153,6 +163,24 @@ void launch_wide_alg(const GroupParams& g, const MixedRun& m, int num_sms, cudaS
 }
 
 } // namespace
+
+void launch_smap_one(const GroupParams& g, const MixedRun& m, int num_sms, cudaStream_t s)
+{
+  if (m.item_end <= m.item_begin)
+    return;
+  constexpr int OCC = 6;
+  switch (g.Ea) {
+    case 1: launch_one<1, 8, 4, 1024, 1, OCC>(g, m, num_sms, s); break;
+    case 2: launch_one<2, 8, 4, 1024, 1, OCC>(g, m, num_sms, s); break;
+    case 3: launch_one<3, 8, 4, 1024, 1, OCC>(g, m, num_sms, s); break;
+    case 4: launch_one<4, 8, 4, 1024, 1, OCC>(g, m, num_sms, s); break;
+    case 5: launch_one<5, 8, 8, 1024, 1, OCC>(g, m, num_sms, s); break;
+    case 6: launch_one<6, 8, 8, 1024, 1, OCC>(g, m, num_sms, s); break;
+    case 7: launch_one<7, 8, 8, 1024, 1, OCC>(g, m, num_sms, s); break;
+    case 8: launch_one<8, 8, 8, 1024, 1, OCC>(g, m, num_sms, s); break;
+    default: break;
+  }
+}
 
 void launch_knn_wide(const GroupParams& g, const MixedRun& m, int num_sms, cudaStream_t s)
 {

@@ -128,12 +128,13 @@ def test_mixed_fp64_operation_count(ctx):
         assert 2000 <= per["smap"] <= 20000, per
 
 
-@pytest.mark.parametrize("solver_warps", ["0", "3", "4", "8"])
-def test_smap_kernel_forms_agree(solver_warps, monkeypatch):
-    """The mixed S-map runs in one of three kernel forms: every warp scans
-    then solves (0), or 8 scan warps hand candidate lists to 4 or 8 FP64
-    solver warps through shared memory.  All give the FP64 path's bits."""
-    monkeypatch.setenv("FEDM_SMAP_SOLVER_WARPS", solver_warps)
+@pytest.mark.parametrize("form", ["one6", "fused2", "ws4", "ws8"])
+def test_smap_kernel_forms_agree(form, monkeypatch):
+    """The mixed S-map runs in one of four kernel forms: every warp scans then
+    solves, with one point per thread at six CTAs per SM or two points per
+    thread at two; or 8 scan warps hand candidate lists to 4 or 8 FP64 solver
+    warps through shared memory.  All give the FP64 path's bits."""
+    monkeypatch.setenv("FEDM_SMAP_KERNEL", form)
     w = workloads.ccm_config(T=6000, reps=3, n_libs=5, hi=5000)
     kw = dict(E=4, library=w["libraries"], numReps=3, seed=w["seed"], algorithm="smap", theta=2.0,
               savePredictions=True, saveSMAPCoeffs=True)
