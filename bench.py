@@ -36,10 +36,10 @@ METRIC = "CCM S-map predictions/s: batched FP32+FP64-fix vs plain FP64 GPU @|Î”Ï
 # DRAM bytes per S-map prediction point of the S-map kernel
 # (knn_one_kernel<4,8,4,1024,1,6>): ncu dram__bytes_read.sum +
 # dram__bytes_write.sum of one launch over the 2-replicate x 20-library
-# workload (2734.6 MB + 10037.9 MB) divided by its 1 999 880 points.  The
+# workload (2767.4 MB + 10088.8 MB) divided by its 1 999 880 points.  The
 # traffic is the solver's per-thread scratch and spills leaving L1, so it
 # scales with the points of a launch.
-SMAP_DRAM_BYTES_PER_POINT = 6386.6
+SMAP_DRAM_BYTES_PER_POINT = 6428.5
 
 
 def hbm_peak():
@@ -287,7 +287,7 @@ def run_ours(a):
             "traffic": traffic,
             "fp32_scan": {"achieved": sm_fp32, "peak": fp32_peak, "frac": sm_fp32 / fp32_peak,
                           "flops": "3*E per (prediction, library) pair"},
-            "simplex_kernel": {"kernel": "knn_mixed_kernel<E=4,C=8,simplex>", "bound": "fp32_simt",
+            "simplex_kernel": {"kernel": "knn_one_kernel<E=4,C=8,simplex,6 CTAs/SM>", "bound": "fp32_simt",
                                "achieved": sx_fp32, "peak": fp32_peak, "frac": sx_fp32 / fp32_peak,
                                "kernel_ms_per_step": sx_ms,
                                "peak_source": "measured FFMA rate of this GPU (fedm_measure_peak kind 0)"},

@@ -14,6 +14,7 @@
 #include <chrono>
 #include <climits>
 #include <cmath>
+#include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <numeric>
@@ -49,13 +50,13 @@ Context::Context(int dev) : device(dev)
   ck(cudaSetDevice(dev), "cudaSetDevice");
   ck(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), "cudaStreamCreate");
   ck(cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, dev), "cudaDeviceGetAttribute");
-  if (const char* v = std::getenv("FEDM_SMAP_KERNEL")) {
+  if (const char* v = std::getenv("FEDM_MIXED_KERNEL")) {
     static const std::pair<const char*, int> forms[] = {
-      { "one6", SMAP_ONE6 }, { "fused2", SMAP_FUSED2 }, { "ws4", SMAP_WS4 }, { "ws8", SMAP_WS8 }
+      { "one6", MIXED_ONE6 }, { "fused2", MIXED_FUSED2 }, { "ws4", MIXED_WS4 }, { "ws8", MIXED_WS8 }
     };
     for (const auto& f : forms)
       if (std::strcmp(v, f.first) == 0)
-        smap_form = f.second;
+        mixed_form = f.second;
   }
 }
 
@@ -579,7 +580,10 @@ void run_group(Context& ctx, const Options& o, const std::vector<Task>& tasks, c
     const bool wide = Ea > 8;
     const int S = Ea <= 4 ? 4 : (Ea <= 8 ? 8 : 16);
     const int C = wide ? 32 : (kmix <= 6 ? 8 : 16);
-    const bool one = !wide && o.algorithm == 1 && C == 8 && ctx.smap_form == SMAP_ONE6;
+    // one point per thread for k <= 6: the default form, and the simplex's
+    // when the S-map uses the warp-specialised kernel
+    const bool ws = o.algorithm == 1 && (ctx.mixed_form == MIXED_WS4 || ctx.mixed_form == MIXED_WS8);
+    const bool one = !wide && C == 8 && ctx.mixed_form != MIXED_FUSED2 && !ws;
     const int item_points = (wide || one) ? WIDE_POINTS : MIX_POINTS;
     const long long nrows = (long long)rows.n_rows;
     double* d_center = (double*)ctx.buf("center", Ea * 8);
@@ -612,7 +616,7 @@ void run_group(Context& ctx, const Options& o, const std::vector<Task>& tasks, c
     m.fp64_ops = (unsigned long long*)(m.counter + 2);
     m.error = m.counter + 4;
     fill_i32(m.counter, 8, 0, s);
-    m.smap_form = o.algorithm == 1 ? ctx.smap_form : SMAP_FUSED2;
+    m.form = ctx.mixed_form;
     m.fb_cap = (int)std::min<long long>(std::max<long long>(P, 1), FB_CAP);
     m.fb_list = (long long*)ctx.buf("fb_list", (size_t)m.fb_cap * 8);
     m.gamma = (Ea + 2) * std::ldexp(1.0, -23);
@@ -628,7 +632,7 @@ void run_group(Context& ctx, const Options& o, const std::vector<Task>& tasks, c
     if (wide)
       timed([&] { launch_knn_wide(g, m, ctx.num_sms, s); });
     else if (one)
-      timed([&] { launch_smap_one(g, m, ctx.num_sms, s); });
+      timed([&] { launch_mixed_one(g, m, ctx.num_sms, s); });
     else
       timed([&] { launch_knn_mixed(g, m, C, ctx.num_sms, s); });
     int nfb = 0, herr = 0;

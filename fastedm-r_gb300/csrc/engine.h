@@ -25,10 +25,10 @@ public:
   cudaStream_t stream = nullptr;
   int precision = FEDM_PRECISION_MIXED;
   int (*keep_going)(void) = nullptr;
-  // In-kernel form of the mixed S-map (SmapForm in kernels.h); the
-  // environment variable FEDM_SMAP_KERNEL (one6, fused2, ws4, ws8)
-  // overrides it when the context is created.
-  int smap_form = SMAP_ONE6;
+  // Kernel form of the mixed path (MixedForm in kernels.h); the environment
+  // variable FEDM_MIXED_KERNEL (one6, fused2, ws4, ws8) overrides it when
+  // the context is created.
+  int mixed_form = MIXED_ONE6;
   std::string last_error;
   fedm_timing timing{};
 

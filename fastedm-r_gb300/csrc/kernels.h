@@ -106,14 +106,15 @@ void launch_stats(const GroupParams& g, const DevTask* tasks_host_unused, int n_
 long long all_mode_slab(int Ea);  // doubles of solver scratch per (point, theta)
 long long smap_nn_scratch_doubles(int num_sms, int n, int kcap);
 
-// In-kernel forms of the mixed S-map (E_a <= 8).  ONE6 applies to k <= 6
-// (8 candidate slots); other k use FUSED2.
-enum SmapForm
+// In-kernel forms of the mixed path (E_a <= 8).  ONE6 applies to k <= 6
+// (8 candidate slots); other k use FUSED2.  WS4 / WS8 are S-map forms; the
+// simplex then uses ONE6.
+enum MixedForm
 {
-  SMAP_FUSED2 = 0,  // knn_mixed_kernel: two points per thread, two CTAs per SM
-  SMAP_ONE6 = 1,    // knn_one_kernel: one point per thread, six CTAs per SM (40 registers)
-  SMAP_WS4 = 2,     // knn_smap_ws_kernel: 8 scan warps, 4 FP64 solver warps
-  SMAP_WS8 = 3      // knn_smap_ws_kernel: 8 scan warps, 8 FP64 solver warps
+  MIXED_FUSED2 = 0,  // knn_mixed_kernel: two points per thread, two CTAs per SM
+  MIXED_ONE6 = 1,    // knn_one_kernel: one point per thread, six CTAs per SM (40 registers)
+  MIXED_WS4 = 2,     // S-map: knn_smap_ws_kernel, 8 scan warps, 4 FP64 solver warps
+  MIXED_WS8 = 3      // S-map: knn_smap_ws_kernel, 8 scan warps, 8 FP64 solver warps
 };
 
 // Mixed-precision neighbour scan for the common case (L2, no missing values,
@@ -139,7 +140,7 @@ struct MixedRun
   int kslots;
   unsigned long long* fp64_ops;  // optional: FP64 operations of the re-rank and forecast stage
   int* error;          // set when a bounded wait of the warp-specialised kernel ran out
-  int smap_form;       // S-map kernel form (SmapForm)
+  int form;            // kernel form (MixedForm)
   int item_begin;      // first item of this launch (the queue head starts here)
   int item_end;        // one past the last item of this launch
 };
@@ -151,8 +152,9 @@ void launch_knn_mixed(const GroupParams& g, const MixedRun& m, int C, int num_sm
 // manifold row stride 16).
 void launch_knn_wide(const GroupParams& g, const MixedRun& m, int num_sms, cudaStream_t s);
 
-// The S-map (E_a <= 8, k <= 6) in the SMAP_ONE6 form; work items of 256 points.
-void launch_smap_one(const GroupParams& g, const MixedRun& m, int num_sms, cudaStream_t s);
+// Simplex or S-map (E_a <= 8, k <= 6) in the MIXED_ONE6 form; work items of
+// 256 points.
+void launch_mixed_one(const GroupParams& g, const MixedRun& m, int num_sms, cudaStream_t s);
 
 // Differentiable S-map over every library neighbour (kernels_adjoint.cu).
 struct AdjointParams

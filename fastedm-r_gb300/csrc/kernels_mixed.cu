@@ -284,9 +284,9 @@ template<int EA, int C, int ALG>
 void launch_ea(const GroupParams& g, const MixedRun& m, int num_sms, cudaStream_t s)
 {
   if constexpr (ALG == 1) {
-    if (m.smap_form == SMAP_WS4)
+    if (m.form == MIXED_WS4)
       return launch_ws<EA, C, 4>(g, m, num_sms, s);
-    if (m.smap_form == SMAP_WS8)
+    if (m.form == MIXED_WS8)
       return launch_ws<EA, C, 8>(g, m, num_sms, s);
   }
   launch_one<EA, C, ALG>(g, m, num_sms, s);

@@ -3,8 +3,9 @@
 //   * wide embeddings, E_a = 9..16 (dt columns double E_a, so E = 5..8 with
 //     dt lands here), up to 30 neighbours: 32 candidate slots, 512-row tiles
 //     of a float manifold with row stride 16;
-//   * the S-map at E_a <= 8, k <= 6 with six CTAs per SM (40 registers):
-//     more warps to hide the FP64 solve's latency (the default form).
+//   * simplex and S-map at E_a <= 8, k <= 6 with six CTAs per SM (40
+//     registers): more warps to hide the scan's and the FP64 solve's
+//     latency (the default form).
 // A 256-thread CTA takes a work item of 256 points, stages library rows of
 // the centred FP32 manifold per tile as interleaved pairs, and every thread
 // scores two rows against its point per packed step.  Certification, the
@@ -21,8 +22,8 @@ constexpr int WC = 32;      // wide form: candidate slots per point
 constexpr int WS = 16;      // wide form: row stride of the float manifold
 
 // One point per thread: C candidate slots, float manifold row stride RS,
-// TR library rows per shared-memory tile.
-template<int EA, int C, int RS, int TR>
+// TR library rows per shared-memory tile, NT threads per CTA.
+template<int EA, int C, int RS, int TR, int NT>
 __device__ __forceinline__ void scan_item_one(const GroupParams& g, const MixedRun& m, const DevTask& T, int first,
                                               int tid, float2* tile, Cand<C>& c0, int& prow0, bool& a0)
 {
@@ -53,7 +54,7 @@ __device__ __forceinline__ void scan_item_one(const GroupParams& g, const MixedR
     const int cnt = min(TR, T.n_lib - t0);
     const int npairs = (cnt + 1) >> 1;
     __syncthreads();
-    for (int i = tid; i < 2 * npairs; i += TPB) {
+    for (int i = tid; i < 2 * npairs; i += NT) {
       float* dst = reinterpret_cast<float*>(tile + (i >> 1) * EA) + (i & 1);
       if (i < cnt) {
         const float* src = m.F32 + (size_t)g.lib_rows[T.lib_off + t0 + i] * RS;
@@ -95,8 +96,8 @@ __device__ __forceinline__ void scan_item_one(const GroupParams& g, const MixedR
     c0.zi[j] = zi0[j];
 }
 
-template<int EA, int C, int RS, int TR, int ALG, int OCC>
-__global__ void __launch_bounds__(TPB, OCC) knn_one_kernel(GroupParams g, MixedRun m)
+template<int EA, int C, int RS, int TR, int ALG, int OCC, int NT = TPB>
+__global__ void __launch_bounds__(NT, OCC) knn_one_kernel(GroupParams g, MixedRun m)
 {
   __shared__ __align__(16) float2 tile[(TR / 2) * EA];
   __shared__ int s_item;
@@ -117,7 +118,7 @@ __global__ void __launch_bounds__(TPB, OCC) knn_one_kernel(GroupParams g, MixedR
     Cand<C> c0;
     int prow0;
     bool a0;
-    scan_item_one<EA, C, RS, TR>(g, m, T, it.y, tid, tile, c0, prow0, a0);
+    scan_item_one<EA, C, RS, TR, NT>(g, m, T, it.y, tid, tile, c0, prow0, a0);
     if (a0) {
       const Cand<C> c = c0;
       ops += finalize_point<EA, C, ALG>(g, m, T, T.point_base + it.y + tid, prow0, c);
@@ -125,11 +126,11 @@ __global__ void __launch_bounds__(TPB, OCC) knn_one_kernel(GroupParams g, MixedR
   }
 }
 
-template<int EA, int C, int RS, int TR, int ALG, int OCC>
+template<int EA, int C, int RS, int TR, int ALG, int OCC, int NT = TPB>
 void launch_one(const GroupParams& g, const MixedRun& m, int num_sms, cudaStream_t s)
 {
   int per_sm = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, knn_one_kernel<EA, C, RS, TR, ALG, OCC>, TPB, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, knn_one_kernel<EA, C, RS, TR, ALG, OCC, NT>, NT, 0);
   if (per_sm < 1)
     per_sm = 1;
   long long blocks = (long long)num_sms * per_sm;
@@ -137,7 +138,7 @@ void launch_one(const GroupParams& g, const MixedRun& m, int num_sms, cudaStream
     blocks = m.item_end - m.item_begin;
   if (blocks < 1)
     blocks = 1;
-  knn_one_kernel<EA, C, RS, TR, ALG, OCC><<<(int)blocks, TPB, 0, s>>>(g, m);
+  knn_one_kernel<EA, C, RS, TR, ALG, OCC, NT><<<(int)blocks, NT, 0, s>>>(g, m);
 }
 
 template<int EA, int ALG>
@@ -164,22 +165,31 @@ void launch_wide_alg(const GroupParams& g, const MixedRun& m, int num_sms, cudaS
 
 } // namespace
 
-void launch_smap_one(const GroupParams& g, const MixedRun& m, int num_sms, cudaStream_t s)
+template<int ALG>
+void launch_one6(const GroupParams& g, const MixedRun& m, int num_sms, cudaStream_t s)
+{
+  constexpr int OCC = 6;
+  switch (g.Ea) {
+    case 1: launch_one<1, 8, 4, 1024, ALG, OCC>(g, m, num_sms, s); break;
+    case 2: launch_one<2, 8, 4, 1024, ALG, OCC>(g, m, num_sms, s); break;
+    case 3: launch_one<3, 8, 4, 1024, ALG, OCC>(g, m, num_sms, s); break;
+    case 4: launch_one<4, 8, 4, 1024, ALG, OCC>(g, m, num_sms, s); break;
+    case 5: launch_one<5, 8, 8, 1024, ALG, OCC>(g, m, num_sms, s); break;
+    case 6: launch_one<6, 8, 8, 1024, ALG, OCC>(g, m, num_sms, s); break;
+    case 7: launch_one<7, 8, 8, 1024, ALG, OCC>(g, m, num_sms, s); break;
+    case 8: launch_one<8, 8, 8, 1024, ALG, OCC>(g, m, num_sms, s); break;
+    default: break;
+  }
+}
+
+void launch_mixed_one(const GroupParams& g, const MixedRun& m, int num_sms, cudaStream_t s)
 {
   if (m.item_end <= m.item_begin)
     return;
-  constexpr int OCC = 6;
-  switch (g.Ea) {
-    case 1: launch_one<1, 8, 4, 1024, 1, OCC>(g, m, num_sms, s); break;
-    case 2: launch_one<2, 8, 4, 1024, 1, OCC>(g, m, num_sms, s); break;
-    case 3: launch_one<3, 8, 4, 1024, 1, OCC>(g, m, num_sms, s); break;
-    case 4: launch_one<4, 8, 4, 1024, 1, OCC>(g, m, num_sms, s); break;
-    case 5: launch_one<5, 8, 8, 1024, 1, OCC>(g, m, num_sms, s); break;
-    case 6: launch_one<6, 8, 8, 1024, 1, OCC>(g, m, num_sms, s); break;
-    case 7: launch_one<7, 8, 8, 1024, 1, OCC>(g, m, num_sms, s); break;
-    case 8: launch_one<8, 8, 8, 1024, 1, OCC>(g, m, num_sms, s); break;
-    default: break;
-  }
+  if (g.algorithm == 1)
+    launch_one6<1>(g, m, num_sms, s);
+  else
+    launch_one6<0>(g, m, num_sms, s);
 }
 
 void launch_knn_wide(const GroupParams& g, const MixedRun& m, int num_sms, cudaStream_t s)

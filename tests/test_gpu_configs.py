@@ -128,16 +128,18 @@ def test_mixed_fp64_operation_count(ctx):
         assert 2000 <= per["smap"] <= 20000, per
 
 
+@pytest.mark.parametrize("algorithm", ["simplex", "smap"])
 @pytest.mark.parametrize("form", ["one6", "fused2", "ws4", "ws8"])
-def test_smap_kernel_forms_agree(form, monkeypatch):
-    """The mixed S-map runs in one of four kernel forms: every warp scans then
-    solves, with one point per thread at six CTAs per SM or two points per
-    thread at two; or 8 scan warps hand candidate lists to 4 or 8 FP64 solver
-    warps through shared memory.  All give the FP64 path's bits."""
-    monkeypatch.setenv("FEDM_SMAP_KERNEL", form)
+def test_mixed_kernel_forms_agree(form, algorithm, monkeypatch):
+    """The mixed path runs in one of four kernel forms: every warp scans then
+    finishes its points, with one point per thread at six CTAs per SM or two
+    points per thread at two; or (S-map) 8 scan warps hand candidate lists to
+    4 or 8 FP64 solver warps through shared memory.  All give the FP64 path's
+    bits."""
+    monkeypatch.setenv("FEDM_MIXED_KERNEL", form)
     w = workloads.ccm_config(T=6000, reps=3, n_libs=5, hi=5000)
-    kw = dict(E=4, library=w["libraries"], numReps=3, seed=w["seed"], algorithm="smap", theta=2.0,
-              savePredictions=True, saveSMAPCoeffs=True)
+    kw = dict(E=4, library=w["libraries"], numReps=3, seed=w["seed"], algorithm=algorithm,
+              theta=2.0 if algorithm == "smap" else 1.0, savePredictions=True, saveSMAPCoeffs=algorithm == "smap")
     cm = fedm.Context(0, precision=fedm.PRECISION_MIXED)
     c64 = fedm.Context(0, precision=fedm.PRECISION_FP64)
     try:
@@ -149,7 +151,8 @@ def test_smap_kernel_forms_agree(form, monkeypatch):
     assert g["rc"] == f["rc"] == 0
     assert np.array_equal(g["stats"]["rho"], f["stats"]["rho"], equal_nan=True)
     assert np.array_equal(g["predictions"], f["predictions"], equal_nan=True)
-    assert np.array_equal(g["coeffs"], f["coeffs"], equal_nan=True)
+    if algorithm == "smap":
+        assert np.array_equal(g["coeffs"], f["coeffs"], equal_nan=True)
 
 
 @pytest.mark.parametrize("E", [5, 8])
