@@ -406,7 +406,7 @@ def run_config(a):
         flush_l2(local)
     barrier(world)
     dev = wall = 0.0
-    preds = launches = 0
+    preds = launches = fallback = 0
     with Clocks(local) as clk:
         for _ in range(a.steps):
             for tm, ws in step():
@@ -414,6 +414,7 @@ def run_config(a):
                 wall += ws
                 preds += tm["predictions"]
                 launches += tm["kernel_launches"]
+                fallback += tm.get("fallback_points", 0)
             flush_l2(local)
     dev = allreduce_max(world, dev)
     wall = allreduce_max(world, wall)
@@ -427,7 +428,8 @@ def run_config(a):
         "ms_per_step": dev / a.steps * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "fp32+fp64", "data": "synthetic (seeded generators)", "config": cfg,
         "e2e": {"value": preds * world / wall, "unit": "predictions/s", "wall_ms_per_step": wall / a.steps * 1e3},
-        "gpu_launches": launches, "predictions_per_step": preds // a.steps, "roofline": None, "cpu_baseline": None,
+        "gpu_launches": launches, "predictions_per_step": preds // a.steps,
+        "fallback_points_per_step": fallback // a.steps, "roofline": None, "cpu_baseline": None,
         "clocks": clk.summary(),
     }
     print(json.dumps(out), flush=True)

@@ -620,7 +620,9 @@ void run_group(Context& ctx, const Options& o, const std::vector<Task>& tasks, c
     m.fb_cap = (int)std::min<long long>(std::max<long long>(P, 1), FB_CAP);
     m.fb_list = (long long*)ctx.buf("fb_list", (size_t)m.fb_cap * 8);
     m.gamma = (Ea + 2) * std::ldexp(1.0, -23);
-    m.err_abs = std::ldexp(R, -21) + 1e-21;
+    // input-rounding term of the certification (kernels_mixed.cu): twice the
+    // proven 2u(1 + 2^-29) R
+    m.err_abs = std::ldexp(R, -22) + 1e-21;
     if (job.detail) {
       m.nn_idx = (int*)ctx.buf("mix_nn_idx", (size_t)std::max<long long>(P, 1) * C * 4);
       m.nn_dist = (double*)ctx.buf("mix_nn_dist", (size_t)std::max<long long>(P, 1) * C * 8);

@@ -1,15 +1,21 @@
 // Mixed-precision neighbour search and forecast (the CCM hot path).
 //
-// Work item = one task x 512 prediction points, taken from a global queue in
-// decreasing library size.  A 256-thread CTA stages 1024 library rows of the
-// centred FP32 manifold in shared memory at a time; every thread scores them
-// against two prediction points and keeps, per point, the C smallest squared
-// FP32 distances (sorted, registers) plus up to two exact zeros.
+// Work item = one task x 512 prediction points (256 in the one-point form of
+// kernels_wide.cu), taken from a global queue in decreasing library size.  A
+// 256-thread CTA stages 1024 library rows of the centred FP32 manifold in
+// shared memory at a time; every thread scores them against two prediction
+// points and keeps, per point, the C smallest squared FP32 distances (sorted,
+// registers) plus up to two exact zeros.
 //
 // Certification.  With u = 2^-24, the FP32 squared distance s of a pair obeys
 // sqrt(s)/sqrt(1+g) - e <= D <= sqrt(s)/sqrt(1-g) + e, where D is the exact
-// distance of the FP64 rows, g = (Ea+2)*2^-23 bounds the accumulation and
-// e = 2^-21 * R (R = largest centred row norm) bounds the input rounding.
+// distance of the FP64 rows, g = (Ea+2)*2^-23 bounds the FP32 subtraction,
+// squares and accumulation ((Ea+3)u suffices), and e bounds the input
+// rounding: each centred coordinate A_i reaches FP32 as A_i(1+d), |d| <=
+// u(1+2^-29) (the FP64 centring adds 2^-53), so the difference vector moves
+// by at most u(1+2^-29)(|A|+|B|) <= 2u(1+2^-29) R with R >= every centred row
+// norm (the engine takes 1.01 times the norm of its bounding box's farthest
+// corner).  The engine sets e = 2^-22 R, twice that bound.
 // The k-th true distance is at most hi = sqrt(s_k)/sqrt(1-g) + e, so every
 // true neighbour has s <= T = ((hi + e) * sqrt(1+g))^2 (widened by 1e-14).
 // If the C-th kept value exceeds T, every entry at or under T is in the list;
