@@ -26,7 +26,6 @@ namespace fedm {
 // Device helpers (kernels_util.cu).
 void fill_f64(double* p, long long n, double v, cudaStream_t s);
 void fill_i32(int* p, long long n, int v, cudaStream_t s);
-void to_f32(const double* src, float* dst, long long n, cudaStream_t s);
 
 namespace {
 
@@ -276,7 +275,6 @@ struct GroupJob
   int Ea = 0;
   const double* dF = nullptr;   // library manifold on the device
   const double* dFp = nullptr;  // prediction manifold on the device
-  const float* dF32 = nullptr;
   const std::vector<double>* hF = nullptr;   // host copies (mixed-path margin)
   const std::vector<double>* hFp = nullptr;
   bool copredict = false;

@@ -1,4 +1,4 @@
-// Small device helpers: fills and precision conversion.
+// Small device helpers: fills, and the peak probes of the roofline.
 #include <cuda_runtime.h>
 
 namespace fedm {
@@ -15,12 +15,6 @@ __global__ void fill_i32_kernel(int* p, long long n, int v)
 {
   for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
     p[i] = v;
-}
-
-__global__ void to_f32_kernel(const double* src, float* dst, long long n)
-{
-  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
-    dst[i] = (float)src[i];
 }
 
 int grid_for(long long n)
@@ -43,12 +37,6 @@ void fill_i32(int* p, long long n, int v, cudaStream_t s)
 {
   if (n > 0)
     fill_i32_kernel<<<grid_for(n), 256, 0, s>>>(p, n, v);
-}
-
-void to_f32(const double* src, float* dst, long long n, cudaStream_t s)
-{
-  if (n > 0)
-    to_f32_kernel<<<grid_for(n), 256, 0, s>>>(src, dst, n);
 }
 
 } // namespace fedm

@@ -46,20 +46,8 @@ struct Rot
   double c, s;
 };
 
-// A matrix element e of one thread stored at base[e * stride] (shared
-// memory interleaved across threads); indexes like a double*.
-struct LaneMat
-{
-  double* base;
-  int stride;
-  __device__ __forceinline__ double& operator[](int e) const { return base[e * stride]; }
-};
-
-// The helpers below take the matrix as a double* or a LaneMat.
-
 // rows p, q <- J [row p; row q], J = [c s; -s c]
-template<class Mat>
-__device__ __forceinline__ void rot_rows(Mat A, int n, int p, int q, Rot j)
+__device__ __forceinline__ void rot_rows(double* A, int n, int p, int q, Rot j)
 {
   for (int i = 0; i < n; i++) {
     const double x = A[p * n + i], y = A[q * n + i];
@@ -69,8 +57,7 @@ __device__ __forceinline__ void rot_rows(Mat A, int n, int p, int q, Rot j)
 }
 
 // cols p, q <- [col p, col q] J^T  (Eigen's applyOnTheRight)
-template<class Mat>
-__device__ __forceinline__ void rot_cols(Mat A, int n, int p, int q, Rot j)
+__device__ __forceinline__ void rot_cols(double* A, int n, int p, int q, Rot j)
 {
   const double c = j.c, s = -j.s;
   for (int i = 0; i < n; i++) {
@@ -81,8 +68,7 @@ __device__ __forceinline__ void rot_cols(Mat A, int n, int p, int q, Rot j)
 }
 
 // ops counts the FP64 add/sub/mul/div/sqrt operations performed.
-template<class Mat>
-__device__ inline void jacobi_2x2(const Mat W, int n, int p, int q, Rot& jl, Rot& jr, int& ops)
+__device__ inline void jacobi_2x2(const double* W, int n, int p, int q, Rot& jl, Rot& jr, int& ops)
 {
   ops += 18;
   const double tiny = DBL_MIN;
@@ -238,50 +224,6 @@ __device__ inline void svd_solve(double* W, double* U, double* V, double* sv, do
 {
   int ops = 0;
   svd_solve(W, U, V, sv, tmp, b, x, n, ops);
-}
-
-// Square-root-free Cholesky (LDL^T) solve of the symmetric normal equations
-// in FP64.  Returns false when a pivot is not clearly positive relative to
-// the largest one (pivot ratio below `min_ratio`), i.e. when the system is too
-// ill-conditioned for the unpivoted factorisation to match the SVD solve; the
-// caller then uses svd_solve.  A (n x n) is overwritten by L and D.
-__device__ inline bool ldlt_solve(double* A, const double* b, double* x, int n, double min_ratio)
-{
-  double dmax = 0;
-  for (int j = 0; j < n; j++) {
-    double d = A[j * n + j];
-    for (int k = 0; k < j; k++)
-      d = sub(d, mul(mul(A[j * n + k], A[j * n + k]), A[k * n + k]));
-    if (!(d > 0))
-      return false;
-    dmax = fmax(dmax, d);
-    A[j * n + j] = d;
-    for (int i = j + 1; i < n; i++) {
-      double s = A[i * n + j];
-      for (int k = 0; k < j; k++)
-        s = sub(s, mul(mul(A[i * n + k], A[j * n + k]), A[k * n + k]));
-      A[i * n + j] = dvd(s, d);
-    }
-  }
-  for (int j = 0; j < n; j++)
-    if (A[j * n + j] < mul(min_ratio, dmax))
-      return false;
-  // L z = b, D y = z, L^T x = y
-  for (int i = 0; i < n; i++) {
-    double s = b[i];
-    for (int k = 0; k < i; k++)
-      s = sub(s, mul(A[i * n + k], x[k]));
-    x[i] = s;
-  }
-  for (int i = 0; i < n; i++)
-    x[i] = dvd(x[i], A[i * n + i]);
-  for (int i = n - 1; i >= 0; i--) {
-    double s = x[i];
-    for (int k = i + 1; k < n; k++)
-      s = sub(s, mul(A[k * n + i], x[k]));
-    x[i] = s;
-  }
-  return true;
 }
 
 } // namespace fedm
