@@ -174,7 +174,7 @@ def run_ours(a):
     def step():
         tot = dict(device_ms=0.0, knn_kernel_ms=0.0, knn_launches=0, predictions=0, distance_pairs=0,
                    h2d_bytes=0, d2h_bytes=0, fallback_points=0, kernel_launches=0, fp64_ops=0, host_ms=0.0,
-                   list_wait_ms=0.0, setup_ms=0.0, finish_ms=0.0, wall_ms=0.0)
+                   list_wait_ms=0.0, setup_ms=0.0, finish_ms=0.0, exact_points=0, wall_ms=0.0)
         base_keys = [k for k in tot if k != "wall_ms"]
         rhos = []
         for args, alg in zip(calls, ("simplex", "smap")):
@@ -296,6 +296,7 @@ def run_ours(a):
         },
         "fp64_plain": fp64,
         "fallback_points_per_step": int(s0["fallback_points"]),
+        "exact_points_per_step": int(s0["exact_points"]),
         "clocks": clocks,
         "cpu_baseline": cpu,
     }
@@ -406,7 +407,7 @@ def run_config(a):
         flush_l2(local)
     barrier(world)
     dev = wall = 0.0
-    preds = launches = fallback = 0
+    preds = launches = fallback = exact = 0
     with Clocks(local) as clk:
         for _ in range(a.steps):
             for tm, ws in step():
@@ -415,6 +416,7 @@ def run_config(a):
                 preds += tm["predictions"]
                 launches += tm["kernel_launches"]
                 fallback += tm.get("fallback_points", 0)
+                exact += tm.get("exact_points", 0)
             flush_l2(local)
     dev = allreduce_max(world, dev)
     wall = allreduce_max(world, wall)
@@ -429,7 +431,8 @@ def run_config(a):
         "dtype": "fp32+fp64", "data": "synthetic (seeded generators)", "config": cfg,
         "e2e": {"value": preds * world / wall, "unit": "predictions/s", "wall_ms_per_step": wall / a.steps * 1e3},
         "gpu_launches": launches, "predictions_per_step": preds // a.steps,
-        "fallback_points_per_step": fallback // a.steps, "roofline": None, "cpu_baseline": None,
+        "fallback_points_per_step": fallback // a.steps, "exact_points_per_step": exact // a.steps,
+        "roofline": None, "cpu_baseline": None,
         "clocks": clk.summary(),
     }
     print(json.dumps(out), flush=True)

@@ -555,10 +555,22 @@ void run_group(Context& ctx, const Options& o, const std::vector<Task>& tasks, c
     knn_ms += ms;
     ctx.timing.knn_launches++;
   };
-  auto exact_pass = [&](bool with_list_path, bool with_all) {
+  auto exact_pass = [&](bool with_list_path, bool with_all, const RefineRun* refine = nullptr) {
     ctx.timing.kernel_launches += 1;  // status fill
     if (with_list_path) {
-      timed([&] { launch_knn_exact(g, c, ctx.num_sms, s); });
+      if (refine) {
+        // uncertified mixed points: the rows under their bound, then the
+        // exact search for the points that bound does not settle
+        timed([&] {
+          launch_knn_refine(g, c, *refine, ctx.num_sms, s);
+          c.redo_only = 1;
+          launch_knn_exact(g, c, ctx.num_sms, s);
+          c.redo_only = 0;
+        });
+        ctx.timing.kernel_launches += 1;
+      } else {
+        timed([&] { launch_knn_exact(g, c, ctx.num_sms, s); });
+      }
       if (o.algorithm == 0)
         launch_simplex_nn(g, c, s);
       else
@@ -608,7 +620,8 @@ void run_group(Context& ctx, const Options& o, const std::vector<Task>& tasks, c
     m.items = (const int2*)ctx.buf("items", std::max<size_t>(items.size(), 1) * sizeof(int2));
     ctx.upload((void*)m.items, items.data(), items.size() * sizeof(int2));
     m.n_items = (int)items.size();
-    // queue head, fallback count, FP64 operation count (8 B), hand-off error
+    // queue head, fallback count, FP64 operation count (8 B), hand-off
+    // error, points left to the exact search by knn_refine_kernel
     m.counter = (int*)ctx.buf("mix_counter", 32);
     m.fb_count = m.counter + 1;
     m.fp64_ops = (unsigned long long*)(m.counter + 2);
@@ -617,6 +630,7 @@ void run_group(Context& ctx, const Options& o, const std::vector<Task>& tasks, c
     m.form = ctx.mixed_form;
     m.fb_cap = (int)std::min<long long>(std::max<long long>(P, 1), FB_CAP);
     m.fb_list = (long long*)ctx.buf("fb_list", (size_t)m.fb_cap * 8);
+    m.fb_thr = (double*)ctx.buf("fb_thr", (size_t)m.fb_cap * 8);
     m.gamma = (Ea + 2) * std::ldexp(1.0, -23);
     // input-rounding term of the certification (kernels_mixed.cu): twice the
     // proven 2u(1 + 2^-29) R
@@ -687,7 +701,8 @@ void run_group(Context& ctx, const Options& o, const std::vector<Task>& tasks, c
         c.p_end = std::min<long long>(nfb - b, chunk);
         c.plist = m.fb_list + b;
         fill_i32(c.status, c.p_end, PT_SKIP, s);
-        exact_pass(true, false);
+        const RefineRun rr{ F32, Fp32, S, m.fb_thr + b, m.counter + 5 };
+        exact_pass(true, false, &rr);
         if (job.detail) {
           std::vector<long long> keep(h_plist.begin() + b, h_plist.begin() + b + c.p_end);
           std::swap(keep, h_plist);
@@ -696,6 +711,10 @@ void run_group(Context& ctx, const Options& o, const std::vector<Task>& tasks, c
         }
       }
       c.plist = nullptr;
+      int nredo = 0;
+      ctx.download(&nredo, m.counter + 5, 4);
+      ck(cudaStreamSynchronize(s), "sync");
+      ctx.timing.exact_points += nredo;
     }
   }
 

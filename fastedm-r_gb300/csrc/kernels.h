@@ -79,7 +79,8 @@ enum : int
   PT_OK = 0,
   PT_EARLY_SUCCESS = 1,  // k == 0 or no valid neighbour: rc SUCCESS, no forecast
   PT_INSUFFICIENT = 2,   // the same without forceCompute: rc 503
-  PT_SKIP = 3            // point belongs to the other (all / finite k) path
+  PT_SKIP = 3,           // point belongs to the other (all / finite k) path
+  PT_REDO = 4            // knn_refine_kernel could not settle the point: knn_exact_kernel runs it
 };
 
 struct ChunkBuffers
@@ -94,6 +95,7 @@ struct ChunkBuffers
   long long scratch_doubles; // its size
   double* gram;              // all-mode S-map solver scratch, [chunk x n_thetas x slab]
   const long long* plist;    // optional: chunk point q is plist[q] (p_begin = 0, p_end = count)
+  int redo_only;             // knn_exact_kernel runs only the points whose status is PT_REDO
 };
 
 // Exact FP64 kernels (reference operation order, no FMA contraction).
@@ -133,6 +135,7 @@ struct MixedRun
   double err_abs;      // bound on | ||fl32 diff|| - ||exact diff|| | from input rounding
   double gamma;        // relative bound of the FP32 accumulation
   long long* fb_list;  // points to recompute exactly
+  double* fb_thr;      // per listed point: the certified bound on its neighbours' FP32 values (+inf: none)
   int* fb_count;
   int fb_cap;
   int* nn_idx;         // optional [total_points x kslots] final neighbour lists
@@ -146,6 +149,19 @@ struct MixedRun
 };
 
 void launch_knn_mixed(const GroupParams& g, const MixedRun& m, int C, int num_sms, cudaStream_t s);
+
+// Points the mixed kernels could not certify (ChunkBuffers::plist): the rows
+// whose FP32 value is within the certified bound, scored in FP64 and ranked
+// (knn_refine_kernel); a point with too many such rows is left PT_REDO.
+struct RefineRun
+{
+  const float* F32;   // centred float library manifold (MixedRun::F32)
+  const float* Fp32;  // centred float prediction manifold
+  int rs;             // row stride of both
+  const double* thr;  // [chunk] the bound of chunk point q
+  int* redo_count;    // points marked PT_REDO
+};
+void launch_knn_refine(const GroupParams& g, const ChunkBuffers& c, const RefineRun& r, int num_sms, cudaStream_t s);
 
 // The mixed path for E_a = 9..16 and up to 30 neighbours (knn_one_kernel:
 // one point per thread, 32 candidate slots, work items of 256 points, float

@@ -124,6 +124,8 @@ __global__ void knn_exact_kernel(GroupParams g, ChunkBuffers c, int warps_per_bl
   const long long nwarps = (long long)gridDim.x * warps_per_block;
   const long long chunk = c.p_end - c.p_begin;
   for (long long q = (long long)blockIdx.x * warps_per_block + wib; q < chunk; q += nwarps) {
+    if (c.redo_only && c.status[q] != PT_REDO)
+      continue;
     const long long p = point_of(c, q);
     const int ti = find_task(g, p);
     const DevTask T = g.tasks[ti];
@@ -243,6 +245,135 @@ __global__ void knn_exact_kernel(GroupParams g, ChunkBuffers c, int warps_per_bl
         note_k(g, T.task, p, keff);
       else if (g.kused)
         g.kused[p] = INT_MIN;
+    }
+    __syncwarp();
+  }
+}
+
+// ------------------------------------------------ uncertified mixed points
+// A point whose FP32 candidate list could not be certified still has a
+// certified bound thr: every row among its true neighbours has an FP32
+// squared distance, evaluated as the scan evaluates it (difference, square,
+// fused accumulation, in coordinate order), of at most thr.  One warp per
+// point re-scans the library in FP32, keeps the rows under thr in library
+// order, scores them with exact_distance and ranks the valid ones by
+// (distance, library index).  Rows outside the kept set have non-zero FP32
+// values and count as valid neighbours, the mixed kernels' rule.  The output
+// (status, count, lists, k statistics) is knn_exact_kernel's; a point with
+// more than REFINE_CAP kept rows, or whose kept rows cannot supply its k, is
+// marked PT_REDO and left to knn_exact_kernel.
+constexpr int REFINE_CAP = 1024;
+constexpr int REFINE_WARPS = 2;
+
+template<int EA>
+__global__ void __launch_bounds__(32 * REFINE_WARPS) knn_refine_kernel(GroupParams g, ChunkBuffers c, RefineRun r)
+{
+  __shared__ int s_idx[REFINE_WARPS][REFINE_CAP];
+  __shared__ double s_dist[REFINE_WARPS][REFINE_CAP];
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  int* sI = s_idx[wib];
+  double* sD = s_dist[wib];
+  const long long nwarps = (long long)gridDim.x * REFINE_WARPS;
+  const long long chunk = c.p_end - c.p_begin;
+  for (long long q = (long long)blockIdx.x * REFINE_WARPS + wib; q < chunk; q += nwarps) {
+    const long long p = point_of(c, q);
+    const DevTask T = g.tasks[find_task(g, p)];
+    const int prow = g.pred_rows[T.pred_off + (int)(p - T.point_base)];
+    const double thr = r.thr[q];
+    float np[EA];
+#pragma unroll
+    for (int j = 0; j < EA; j++)
+      np[j] = -r.Fp32[(size_t)prow * r.rs + j];
+    int count = 0;
+    bool over = false;
+    for (int b0 = 0; b0 < T.n_lib; b0 += 32) {
+      const int i = b0 + lane;
+      bool hit = false;
+      if (i < T.n_lib) {
+        const float* x = r.F32 + (size_t)g.lib_rows[T.lib_off + i] * r.rs;
+        float d = __fadd_rn(x[0], np[0]);
+        float sq = __fmul_rn(d, d);
+#pragma unroll
+        for (int j = 1; j < EA; j++) {
+          d = __fadd_rn(x[j], np[j]);
+          sq = __fmaf_rn(d, d, sq);
+        }
+        hit = (double)sq <= thr;
+      }
+      const unsigned hm = __ballot_sync(FULL, hit);
+      if (count + __popc(hm) > REFINE_CAP) {
+        over = true;  // the same decision in every lane
+        break;
+      }
+      if (hit)
+        sI[count + __popc(hm & ((1u << lane) - 1u))] = i;
+      count += __popc(hm);
+    }
+    __syncwarp();
+    int status = PT_REDO, keff = 0;
+    if (!over) {
+      const double* y = g.Fp + (size_t)prow * g.Ea;
+      const int ppanel = g.panel ? g.panel[prow] : 0;
+      const double ptime = g.point_time[prow];
+      int nvalid = 0;
+      for (int e = lane; e < count; e += 32) {
+        double d = 0;
+        const bool valid = exact_distance(g, g.lib_rows[T.lib_off + sI[e]], prow, y, ppanel, ptime, d);
+        sD[e] = valid ? d : -1.0;
+        nvalid += valid ? 1 : 0;
+      }
+      nvalid = __reduce_add_sync(FULL, nvalid);
+      __syncwarp();
+      const int numValid = T.n_lib - (count - nvalid);
+      // src/edm.cpp:595-617, as in knn_exact_kernel
+      status = PT_OK;
+      keff = T.k_req < 0 ? numValid : T.k_req;
+      if (T.k_req > numValid) {
+        if (g.force_compute)
+          keff = numValid;
+        else
+          status = PT_INSUFFICIENT;
+      }
+      if (status == PT_OK && (keff == 0 || numValid == 0))
+        status = g.force_compute ? PT_EARLY_SUCCESS : PT_INSUFFICIENT;
+      if (status == PT_OK && nvalid < keff)
+        status = PT_REDO;
+      if (status == PT_OK) {
+        // rank among the valid kept rows: (distance, index), or library
+        // order when every valid neighbour is used (src/edm.cpp:615-616)
+        const bool lib_order = keff == numValid;
+        int* oi = c.nn_idx + q * c.kcap;
+        double* od = c.nn_dist + q * c.kcap;
+        for (int e = lane; e < count; e += 32) {
+          const double de = sD[e];
+          if (de < 0)
+            continue;
+          const int ie = sI[e];
+          int rank = 0;
+          for (int f = 0; f < count; f++) {
+            const double df = sD[f];
+            if (df < 0)
+              continue;
+            rank += lib_order ? (sI[f] < ie) : (df < de || (df == de && sI[f] < ie));
+          }
+          if (rank < keff) {
+            oi[rank] = ie;
+            od[rank] = de;
+          }
+        }
+      }
+    }
+    if (lane == 0) {
+      c.status[q] = status;
+      if (status == PT_REDO)
+        atomicAdd(r.redo_count, 1);
+      else {
+        c.nn_count[q] = keff;
+        if (status == PT_OK)
+          note_k(g, T.task, p, keff);
+        else if (g.kused)
+          g.kused[p] = INT_MIN;
+      }
     }
     __syncwarp();
   }
@@ -683,6 +814,37 @@ void launch_knn_exact(const GroupParams& g, const ChunkBuffers& c, int num_sms, 
   if (blocks < 1)
     blocks = 1;
   knn_exact_kernel<<<(int)blocks, 32 * w, smem, s>>>(g, c, w, per_warp);
+}
+
+void launch_knn_refine(const GroupParams& g, const ChunkBuffers& c, const RefineRun& r, int num_sms, cudaStream_t s)
+{
+  const long long chunk = c.p_end - c.p_begin;
+  if (chunk <= 0)
+    return;
+  long long blocks = (chunk + REFINE_WARPS - 1) / REFINE_WARPS;
+  const long long cap = (long long)num_sms * 16;
+  if (blocks > cap)
+    blocks = cap;
+  const int b = (int)blocks, t = 32 * REFINE_WARPS;
+  switch (g.Ea) {
+    case 1: knn_refine_kernel<1><<<b, t, 0, s>>>(g, c, r); break;
+    case 2: knn_refine_kernel<2><<<b, t, 0, s>>>(g, c, r); break;
+    case 3: knn_refine_kernel<3><<<b, t, 0, s>>>(g, c, r); break;
+    case 4: knn_refine_kernel<4><<<b, t, 0, s>>>(g, c, r); break;
+    case 5: knn_refine_kernel<5><<<b, t, 0, s>>>(g, c, r); break;
+    case 6: knn_refine_kernel<6><<<b, t, 0, s>>>(g, c, r); break;
+    case 7: knn_refine_kernel<7><<<b, t, 0, s>>>(g, c, r); break;
+    case 8: knn_refine_kernel<8><<<b, t, 0, s>>>(g, c, r); break;
+    case 9: knn_refine_kernel<9><<<b, t, 0, s>>>(g, c, r); break;
+    case 10: knn_refine_kernel<10><<<b, t, 0, s>>>(g, c, r); break;
+    case 11: knn_refine_kernel<11><<<b, t, 0, s>>>(g, c, r); break;
+    case 12: knn_refine_kernel<12><<<b, t, 0, s>>>(g, c, r); break;
+    case 13: knn_refine_kernel<13><<<b, t, 0, s>>>(g, c, r); break;
+    case 14: knn_refine_kernel<14><<<b, t, 0, s>>>(g, c, r); break;
+    case 15: knn_refine_kernel<15><<<b, t, 0, s>>>(g, c, r); break;
+    case 16: knn_refine_kernel<16><<<b, t, 0, s>>>(g, c, r); break;
+    default: break;
+  }
 }
 
 void launch_simplex_nn(const GroupParams& g, const ChunkBuffers& c, cudaStream_t s)

@@ -107,8 +107,13 @@ __device__ __forceinline__ bool prepare_point(const GroupParams& g, const MixedR
   for (int j = 0; j < C; j++)
     lc += D[j] < INFINITY ? 1 : 0;
   bool fallback = z > ZCAP;
+  // With k kept non-zero values the bound exists even when the list has to
+  // fall back (too many zeros, or the C-th value inside it): every row with
+  // a non-zero FP32 value is a valid FP64 neighbour, so the k-th true
+  // distance is at most the k-th kept row's.  With fewer, the library holds
+  // fewer than k non-zero rows and the bound is +inf.
   double thr = INFINITY;
-  if (!fallback && lc >= k) {
+  if (lc >= k) {
     const double sq = sqrt((double)pick(D, k - 1));
     const double hi = sq / sqrt(1.0 - m.gamma) + m.err_abs;
     const double td = (hi * (1.0 + 1e-14) + m.err_abs) * sqrt(1.0 + m.gamma);
@@ -117,9 +122,12 @@ __device__ __forceinline__ bool prepare_point(const GroupParams& g, const MixedR
       fallback = true;
   }
   if (fallback) {
+    // knn_refine_kernel re-scans the library for the rows under thr
     const int slot = atomicAdd(m.fb_count, 1);
-    if (slot < m.fb_cap)
+    if (slot < m.fb_cap) {
       m.fb_list[slot] = p;
+      m.fb_thr[slot] = thr;
+    }
     return false;
   }
   double y[EA];

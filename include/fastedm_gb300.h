@@ -182,7 +182,9 @@ typedef struct fedm_timing {
   long long predictions;     /* (prediction point, theta) forecasts made    */
   long long h2d_bytes;
   long long d2h_bytes;
-  int fallback_points;       /* mixed path: points re-run in exact FP64      */
+  int fallback_points;       /* mixed path: points whose candidate list could
+                                not be certified (re-run by the refine and,
+                                if needed, the exact FP64 search)            */
   int kernel_launches;       /* kernels this library launched                */
   long long fp64_ops;        /* mixed path: FP64 add/sub/mul/div/sqrt of the
                                 re-rank and forecast stage (exp = 32)        */
@@ -192,6 +194,8 @@ typedef struct fedm_timing {
                                 first kernel (row pools, uploads)            */
   double finish_ms;          /* host time after each batch's statistics
                                 (downloads, per-task results)                */
+  int exact_points;          /* of fallback_points, those the bounded FP32
+                                re-scan could not settle (full FP64 search)  */
 } fedm_timing;
 
 int fedm_last_timing(const fedm_ctx* ctx, fedm_timing* out);

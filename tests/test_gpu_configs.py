@@ -164,14 +164,19 @@ def test_wide_embedding_task_bit_exact(ctx, E, algorithm):
     w = workloads.panel_config(n_panels=24, lo=80, hi=400)
     n = len(w["t"])
     rng = np.random.default_rng(E)
-    lib = rng.uniform(size=n) < 0.5
-    pred = ~lib
     kw = dict(panel=w["panel"], E=E, dt=True, algorithm=algorithm, theta=[0.5, 2.0])
     a = fedm.normalise(w["t"], w["x"], **kw)
+    # rows with a complete manifold only, as run_command's usable mask: a
+    # missing coordinate in the library sends the task to the exact kernels
+    usable = fedm.host_usable(a, E)
+    lib = (rng.uniform(size=n) < 0.5) & usable
+    pred = ~lib & usable
     Ea = fedm.host_manifold(a, E).shape[1]
     assert Ea == 2 * E
     k = Ea + 1 + (algorithm == "smap")
     g = ctx.run_task(a, lib, pred, E, k)
+    if ctx.precision == fedm.PRECISION_MIXED:
+        assert ctx.timing()["fp64_ops"] > 0  # the mixed kernels ran
     o = edm_oracle.oracle_task(edm_oracle.normalise(w["t"], w["x"], **kw), lib, pred, E, k)
     assert g["n_pred"] > 1000
     assert np.array_equal(g["nn_idx"], o["nn_idx"])
@@ -216,14 +221,60 @@ def test_ties_and_duplicate_rows_bit_exact(ctx, levels, algorithm):
     oracle's bits."""
     t, x, _ = workloads.coupled_logistic(3000, seed=11)
     xq = np.round(x * levels) / levels
-    lib = np.zeros(3000, bool)
-    lib[:1800] = True
     kw = dict(E=3, theta=[0.0, 1.5], algorithm=algorithm)
     a = fedm.normalise(t, xq, **kw)
+    usable = fedm.host_usable(a, 3)
+    lib = np.zeros(3000, bool)
+    lib[:1800] = True
+    lib, pred = lib & usable, ~lib & usable
     k = 4 + (algorithm == "smap")
-    g = ctx.run_task(a, lib, ~lib, 3, k)
-    o = edm_oracle.oracle_task(edm_oracle.normalise(t, xq, **kw), lib, ~lib, 3, k)
+    g = ctx.run_task(a, lib, pred, 3, k)
+    o = edm_oracle.oracle_task(edm_oracle.normalise(t, xq, **kw), lib, pred, 3, k)
     assert np.array_equal(g["nn_idx"], o["nn_idx"])
     assert np.array_equal(g["nn_dist"].view(np.int64), o["nn_dist"].view(np.int64))
     assert np.array_equal(g["predictions"], o["predictions"], equal_nan=True)
     assert np.array_equal(g["kused"], o["kused"])
+    if ctx.precision == fedm.PRECISION_MIXED:
+        # uncertified points (a few hundred rows under their bound at most)
+        # are all settled by the bounded re-scan
+        tm = ctx.timing()
+        assert tm["fallback_points"] > 0 and tm["exact_points"] == 0
+
+
+@pytest.mark.parametrize("case", ["over_capacity", "wide_dt"])
+@pytest.mark.parametrize("algorithm", ["simplex", "smap"])
+def test_uncertified_points_bit_exact(ctx, case, algorithm):
+    """Points whose FP32 candidate list cannot be certified are re-scanned
+    for the rows under their certified bound, which are scored in FP64 and
+    ranked (knn_refine_kernel); past 1024 such rows the point goes to the
+    full exact search.  'over_capacity': a two-level series at E = 2, where
+    every point has well over a thousand rows at distance zero or one level
+    away, so every uncertified point takes the exact search.  'wide_dt': a
+    quantised panel series with dt (E_a = 10, the wide kernel), where the
+    re-scan settles every uncertified point.  Both give the oracle's bits."""
+    if case == "over_capacity":
+        t, x, _ = workloads.coupled_logistic(6000, seed=11)
+        x = np.round(x * 2) / 2
+        lib = np.zeros(6000, bool)
+        lib[:4000] = True
+        E, kw = 2, dict(E=2, theta=[0.0, 1.5], algorithm=algorithm)
+        k = E + 1 + (algorithm == "smap")
+    else:
+        w = workloads.panel_config(n_panels=24, lo=80, hi=400)
+        t, x = w["t"], np.round(w["x"] * 6) / 6
+        lib = np.random.default_rng(5).uniform(size=len(t)) < 0.5
+        E, kw = 5, dict(panel=w["panel"], E=5, dt=True, theta=[0.5, 2.0], algorithm=algorithm)
+        k = 2 * E + 1 + (algorithm == "smap")
+    a = fedm.normalise(t, x, **kw)
+    usable = fedm.host_usable(a, E)
+    lib, pred = lib & usable, ~lib & usable
+    g = ctx.run_task(a, lib, pred, E, k)
+    o = edm_oracle.oracle_task(edm_oracle.normalise(t, x, **kw), lib, pred, E, k)
+    assert np.array_equal(g["nn_idx"], o["nn_idx"])
+    assert np.array_equal(g["nn_dist"].view(np.int64), o["nn_dist"].view(np.int64))
+    assert np.array_equal(g["predictions"], o["predictions"], equal_nan=True)
+    assert np.array_equal(g["kused"], o["kused"])
+    if ctx.precision == fedm.PRECISION_MIXED:
+        tm = ctx.timing()
+        assert tm["fallback_points"] > 500
+        assert tm["exact_points"] == (tm["fallback_points"] if case == "over_capacity" else 0)
