@@ -18,9 +18,16 @@
 //                 + g_{j+1} S_j - c_{j+1} T_j
 // (from dyhat = dv.c + g.(db - dA c), A symmetric).  Each point writes r,
 // and 2 r dyhat/d(.) ; the host sums them in a fixed order.
+//
+// Only the distances follow the reference's rounding: the sums over the
+// library are lane-strided and warp-reduced, so the forecast agrees with the
+// reference's k = all S-map to reduction-order rounding, not bit for bit.
+// The passes therefore use what the FP64 pipe does cheaply: one reciprocal
+// of d per row instead of a division per lag, a2 = exp(-2 theta d / mu) in
+// one call, and fused multiply-adds for the normal equations and the
+// adjoint sums.  The weights are recomputed in pass 3, not stored.
 #include <cfloat>
 
-#include "exp_rn.cuh"
 #include "kernels.h"
 #include "smap_solve.cuh"
 
@@ -72,16 +79,18 @@ __global__ void __launch_bounds__(128) smap_grad_kernel(AdjointParams a)
     }
     if (s != 0) {
       const double d = __dsqrt_rn(s);
+      const double inv = __drcp_rn(d);
       sd += d;
       cnt++;
 #pragma unroll
       for (int j = 0; j < EA; j++)
-        dmu[j] += diff[j] * (m[j] - y[j]) / d;
+        dmu[j] = fma(diff[j] * (m[j] - y[j]), inv, dmu[j]);
     }
   }
   const double total = wsum(sd);
   const double nv = (double)__reduce_add_sync(FULL, cnt);
   const double mu = total / nv;
+  const double c2 = -2.0 * a.theta / mu;  // a^2 = exp(c2 d)
 #pragma unroll
   for (int j = 0; j < EA; j++)
     dmu[j] = wsum(dmu[j]) / nv;
@@ -105,16 +114,18 @@ __global__ void __launch_bounds__(128) smap_grad_kernel(AdjointParams a)
     }
     if (s == 0)
       continue;
-    const double aw = exp_rn(mul(-a.theta, dvd(__dsqrt_rn(s), mu)));
-    const double a2 = aw * aw;
+    const double a2 = exp(c2 * __dsqrt_rn(s));
     const double t = a.lib_t[i];
     int e = 0;
 #pragma unroll
     for (int r = 0; r < n; r++) {
+      const double au = a2 * u[r];
 #pragma unroll
-      for (int c = r; c < n; c++)
-        A[e++] += a2 * u[r] * u[c];
-      b[r] += a2 * u[r] * t;
+      for (int c = r; c < n; c++) {
+        A[e] = fma(au, u[c], A[e]);
+        e++;
+      }
+      b[r] = fma(au, t, b[r]);
     }
   }
 #pragma unroll
@@ -179,22 +190,23 @@ __global__ void __launch_bounds__(128) smap_grad_kernel(AdjointParams a)
     if (s == 0)
       continue;
     const double d = __dsqrt_rn(s);
-    const double aw = exp_rn(mul(-a.theta, dvd(d, mu)));
-    const double a2 = aw * aw;
+    const double a2 = exp(c2 * d);
     double su = 0, uc = 0;
 #pragma unroll
     for (int k = 0; k < n; k++) {
-      su += gv[k] * u[k];
-      uc += u[k] * c[k];
+      su = fma(gv[k], u[k], su);
+      uc = fma(u[k], c[k], uc);
     }
     const double ei = a.lib_t[i] - uc;
-    const double ase = a2 * su * ei;
-    Q += ase * d;
+    const double ae = a2 * ei, as = a2 * su;
+    const double ase = as * ei;
+    Q = fma(ase, d, Q);
+    const double ased = ase * __drcp_rn(d);
 #pragma unroll
     for (int j = 0; j < EA; j++) {
-      R[j] += ase * (diff[j] * (m[j] - y[j]) / d);
-      S[j] += a2 * ei * m[j];
-      Tt[j] += a2 * su * m[j];
+      R[j] = fma(ased, diff[j] * (m[j] - y[j]), R[j]);
+      S[j] = fma(ae, m[j], S[j]);
+      Tt[j] = fma(as, m[j], Tt[j]);
     }
   }
   Q = wsum(Q);

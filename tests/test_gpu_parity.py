@@ -103,10 +103,15 @@ def test_simplex_config_neighbours_bit_exact(ctx):
         _task_pair(ctx, a, w["library_rows"], w["prediction_rows"], E, E + 1)
 
 
+@pytest.mark.parametrize("masks", ["raw", "usable"])
 @pytest.mark.parametrize("algorithm", ["simplex", "smap"])
 @pytest.mark.parametrize("k", [0, 1, 3, 7, 40, -1, 500])
-def test_random_task_edges(ctx, algorithm, k):
-    """Ties (duplicated values), self matches, k beyond the library, k = all."""
+def test_random_task_edges(ctx, algorithm, k, masks):
+    """Ties (duplicated values), self matches, k beyond the library, k = all.
+    'raw' masks include the first rows, whose lags are missing (the exact
+    kernels serve any task whose library holds such a row); 'usable' masks
+    keep complete rows only, so the mixed context runs 1 <= k <= 16 through
+    the FP32 scan, its certification and the bounded re-scan."""
     rng = np.random.default_rng(11)
     n = 300
     x = np.round(rng.normal(size=n), 1)  # many exact ties
@@ -115,7 +120,12 @@ def test_random_task_edges(ctx, algorithm, k):
     a = edm_oracle.normalise(t, x, E=3, theta=[0.0, 1.0, 3.0], algorithm=algorithm)
     lib = rng.uniform(size=n) < 0.5
     pred = np.ones(n, bool)
+    if masks == "usable":
+        usable = fedm.host_usable(a, 3)
+        lib, pred = lib & usable, pred & usable
     _task_pair(ctx, a, lib, pred, 3, k)
+    if masks == "usable" and ctx.precision == fedm.PRECISION_MIXED and 1 <= k <= 16:
+        assert ctx.timing()["fp64_ops"] > 0  # the mixed kernels ran
 
 
 def test_empty_library(ctx):
