@@ -42,6 +42,15 @@ METRIC = "CCM S-map predictions/s: batched FP32+FP64-fix vs plain FP64 GPU @|Î”Ï
 SMAP_DRAM_BYTES_PER_POINT = 6428.5
 
 
+def form_kernel(form, alg):
+    """The kernel a mixed run used (fedm_timing.mixed_form), for the E = 4, k <= 6 benchmark."""
+    return {0: f"knn_mixed_kernel<E=4,C=8,{alg},2 points per thread>",
+            1: f"knn_one_kernel<E=4,C=8,{alg},6 CTAs/SM>",
+            2: "knn_smap_ws_kernel<E=4,C=8,4 solver warps>",
+            3: "knn_smap_ws_kernel<E=4,C=8,8 solver warps>",
+            4: f"knn_one_kernel wide form ({alg})"}.get(int(form), "none")
+
+
 def hbm_peak():
     try:
         return float(json.loads((ROOT / "MEASURED_PEAKS.json").read_text())["hbm_gbs"]), "MEASURED_PEAKS.json"
@@ -174,7 +183,7 @@ def run_ours(a):
     def step():
         tot = dict(device_ms=0.0, knn_kernel_ms=0.0, knn_launches=0, predictions=0, distance_pairs=0,
                    h2d_bytes=0, d2h_bytes=0, fallback_points=0, kernel_launches=0, fp64_ops=0, host_ms=0.0,
-                   list_wait_ms=0.0, setup_ms=0.0, finish_ms=0.0, exact_points=0, wall_ms=0.0)
+                   list_wait_ms=0.0, setup_ms=0.0, finish_ms=0.0, exact_points=0, autotune_probes=0, wall_ms=0.0)
         base_keys = [k for k in tot if k != "wall_ms"]
         rhos = []
         for args, alg in zip(calls, ("simplex", "smap")):
@@ -186,13 +195,14 @@ def run_ours(a):
             tm = ctx.timing()
             for k in base_keys:
                 tot[k] += tm[k]
-            for k in ("knn_kernel_ms", "knn_launches", "fp64_ops", "distance_pairs", "predictions"):
+            for k in ("knn_kernel_ms", "knn_launches", "fp64_ops", "distance_pairs", "predictions", "mixed_form"):
                 tot[f"{alg}_{k}"] = tm[k]
             rhos.append(r["stats"]["rho"])
         return tot, rhos
 
+    warm_probes = 0
     for _ in range(max(3, a.warmup)):
-        step()
+        warm_probes += step()[0]["autotune_probes"]
         flush_l2(local)
     per_step = []
     barrier(world)
@@ -275,7 +285,7 @@ def run_ours(a):
                 "host_ms_per_step": {k: mean_of(k) for k in ("host_ms", "list_wait_ms", "setup_ms", "finish_ms")}},
         "gpu_launches": int(sum(s["kernel_launches"] for s in per_step)),
         "roofline": {
-            "kernel": "knn_one_kernel<E=4,C=8,smap,6 CTAs/SM> (FP32 scan + FP64 re-rank + JacobiSVD solve)",
+            "kernel": form_kernel(s0["smap_mixed_form"], "smap") + " (FP32 scan + FP64 re-rank + JacobiSVD solve)",
             "bound": "fp64_simt", "achieved": sm_fp64, "peak": fp64_unfused_peak, "unit": "TFLOP/s",
             "frac": sm_fp64 / fp64_unfused_peak,
             "peak_source": "measured FP64 multiply+add rate without fusion on this GPU (fedm_measure_peak kind 3; "
@@ -287,7 +297,7 @@ def run_ours(a):
             "traffic": traffic,
             "fp32_scan": {"achieved": sm_fp32, "peak": fp32_peak, "frac": sm_fp32 / fp32_peak,
                           "flops": "3*E per (prediction, library) pair"},
-            "simplex_kernel": {"kernel": "knn_one_kernel<E=4,C=8,simplex,6 CTAs/SM>", "bound": "fp32_simt",
+            "simplex_kernel": {"kernel": form_kernel(s0["simplex_mixed_form"], "simplex"), "bound": "fp32_simt",
                                "achieved": sx_fp32, "peak": fp32_peak, "frac": sx_fp32 / fp32_peak,
                                "kernel_ms_per_step": sx_ms,
                                "peak_source": "measured FFMA rate of this GPU (fedm_measure_peak kind 0)"},
@@ -297,6 +307,9 @@ def run_ours(a):
         "fp64_plain": fp64,
         "fallback_points_per_step": int(s0["fallback_points"]),
         "exact_points_per_step": int(s0["exact_points"]),
+        "autotune": {"smap_form": form_kernel(s0["smap_mixed_form"], "smap"),
+                     "simplex_form": form_kernel(s0["simplex_mixed_form"], "simplex"),
+                     "probes_during_warmup": warm_probes, "probes_during_timed_steps": int(s0["autotune_probes"])},
         "clocks": clocks,
         "cpu_baseline": cpu,
     }

@@ -54,9 +54,21 @@ Context::Context(int dev) : device(dev)
       { "one6", MIXED_ONE6 }, { "fused2", MIXED_FUSED2 }, { "ws4", MIXED_WS4 }, { "ws8", MIXED_WS8 }
     };
     for (const auto& f : forms)
-      if (std::strcmp(v, f.first) == 0)
+      if (std::strcmp(v, f.first) == 0) {
         mixed_form = f.second;
+        autotune = false;  // a named form is used as given
+      }
   }
+  if (const char* v = std::getenv("FEDM_AUTOTUNE"))
+    if (std::strcmp(v, "0") == 0)
+      autotune = false;
+  reset_timing();
+}
+
+void Context::reset_timing()
+{
+  timing = fedm_timing{};
+  timing.mixed_form = -1;
 }
 
 Context::~Context()
@@ -592,9 +604,11 @@ void run_group(Context& ctx, const Options& o, const std::vector<Task>& tasks, c
     const int C = wide ? 32 : (kmix <= 6 ? 8 : 16);
     // one point per thread for k <= 6: the default form, and the simplex's
     // when the S-map uses the warp-specialised kernel
-    const bool ws = o.algorithm == 1 && (ctx.mixed_form == MIXED_WS4 || ctx.mixed_form == MIXED_WS8);
-    const bool one = !wide && C == 8 && ctx.mixed_form != MIXED_FUSED2 && !ws;
-    const int item_points = (wide || one) ? WIDE_POINTS : MIX_POINTS;
+    auto is_one = [&](int form) {
+      const bool ws = o.algorithm == 1 && (form == MIXED_WS4 || form == MIXED_WS8);
+      return !wide && C == 8 && form != MIXED_FUSED2 && !ws;
+    };
+    auto points_per_item = [&](int form) { return (wide || is_one(form)) ? WIDE_POINTS : MIX_POINTS; };
     const long long nrows = (long long)rows.n_rows;
     double* d_center = (double*)ctx.buf("center", Ea * 8);
     ctx.upload(d_center, center.data(), Ea * 8);
@@ -610,16 +624,30 @@ void run_group(Context& ctx, const Options& o, const std::vector<Task>& tasks, c
       if (dt[j].mixed)
         order.push_back(j);
     std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return dt[a].n_lib > dt[b].n_lib; });
-    std::vector<int2> items;
-    for (int j : order)
-      for (int b = 0; b < dt[j].n_pred; b += item_points)
-        items.push_back(make_int2(j, b));
+    // work items of the tasks in LPT order, up to the task that takes the
+    // count of points past max_points
+    auto items_of = [&](int per_item, long long max_points) {
+      std::vector<int2> it;
+      long long covered = 0;
+      for (int j : order) {
+        if (covered >= max_points)
+          break;
+        for (int b = 0; b < dt[j].n_pred; b += per_item)
+          it.push_back(make_int2(j, b));
+        covered += dt[j].n_pred;
+      }
+      return it;
+    };
+    long long mixed_points = 0;
+    size_t max_items = 1;
+    for (int j : order) {
+      mixed_points += dt[j].n_pred;
+      max_items += (dt[j].n_pred + WIDE_POINTS - 1) / WIDE_POINTS;
+    }
     MixedRun m{};
     m.F32 = F32;
     m.Fp32 = Fp32;
-    m.items = (const int2*)ctx.buf("items", std::max<size_t>(items.size(), 1) * sizeof(int2));
-    ctx.upload((void*)m.items, items.data(), items.size() * sizeof(int2));
-    m.n_items = (int)items.size();
+    m.items = (const int2*)ctx.buf("items", max_items * sizeof(int2));  // 256-point items: the longest list
     // queue head, fallback count, FP64 operation count (8 B), hand-off
     // error, points left to the exact search by knn_refine_kernel
     m.counter = (int*)ctx.buf("mix_counter", 32);
@@ -641,14 +669,94 @@ void run_group(Context& ctx, const Options& o, const std::vector<Task>& tasks, c
     }
     ctx.timing.kernel_launches += (job.dFp != job.dF ? 2 : 1) + 1;  // centring, counter fill
     m.kslots = C;
-    m.item_begin = 0;
-    m.item_end = m.n_items;
+    auto launch_form = [&](int form) {
+      m.form = form;
+      if (wide)
+        launch_knn_wide(g, m, ctx.num_sms, s);
+      else if (is_one(form))
+        launch_mixed_one(g, m, ctx.num_sms, s);
+      else
+        launch_knn_mixed(g, m, C, ctx.num_sms, s);
+    };
+    auto run_items = [&](const std::vector<int2>& it) {
+      ctx.upload((void*)m.items, it.data(), it.size() * sizeof(int2));
+      m.n_items = (int)it.size();
+      m.item_begin = 0;
+      m.item_end = m.n_items;
+    };
+    int form = ctx.mixed_form;
+    if (!wide && C == 8 && ctx.autotune) {
+      // Autotuner: every form gives the same bits, so the first batch of
+      // each (algorithm, E_a, k) with enough points times each candidate
+      // form on the same leading tasks (about two waves of the default
+      // form) and the context keeps the fastest.  Each candidate first runs
+      // once on one work item, untimed, so that module loading and the
+      // clock ramp of a first launch fall outside the timing; then two
+      // rounds in alternating order, the minimum per candidate.  The probes
+      // write the values the real run writes again; the counters are reset
+      // after.
+      const std::array<int, 3> key{ o.algorithm, Ea, kmix };
+      auto hit = ctx.tuned_forms.find(key);
+      const long long probe_points = 2LL * ctx.num_sms * 6 * WIDE_POINTS;
+      if (hit != ctx.tuned_forms.end()) {
+        form = hit->second;
+      } else if (mixed_points >= probe_points) {
+        std::vector<int> cands{ MIXED_ONE6, MIXED_FUSED2 };
+        if (o.algorithm == 1)
+          cands.push_back(MIXED_WS8);
+        std::vector<float> best(cands.size(), INFINITY);
+        for (int f : cands) {
+          fill_i32(m.counter, 8, 0, s);
+          std::vector<int2> one_item = items_of(points_per_item(f), 1);
+          one_item.resize(1);
+          run_items(one_item);
+          launch_form(f);
+          ctx.timing.kernel_launches += 2;
+        }
+        cudaEvent_t p0, p1;
+        ck(cudaEventCreate(&p0), "event");
+        ck(cudaEventCreate(&p1), "event");
+        for (int round = 0; round < 2; round++)
+          for (size_t c = 0; c < cands.size(); c++) {
+            const size_t ci = round == 0 ? c : cands.size() - 1 - c;
+            const int f = cands[ci];
+            fill_i32(m.counter, 8, 0, s);
+            run_items(items_of(points_per_item(f), probe_points));
+            ck(cudaEventRecord(p0, s), "event");
+            launch_form(f);
+            ck(cudaEventRecord(p1, s), "event");
+            ctx.check("autotune probe");
+            ck(cudaEventSynchronize(p1), "sync");
+            int herr = 0;
+            ctx.download(&herr, m.error, 4);
+            ck(cudaStreamSynchronize(s), "sync");
+            float ms = 0;
+            cudaEventElapsedTime(&ms, p0, p1);
+            if (!herr)
+              best[ci] = std::min(best[ci], ms);
+            ctx.timing.autotune_probes++;
+            ctx.timing.kernel_launches += 2;
+          }
+        cudaEventDestroy(p0);
+        cudaEventDestroy(p1);
+        size_t bi = 0;  // ties keep the earlier candidate
+        for (size_t c = 1; c < cands.size(); c++)
+          if (best[c] < best[bi])
+            bi = c;
+        if (best[bi] < INFINITY)
+          form = cands[bi];
+        fill_i32(m.counter, 8, 0, s);
+        ctx.tuned_forms[key] = form;
+      }
+    }
     if (wide)
-      timed([&] { launch_knn_wide(g, m, ctx.num_sms, s); });
-    else if (one)
-      timed([&] { launch_mixed_one(g, m, ctx.num_sms, s); });
+      ctx.timing.mixed_form = MIXED_WIDE;
+    else if (is_one(form))
+      ctx.timing.mixed_form = MIXED_ONE6;
     else
-      timed([&] { launch_knn_mixed(g, m, C, ctx.num_sms, s); });
+      ctx.timing.mixed_form = (o.algorithm == 1 && (form == MIXED_WS4 || form == MIXED_WS8)) ? form : MIXED_FUSED2;
+    run_items(items_of(points_per_item(form), LLONG_MAX));
+    timed([&] { launch_form(form); });
     int nfb = 0, herr = 0;
     unsigned long long nops = 0;
     ctx.download(&nfb, m.fb_count, 4);
@@ -873,7 +981,7 @@ CommandResult run_command(Context& ctx, const fedm_args& a)
 {
   CommandResult R;
   const double t0 = now_ms();
-  ctx.timing = fedm_timing{};
+  ctx.reset_timing();
   ck(cudaSetDevice(ctx.device), "cudaSetDevice");
   Prepared P;
   prepare(a, P);
@@ -1057,7 +1165,7 @@ int smap_grad(Context& ctx, const double* lib, const double* lib_t, int n_lib, c
     throw Error{ RC_NOT_IMPLEMENTED, "differentiable S-map supports 1 <= E_actual <= 8" };
   if (n_lib < 1 || n_pred < 1)
     throw Error{ RC_UNKNOWN_ERROR, "empty library or prediction set" };
-  ctx.timing = fedm_timing{};
+  ctx.reset_timing();
   const double t0 = now_ms();
   ck(cudaSetDevice(ctx.device), "cudaSetDevice");
   cudaStream_t s = ctx.stream;
@@ -1201,7 +1309,7 @@ int host_plan(const fedm_args& a, int max_tasks, int* task_E, int* task_k, int* 
 int run_task(Context& ctx, const fedm_args& a, fedm_task_io& io)
 {
   const double t0 = now_ms();
-  ctx.timing = fedm_timing{};
+  ctx.reset_timing();
   ck(cudaSetDevice(ctx.device), "cudaSetDevice");
   Prepared P;
   prepare(a, P);

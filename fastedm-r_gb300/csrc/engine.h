@@ -2,6 +2,7 @@
 // pipeline and the single-task seam.
 #pragma once
 
+#include <array>
 #include <map>
 #include <string>
 #include <vector>
@@ -29,11 +30,17 @@ public:
   // variable FEDM_MIXED_KERNEL (one6, fused2, ws4, ws8) overrides it when
   // the context is created.
   int mixed_form = MIXED_ONE6;
+  // With autotune on (the default; FEDM_AUTOTUNE=0 or a named form turns it
+  // off) the form for E_a <= 8, k <= 6 is chosen per (algorithm, E_a, k) by
+  // timing the candidates on the first batch large enough to measure.
+  bool autotune = true;
+  std::map<std::array<int, 3>, int> tuned_forms;
   std::string last_error;
   fedm_timing timing{};
 
   explicit Context(int dev);
   ~Context();
+  void reset_timing();
   // Grow-only named device buffers (the context's memory pool).
   void* buf(const std::string& name, size_t bytes);
   void upload(void* dst, const void* src, size_t bytes);

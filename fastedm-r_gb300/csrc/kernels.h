@@ -116,7 +116,8 @@ enum MixedForm
   MIXED_FUSED2 = 0,  // knn_mixed_kernel: two points per thread, two CTAs per SM
   MIXED_ONE6 = 1,    // knn_one_kernel: one point per thread, six CTAs per SM (40 registers)
   MIXED_WS4 = 2,     // S-map: knn_smap_ws_kernel, 8 scan warps, 4 FP64 solver warps
-  MIXED_WS8 = 3      // S-map: knn_smap_ws_kernel, 8 scan warps, 8 FP64 solver warps
+  MIXED_WS8 = 3,     // S-map: knn_smap_ws_kernel, 8 scan warps, 8 FP64 solver warps
+  MIXED_WIDE = 4     // knn_one_kernel's wide form (E_a 9..16), chosen by E_a; reported in timings only
 };
 
 // Mixed-precision neighbour scan for the common case (L2, no missing values,

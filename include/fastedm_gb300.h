@@ -196,6 +196,12 @@ typedef struct fedm_timing {
                                 (downloads, per-task results)                */
   int exact_points;          /* of fallback_points, those the bounded FP32
                                 re-scan could not settle (full FP64 search)  */
+  int mixed_form;            /* kernel form of the last mixed launch: 0
+                                two points per thread, 1 one point per
+                                thread at six CTAs per SM, 2 / 3 warp-
+                                specialised S-map (4 / 8 solver warps),
+                                4 the wide form (E_actual 9..16); -1 none    */
+  int autotune_probes;       /* timed form probes of the autotuner          */
 } fedm_timing;
 
 int fedm_last_timing(const fedm_ctx* ctx, fedm_timing* out);

@@ -155,6 +155,44 @@ def test_mixed_kernel_forms_agree(form, algorithm, monkeypatch):
         assert np.array_equal(g["coeffs"], f["coeffs"], equal_nan=True)
 
 
+@pytest.mark.parametrize("algorithm", ["simplex", "smap"])
+def test_autotuner_keeps_bits_and_its_choice(algorithm, monkeypatch):
+    """With autotuning on (the default), the first batch of an (algorithm,
+    E_a, k) large enough to measure times each candidate form on the same
+    leading tasks (simplex: two forms, S-map: three; two rounds) and the
+    context keeps the fastest; a second call reuses it without probing.  Every form gives
+    the same bits, so rho, forecasts and coefficients equal a context fixed
+    to one form."""
+    monkeypatch.delenv("FEDM_AUTOTUNE", raising=False)
+    monkeypatch.delenv("FEDM_MIXED_KERNEL", raising=False)
+    w = workloads.ccm_config(T=20000, reps=8, n_libs=4, hi=15000)
+    kw = dict(E=4, library=w["libraries"], numReps=8, seed=w["seed"], algorithm=algorithm,
+              theta=2.0 if algorithm == "smap" else 1.0, savePredictions=True, saveSMAPCoeffs=algorithm == "smap")
+    tuned = fedm.Context(0, precision=fedm.PRECISION_MIXED)
+    monkeypatch.setenv("FEDM_MIXED_KERNEL", "one6")
+    fixed = fedm.Context(0, precision=fedm.PRECISION_MIXED)
+    try:
+        g = fedm.edm(w["t"], w["x"], w["y"], ctx=tuned, **kw)
+        t1 = tuned.timing()
+        g2 = fedm.edm(w["t"], w["x"], w["y"], ctx=tuned, **kw)
+        t2 = tuned.timing()
+        f = fedm.edm(w["t"], w["x"], w["y"], ctx=fixed, **kw)
+        tf = fixed.timing()
+    finally:
+        tuned.close()
+        fixed.close()
+    assert t1["autotune_probes"] == 2 * (3 if algorithm == "smap" else 2)  # two timed rounds
+    assert t1["mixed_form"] in ((0, 1, 3) if algorithm == "smap" else (0, 1))
+    assert t2["autotune_probes"] == 0 and t2["mixed_form"] == t1["mixed_form"]
+    assert tf["autotune_probes"] == 0 and tf["mixed_form"] == 1
+    for r in (g, g2):
+        assert r["rc"] == f["rc"] == 0
+        assert np.array_equal(r["stats"]["rho"], f["stats"]["rho"], equal_nan=True)
+        assert np.array_equal(r["predictions"], f["predictions"], equal_nan=True)
+        if algorithm == "smap":
+            assert np.array_equal(r["coeffs"], f["coeffs"], equal_nan=True)
+
+
 @pytest.mark.parametrize("E", [5, 8])
 @pytest.mark.parametrize("algorithm", ["simplex", "smap"])
 def test_wide_embedding_task_bit_exact(ctx, E, algorithm):
