@@ -213,7 +213,7 @@ int fedm_smap_fwd(fedm_ctx* ctx, const double* lib_manifold, const double* lib_t
     return FEDM_UNKNOWN_ERROR;
   return guarded(ctx, [&] {
     return fedm::smap_grad(*ctx->c, lib_manifold, lib_targets, n_lib, pred_manifold, pred_targets, n_pred, e_actual,
-                           theta, w, mse, predictions, nullptr, nullptr);
+                           theta, w, 0, mse, predictions, nullptr, nullptr);
   });
 }
 
@@ -226,7 +226,21 @@ int fedm_smap_bwd(fedm_ctx* ctx, const double* lib_manifold, const double* lib_t
     return FEDM_UNKNOWN_ERROR;
   return guarded(ctx, [&] {
     return fedm::smap_grad(*ctx->c, lib_manifold, lib_targets, n_lib, pred_manifold, pred_targets, n_pred, e_actual,
-                           theta, w, mse, nullptr, dmse_dtheta, dmse_dw);
+                           theta, w, 0, mse, nullptr, dmse_dtheta, dmse_dw);
+  });
+}
+
+int fedm_smap_grad(fedm_ctx* ctx, const double* lib_manifold, const double* lib_targets, int n_lib,
+                   const double* pred_manifold, const double* pred_targets, int n_pred, int e_actual, double theta,
+                   const double* w, int objective, double* value, double* dvalue_dtheta, double* dvalue_dw,
+                   double* predictions)
+{
+  if (!ctx || !lib_manifold || !lib_targets || !pred_manifold || !pred_targets || !w || !value ||
+      !dvalue_dtheta || !dvalue_dw)
+    return FEDM_UNKNOWN_ERROR;
+  return guarded(ctx, [&] {
+    return fedm::smap_grad(*ctx->c, lib_manifold, lib_targets, n_lib, pred_manifold, pred_targets, n_pred, e_actual,
+                           theta, w, objective, value, predictions, dvalue_dtheta, dvalue_dw);
   });
 }
 

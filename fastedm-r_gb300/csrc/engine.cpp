@@ -1158,9 +1158,11 @@ CommandResult run_command(Context& ctx, const fedm_args& a)
 
 // ------------------------------------------------------ differentiable S-map
 int smap_grad(Context& ctx, const double* lib, const double* lib_t, int n_lib, const double* pred,
-              const double* pred_t, int n_pred, int e_actual, double theta, const double* w, double* mse,
-              double* predictions, double* dtheta, double* dw)
+              const double* pred_t, int n_pred, int e_actual, double theta, const double* w, int objective,
+              double* value, double* predictions, double* dtheta, double* dw)
 {
+  if (objective != 0 && objective != 1)
+    throw Error{ RC_UNKNOWN_ERROR, "objective must be 0 (MSE) or 1 (rho)" };
   if (e_actual < 1 || e_actual > 8)
     throw Error{ RC_NOT_IMPLEMENTED, "differentiable S-map supports 1 <= E_actual <= 8" };
   if (n_lib < 1 || n_pred < 1)
@@ -1207,25 +1209,61 @@ int smap_grad(Context& ctx, const double* lib, const double* lib_t, int n_lib, c
   cudaEventElapsedTime(&ms, e0, e1);
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
-  // fixed-order host reduction over prediction points
-  double se = 0, gt = 0;
-  std::vector<double> gw(E, 0.0);
-  for (int p = 0; p < n_pred; p++) {
-    const double* o = &out[(size_t)p * (E + 3)];
-    se += o[0] * o[0];
-    if (predictions)
-      predictions[p] = o[1];
-    if (dtheta) {
-      gt += o[2];
-      for (size_t j = 0; j < E; j++)
-        gw[j] += o[3 + j];
+  // fixed-order host reductions over prediction points; per point the
+  // kernel gives r = yhat - target, yhat, dyhat/dtheta and dyhat/dw
+  auto o = [&](int p) { return &out[(size_t)p * (E + 3)]; };
+  if (predictions)
+    for (int p = 0; p < n_pred; p++)
+      predictions[p] = o(p)[1];
+  // dvalue/dyhat_p for the chosen objective
+  std::vector<double> dv(n_pred);
+  if (objective == 0) {
+    // MSE = mean r^2, dMSE/dyhat_p = 2 r_p / n
+    double se = 0;
+    for (int p = 0; p < n_pred; p++) {
+      se += o(p)[0] * o(p)[0];
+      dv[p] = 2 * o(p)[0] / n_pred;
+    }
+    *value = se / n_pred;
+  } else {
+    // rho as src/stats.cpp:64-80 computes it (centred sums; no value when
+    // either series is constant), and
+    // drho/dyhat_p = ((t_p - tbar) - (Sxy / Sxx)(yhat_p - ybar)) / sqrt(Sxx Syy)
+    double ybar = 0, tbar = 0;
+    for (int p = 0; p < n_pred; p++) {
+      ybar += o(p)[1];
+      tbar += pred_t[p];
+    }
+    ybar /= n_pred;
+    tbar /= n_pred;
+    double sxx = 0, syy = 0, sxy = 0;
+    for (int p = 0; p < n_pred; p++) {
+      const double a = o(p)[1] - ybar, b = pred_t[p] - tbar;
+      sxx += a * a;
+      syy += b * b;
+      sxy += a * b;
+    }
+    const double sdx = std::sqrt(sxx), sdy = std::sqrt(syy);
+    if (sdx < 1e-9 || sdy < 1e-9) {
+      *value = NAN;
+      std::fill(dv.begin(), dv.end(), NAN);
+    } else {
+      *value = sxy / (sdx * sdy);
+      for (int p = 0; p < n_pred; p++)
+        dv[p] = ((pred_t[p] - tbar) - (sxy / sxx) * (o(p)[1] - ybar)) / (sdx * sdy);
     }
   }
-  *mse = se / n_pred;
   if (dtheta) {
-    *dtheta = gt / n_pred;
+    double gt = 0;
+    std::vector<double> gw(E, 0.0);
+    for (int p = 0; p < n_pred; p++) {
+      gt += dv[p] * o(p)[2];
+      for (size_t j = 0; j < E; j++)
+        gw[j] += dv[p] * o(p)[3 + j];
+    }
+    *dtheta = gt;
     for (size_t j = 0; j < E; j++)
-      dw[j] = gw[j] / n_pred;
+      dw[j] = gw[j];
   }
   ctx.timing.device_ms = ms;
   ctx.timing.knn_kernel_ms = ms;

@@ -72,10 +72,11 @@ int host_manifold(const fedm_args& a, int E, int copredict, double* out);
 int host_plan(const fedm_args& a, int max_tasks, int* task_E, int* task_k, int* task_library, int* task_copredict,
               unsigned char* lib_masks, unsigned char* pred_masks);
 int run_task(Context& ctx, const fedm_args& a, fedm_task_io& io);
-// Differentiable S-map (all library neighbours, per-lag weights w): MSE and,
+// Differentiable S-map (all library neighbours, per-lag weights w): the
+// objective (0: MSE of the forecasts, 1: their rho with the targets) and,
 // when dtheta is not null, its gradient.  predictions may be null.
 int smap_grad(Context& ctx, const double* lib, const double* lib_t, int n_lib, const double* pred,
-              const double* pred_t, int n_pred, int e_actual, double theta, const double* w, double* mse,
-              double* predictions, double* dtheta, double* dw);
+              const double* pred_t, int n_pred, int e_actual, double theta, const double* w, int objective,
+              double* value, double* predictions, double* dtheta, double* dw);
 
 } // namespace fedm

@@ -183,7 +183,7 @@ struct AdjointParams
   const double* w;       // [e_actual] per-lag embedding weights
   double theta;
   int n_lib, n_pred, e_actual;
-  int backward;          // 0: r, yhat only; 1: also 2 r dyhat/dtheta and 2 r dyhat/dw
+  int backward;          // 0: r, yhat only; 1: also dyhat/dtheta and dyhat/dw
   double* out;           // [n_pred x (e_actual + 3)]
 };
 void launch_smap_grad(const AdjointParams& a, cudaStream_t s);

@@ -17,7 +17,8 @@
 //   dyhat/dw_j  = m_pj c_{j+1} - (2 theta/mu) R_j + (2 theta dmu/dw_j/mu^2) Q
 //                 + g_{j+1} S_j - c_{j+1} T_j
 // (from dyhat = dv.c + g.(db - dA c), A symmetric).  Each point writes r,
-// and 2 r dyhat/d(.) ; the host sums them in a fixed order.
+// yhat, dyhat/dtheta and dyhat/dw; the host composes the objective's
+// gradient (MSE or rho) from them in a fixed order.
 //
 // Only the distances follow the reference's rounding: the sums over the
 // library are lane-strided and warp-reduced, so the forecast agrees with the
@@ -219,13 +220,11 @@ __global__ void __launch_bounds__(128) smap_grad_kernel(AdjointParams a)
   if (lane == 0) {
     out[0] = r;
     out[1] = yhat;
-    out[2] = 2 * r * (-(2 / mu) * Q);
+    out[2] = -(2 / mu) * Q;
 #pragma unroll
-    for (int j = 0; j < EA; j++) {
-      const double dy = y[j] * c[j + 1] - (2 * a.theta / mu) * R[j] + (2 * a.theta * dmu[j] / (mu * mu)) * Q +
-                        gv[j + 1] * S[j] - c[j + 1] * Tt[j];
-      out[3 + j] = 2 * r * dy;
-    }
+    for (int j = 0; j < EA; j++)
+      out[3 + j] = y[j] * c[j + 1] - (2 * a.theta / mu) * R[j] + (2 * a.theta * dmu[j] / (mu * mu)) * Q +
+                   gv[j + 1] * S[j] - c[j + 1] * Tt[j];
   }
 }
 

@@ -77,7 +77,7 @@ EXPORTS = [
     "fedm_create", "fedm_destroy", "fedm_last_error", "fedm_set_precision", "fedm_set_keep_going",
     "fedm_run_command", "fedm_free_result", "fedm_run_task", "fedm_last_timing", "fedm_measure_peak",
     "fedm_host_usable", "fedm_host_manifold", "fedm_host_mt_real2", "fedm_host_plan",
-    "fedm_smap_fwd", "fedm_smap_bwd", "fedm_predict_static",
+    "fedm_smap_fwd", "fedm_smap_bwd", "fedm_smap_grad", "fedm_predict_static",
 ]
 
 _lib = None
@@ -105,6 +105,8 @@ def load():
                      C.c_double, C.c_void_p, C.POINTER(C.c_double)]
         lib.fedm_smap_fwd.argtypes = grad_args + [C.c_void_p]
         lib.fedm_smap_bwd.argtypes = grad_args + [C.POINTER(C.c_double), C.c_void_p]
+        lib.fedm_smap_grad.argtypes = grad_args[:-1] + [C.c_int, C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                                        C.c_void_p, C.c_void_p]
         lib.fedm_host_usable.argtypes = [C.POINTER(Args), C.c_int, C.c_int, C.c_void_p]
         lib.fedm_host_manifold.argtypes = [C.POINTER(Args), C.c_int, C.c_int, C.c_void_p, C.POINTER(C.c_int)]
         lib.fedm_host_mt_real2.argtypes = [C.c_ulonglong, C.c_longlong, C.c_void_p]
@@ -188,6 +190,23 @@ class Context:
         if rc != 0:
             raise RuntimeError(f"fedm_smap_fwd rc={rc}: {self.last_error()}")
         return mse.value, None, None, yh
+
+    def smap_objective_grad(self, lib, lib_t, pred, pred_t, theta, w, objective="mse"):
+        """The same pass for a chosen objective, "mse" or "rho" (forecasts
+        against targets): (value, dvalue/dtheta, dvalue/dw, predictions)."""
+        arrs = [np.ascontiguousarray(v, dtype=np.float64) for v in (lib, lib_t, pred, pred_t, w)]
+        lib, lib_t, pred, pred_t, w = arrs
+        E = lib.shape[1]
+        val, dth = C.c_double(), C.c_double()
+        dw = np.zeros(E)
+        yh = np.zeros(pred.shape[0])
+        obj = {"mse": 0, "rho": 1}[objective]
+        rc = self.lib.fedm_smap_grad(self.h, lib.ctypes.data, lib_t.ctypes.data, lib.shape[0], pred.ctypes.data,
+                                     pred_t.ctypes.data, pred.shape[0], E, float(theta), w.ctypes.data, obj,
+                                     C.byref(val), C.byref(dth), dw.ctypes.data, yh.ctypes.data)
+        if rc != 0:
+            raise RuntimeError(f"fedm_smap_grad rc={rc}: {self.last_error()}")
+        return val.value, dth.value, dw, yh
 
     def run_command(self, a):
         keep = []

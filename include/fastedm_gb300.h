@@ -243,6 +243,17 @@ int fedm_smap_fwd(fedm_ctx* ctx, const double* lib_manifold, const double* lib_t
 int fedm_smap_bwd(fedm_ctx* ctx, const double* lib_manifold, const double* lib_targets, int n_lib,
                   const double* pred_manifold, const double* pred_targets, int n_pred, int e_actual, double theta,
                   const double* w, double* mse, double* dmse_dtheta, double* dmse_dw);
+/*  fedm_smap_grad: the same forward and backward pass for a chosen
+ *                 objective: 0 the MSE (as fedm_smap_bwd), 1 rho, the
+ *                 correlation of forecasts and targets computed as
+ *                 src/stats.cpp:64-80 does (NaN, with NaN gradients, when
+ *                 either has a root sum of squared deviations below 1e-9).
+ *                 value, dvalue_dtheta, dvalue_dw [e_actual]; predictions
+ *                 [n_pred] may be NULL. */
+int fedm_smap_grad(fedm_ctx* ctx, const double* lib_manifold, const double* lib_targets, int n_lib,
+                   const double* pred_manifold, const double* pred_targets, int n_pred, int e_actual, double theta,
+                   const double* w, int objective, double* value, double* dvalue_dtheta, double* dvalue_dw,
+                   double* predictions);
 
 /* Allocation-free prediction for one task on caller-owned device buffers.
  * No counterpart in the reference: it exists for callers that cannot let a

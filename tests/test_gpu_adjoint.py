@@ -97,6 +97,47 @@ def test_gradient_matches_finite_differences(ctx, small, h, rtol_theta, rtol_w):
         assert np.isclose(gw[j], fd, rtol=rtol_w, atol=1e-12), (j, gw[j], fd)
 
 
+def test_objective_entry_mse_is_the_backward_pass(ctx, small):
+    s = small
+    w = np.linspace(0.9, 1.2, E)
+    m, gt, gw, _ = ctx.smap_grad(s["lib"], s["lib_t"], s["pred"], s["pred_t"], 0.8, w)
+    v, vt, vw, yh = ctx.smap_objective_grad(s["lib"], s["lib_t"], s["pred"], s["pred_t"], 0.8, w, "mse")
+    assert v == m and vt == gt and np.array_equal(vw, gw)
+    assert np.isclose(v, np.mean((yh - s["pred_t"]) ** 2), rtol=1e-12)
+
+
+def test_rho_objective_value(ctx, small):
+    """rho of the forecasts against the targets, by the reference's
+    centred-sum formula (src/stats.cpp:64-80)."""
+    s = small
+    v, _, _, yh = ctx.smap_objective_grad(s["lib"], s["lib_t"], s["pred"], s["pred_t"], 1.5, np.ones(E), "rho")
+    a, b = yh - yh.mean(), s["pred_t"] - s["pred_t"].mean()
+    assert np.isclose(v, np.sum(a * b) / (np.sqrt(np.sum(a * a)) * np.sqrt(np.sum(b * b))), rtol=1e-12)
+    assert 0.5 < v < 1.0
+
+
+@pytest.mark.parametrize("theta", [0.3, 2.0])
+def test_rho_gradient_matches_finite_differences(ctx, small, theta):
+    """drho/dtheta and drho/dw from the adjoint (drho/dyhat composed on the
+    host with the kernel's dyhat/d(.)) against central differences of the
+    forward pass, h = 1e-3 (past the forward pass's rounding noise)."""
+    s = small
+    w = np.linspace(0.8, 1.3, E)
+    _, gt, gw, _ = ctx.smap_objective_grad(s["lib"], s["lib_t"], s["pred"], s["pred_t"], theta, w, "rho")
+
+    def f(th, ww):
+        return ctx.smap_objective_grad(s["lib"], s["lib_t"], s["pred"], s["pred_t"], th, ww, "rho")[0]
+
+    h = 1e-3
+    fd_t = (f(theta + h, w) - f(theta - h, w)) / (2 * h)
+    assert np.isclose(gt, fd_t, rtol=1e-4, atol=1e-9), (gt, fd_t)
+    for j in range(E):
+        e = np.zeros(E)
+        e[j] = h
+        fd = (f(theta, w + e) - f(theta, w - e)) / (2 * h)
+        assert np.isclose(gw[j], fd, rtol=1e-3, atol=1e-8), (j, gw[j], fd)
+
+
 def test_gradient_descent_on_theta(ctx, small):
     s = small
     w = np.ones(E)
