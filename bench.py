@@ -413,7 +413,7 @@ def config_steps(fedm, workloads, ctx, name):
 def run_config(a):
     fedm, workloads = load_pkg()
     world, rank, local = dist_setup()
-    ctx = fedm.Context(local, precision=fedm.PRECISION_MIXED)
+    ctx = fedm.Context(local, precision={"mixed": fedm.PRECISION_MIXED, "fast": fedm.PRECISION_FAST}[a.precision])
     cfg, step = config_steps(fedm, workloads, ctx, a.workload)
     for _ in range(max(3, a.warmup)):
         step()
@@ -438,7 +438,7 @@ def run_config(a):
     cfg["l2"] = "flushed between steps (512 MiB write)"
     cfg["parallelism"] = f"replicas x{world}"
     out = {
-        "metric": f"{a.workload} predictions/s (full-size configuration, mixed precision path)", "value":
+        "metric": f"{a.workload} predictions/s (full-size configuration, {a.precision} precision path)", "value":
         preds * world / dev, "unit": "predictions/s", "n_gpus": world, "steps": a.steps, "warmup": max(3, a.warmup),
         "ms_per_step": dev / a.steps * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "fp32+fp64", "data": "synthetic (seeded generators)", "config": cfg,
@@ -495,6 +495,9 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-fp64", dest="no_fp64", action="store_true",
                     help="skip the plain FP64 sample (profiling runs)")
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fast"],
+                    help="context precision for the non-headline workloads: mixed (bit-exact) or fast (FP32 "
+                         "weights and double-float normal equations for the k = all S-map)")
     ap.add_argument("--workload", default="ccm",
                     choices=["ccm", "simplex_explore", "smap_sweep", "panels", "adjoint"],
                     help="ccm (default): the headline CCM benchmark; the others time the other benchmark "

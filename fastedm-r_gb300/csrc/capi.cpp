@@ -78,7 +78,8 @@ const char* fedm_last_error(const fedm_ctx* ctx)
 
 int fedm_set_precision(fedm_ctx* ctx, int precision)
 {
-  if (!ctx || (precision != FEDM_PRECISION_FP64 && precision != FEDM_PRECISION_MIXED))
+  if (!ctx || (precision != FEDM_PRECISION_FP64 && precision != FEDM_PRECISION_MIXED &&
+               precision != FEDM_PRECISION_FAST))
     return FEDM_UNKNOWN_ERROR;
   ctx->c->precision = precision;
   return FEDM_SUCCESS;

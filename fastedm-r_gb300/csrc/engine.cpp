@@ -316,7 +316,7 @@ constexpr long long FB_CAP = 1 << 24;
 bool mixed_eligible(const Context& ctx, const Options& o, const GroupJob& job, std::vector<double>& center,
                     double& R)
 {
-  if (ctx.precision != FEDM_PRECISION_MIXED || o.distance != 1 || o.has_missing || o.low_memory || o.past_only ||
+  if (ctx.precision == FEDM_PRECISION_FP64 || o.distance != 1 || o.has_missing || o.low_memory || o.past_only ||
       !o.force_compute || job.Ea > WIDE_EA || job.Ea < 1 || !job.hF || !job.hFp)
     return false;
   if (o.panel_mode && (o.idw != 0 || o.has_id_weights))
@@ -499,6 +499,28 @@ void run_group(Context& ctx, const Options& o, const std::vector<Task>& tasks, c
   ctx.timing.setup_ms += now_ms() - t_enter;
   ctx.timing.kernel_launches += 6;  // fills
 
+  // FAST precision: the k = all S-map accumulates its normal equations in
+  // double-float arithmetic from a per-row table of products
+  const float2* gram_terms = nullptr;
+  if (ctx.precision == FEDM_PRECISION_FAST && any_all && o.algorithm == 1 && Ea <= 8 && !o.has_missing &&
+      !o.low_memory) {
+    const long long pool = (long long)lib_pool.size();
+    const long long bytes = pool * gram_terms_per_row(Ea) * (long long)sizeof(float2);
+    if (pool > 0 && bytes <= (2LL << 30)) {
+      float2* P = (float2*)ctx.buf("gram_terms", (size_t)bytes);
+      int* bad = (int*)ctx.buf("gram_bad", 4);
+      fill_i32(bad, 1, 0, s);
+      launch_gram_terms(g, pool, P, bad, s);
+      ctx.check("gram terms");
+      int hbad = 0;
+      ctx.download(&hbad, bad, 4);
+      ck(cudaStreamSynchronize(s), "sync");
+      if (!hbad)
+        gram_terms = P;
+      ctx.timing.kernel_launches += 2;
+    }
+  }
+
   // chunking: neighbour lists, statuses and the all-mode Gram buffer
   const long long budget = 2LL << 30;
   long long per_point = (long long)kcap * 12 + 8;
@@ -591,7 +613,7 @@ void run_group(Context& ctx, const Options& o, const std::vector<Task>& tasks, c
       ctx.timing.kernel_launches += 1;
     }
     if (with_all) {
-      launch_all_mode(g, c, ctx.num_sms, max_nlib_all, s);
+      launch_all_mode(g, c, ctx.num_sms, max_nlib_all, s, gram_terms);
       ctx.check("all_mode");
       ctx.timing.kernel_launches += o.algorithm == 1 ? 2 : 1;
     }

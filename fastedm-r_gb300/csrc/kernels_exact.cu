@@ -716,6 +716,126 @@ __global__ void __launch_bounds__(128) all_smap_kernel(GroupParams g, ChunkBuffe
   smap_finish(g, T, p, prow, t, xs, n);
 }
 
+// ------------------------------------------- k = all S-map, FAST precision
+// The normal equations of the k = all S-map are sum_i w_i^2 u_i u_i^T and
+// sum_i w_i^2 t_i u_i (u_i = [1, m_i]): per library row a fixed table of
+// n(n+1)/2 + n products, scaled by one weight per (point, theta, row).
+// gram_terms_kernel writes each pool row's products, rounded to FP64 and
+// split into a float pair hi + lo (48 significant bits);
+// all_smap_df_kernel computes w^2 = exp(-2 theta d / mean) in FP32 and
+// accumulates every entry in double-float arithmetic: the product w^2 * hi
+// exactly by TwoProd (an FMA), the sum exactly by Knuth's TwoSum, and the
+// rounding errors with w^2 * lo in a float correction term.  The solve is
+// the FP64 JacobiSVD of the exact path.  The weights carry FP32 rounding
+// (~1e-7 relative); the sums carry ~1e-13.  A term of 1e30 or more, or not
+// finite, sets *bad and the caller keeps the exact path.
+template<int EA>
+__global__ void gram_terms_kernel(GroupParams g, long long pool_size, float2* P, int* bad)
+{
+  constexpr int n = EA + 1, NP = n * (n + 1) / 2 + n;
+  const long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= pool_size)
+    return;
+  const int row = g.lib_rows[i];
+  double u[n];
+  u[0] = 1.0;
+#pragma unroll
+  for (int j = 1; j < n; j++)
+    u[j] = g.F[(size_t)row * EA + j - 1];
+  const double t = g.lib_target[row];
+  float2* out = P + (size_t)i * NP;
+  int e = 0;
+  bool ok = true;
+  auto put = [&](double v) {
+    const float hi = (float)v;
+    const float lo = (float)(v - (double)hi);
+    ok = ok && fabs(v) < 1e30;
+    out[e++] = make_float2(hi, lo);
+  };
+#pragma unroll
+  for (int a = 0; a < n; a++)
+#pragma unroll
+    for (int b = a; b < n; b++)
+      put(u[a] * u[b]);
+#pragma unroll
+  for (int a = 0; a < n; a++)
+    put(t * u[a]);
+  if (!ok)
+    atomicExch(bad, 1);
+}
+
+template<int EA>
+__global__ void __launch_bounds__(128) all_smap_df_kernel(GroupParams g, ChunkBuffers c, long long max_nlib,
+                                                           const float2* P)
+{
+  constexpr int n = EA + 1, NA = n * (n + 1) / 2, NP = NA + n;
+  const long long chunk = c.p_end - c.p_begin;
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= chunk * g.n_thetas)
+    return;
+  const long long q = idx / g.n_thetas;
+  const int t = (int)(idx - q * g.n_thetas);
+  const long long p = point_of(c, q);
+  const DevTask T = g.tasks[find_task(g, p)];
+  if (!T.all_mode)
+    return;
+  const int st = c.status[q];
+  if (st != PT_OK) {
+    early_rc(g, T.task, st, t);
+    return;
+  }
+  const double* dq = c.scratch + q * max_nlib;
+  const int ke = c.nn_count[q];
+  double mean = 0;
+  for (int i = 0; i < T.n_lib; i++)
+    if (dq[i] >= 0)
+      mean += dq[i];
+  mean /= (double)ke;
+  const float c2 = (float)(-2.0 * g.thetas[t] / mean);
+  float S[NP], Cr[NP];
+#pragma unroll
+  for (int e = 0; e < NP; e++)
+    S[e] = Cr[e] = 0.f;
+  const float2* pool = P + (size_t)T.lib_off * NP;
+  for (int i = 0; i < T.n_lib; i++) {
+    const double d = dq[i];
+    if (d < 0)
+      continue;
+    const float om = expf(__fmul_rn(c2, (float)d));
+    const float2* pr = pool + (size_t)i * NP;
+#pragma unroll
+    for (int e = 0; e < NP; e++) {
+      const float2 v = pr[e];
+      const float prod = __fmul_rn(om, v.x);
+      const float perr = __fmaf_rn(om, v.x, -prod);  // om * hi = prod + perr exactly
+      const float s = __fadd_rn(S[e], prod);
+      const float bp = __fsub_rn(s, S[e]);
+      const float ds = __fadd_rn(__fsub_rn(S[e], __fsub_rn(s, bp)), __fsub_rn(prod, bp));  // S + prod = s + ds exactly
+      S[e] = s;
+      Cr[e] = __fadd_rn(Cr[e], __fadd_rn(ds, __fmaf_rn(om, v.y, perr)));
+    }
+  }
+  double Wl[n * n], bv[n], U[n * n], V[n * n], sv[n], tmp[n], xs[n];
+  int e = 0;
+#pragma unroll
+  for (int a = 0; a < n; a++)
+#pragma unroll
+    for (int b = a; b < n; b++) {
+      const double v = (double)S[e] + (double)Cr[e];
+      Wl[a * n + b] = v;
+      Wl[b * n + a] = v;
+      e++;
+    }
+#pragma unroll
+  for (int a = 0; a < n; a++) {
+    bv[a] = (double)S[e] + (double)Cr[e];
+    e++;
+  }
+  svd_solve(Wl, U, V, sv, tmp, bv, xs, n);
+  const int prow = g.pred_rows[T.pred_off + (int)(p - T.point_base)];
+  smap_finish(g, T, p, prow, t, xs, n);
+}
+
 // ----------------------------------------------------------------- stats
 // rho and MAE per (task, theta) over forecasts whose target is observed
 // (src/edm.cpp:441-467, src/stats.cpp:64-94).  Two passes like the
@@ -890,7 +1010,32 @@ long long all_mode_slab(int Ea)
   return 3LL * n * n + 4LL * n;
 }
 
-void launch_all_mode(const GroupParams& g, const ChunkBuffers& c, int num_sms, long long max_nlib, cudaStream_t s)
+int gram_terms_per_row(int Ea)
+{
+  const int n = Ea + 1;
+  return n * (n + 1) / 2 + n;
+}
+
+void launch_gram_terms(const GroupParams& g, long long pool_size, float2* P, int* bad, cudaStream_t s)
+{
+  if (pool_size <= 0)
+    return;
+  const int b = (int)((pool_size + 127) / 128);
+  switch (g.Ea) {
+    case 1: gram_terms_kernel<1><<<b, 128, 0, s>>>(g, pool_size, P, bad); break;
+    case 2: gram_terms_kernel<2><<<b, 128, 0, s>>>(g, pool_size, P, bad); break;
+    case 3: gram_terms_kernel<3><<<b, 128, 0, s>>>(g, pool_size, P, bad); break;
+    case 4: gram_terms_kernel<4><<<b, 128, 0, s>>>(g, pool_size, P, bad); break;
+    case 5: gram_terms_kernel<5><<<b, 128, 0, s>>>(g, pool_size, P, bad); break;
+    case 6: gram_terms_kernel<6><<<b, 128, 0, s>>>(g, pool_size, P, bad); break;
+    case 7: gram_terms_kernel<7><<<b, 128, 0, s>>>(g, pool_size, P, bad); break;
+    case 8: gram_terms_kernel<8><<<b, 128, 0, s>>>(g, pool_size, P, bad); break;
+    default: break;
+  }
+}
+
+void launch_all_mode(const GroupParams& g, const ChunkBuffers& c, int num_sms, long long max_nlib, cudaStream_t s,
+                     const float2* gram_terms)
 {
   int per_warp;
   const int w = all_warps_per_block(g.Ea, per_warp);
@@ -905,6 +1050,19 @@ void launch_all_mode(const GroupParams& g, const ChunkBuffers& c, int num_sms, l
   if (total <= 0)
     return;
   const int fb = (int)((total + 127) / 128);
+  if (g.algorithm == 1 && g.Ea <= 8 && gram_terms) {
+    switch (g.Ea) {
+      case 1: all_smap_df_kernel<1><<<fb, 128, 0, s>>>(g, c, max_nlib, gram_terms); return;
+      case 2: all_smap_df_kernel<2><<<fb, 128, 0, s>>>(g, c, max_nlib, gram_terms); return;
+      case 3: all_smap_df_kernel<3><<<fb, 128, 0, s>>>(g, c, max_nlib, gram_terms); return;
+      case 4: all_smap_df_kernel<4><<<fb, 128, 0, s>>>(g, c, max_nlib, gram_terms); return;
+      case 5: all_smap_df_kernel<5><<<fb, 128, 0, s>>>(g, c, max_nlib, gram_terms); return;
+      case 6: all_smap_df_kernel<6><<<fb, 128, 0, s>>>(g, c, max_nlib, gram_terms); return;
+      case 7: all_smap_df_kernel<7><<<fb, 128, 0, s>>>(g, c, max_nlib, gram_terms); return;
+      case 8: all_smap_df_kernel<8><<<fb, 128, 0, s>>>(g, c, max_nlib, gram_terms); return;
+      default: break;
+    }
+  }
   if (g.algorithm == 1 && g.Ea <= 8) {
     switch (g.Ea) {
       case 1: all_smap_kernel<1><<<fb, 128, 0, s>>>(g, c, max_nlib); return;

@@ -18,6 +18,7 @@ INT_MIN = -(2**31)
 
 PRECISION_FP64 = 0
 PRECISION_MIXED = 1
+PRECISION_FAST = 2
 
 
 class Args(C.Structure):

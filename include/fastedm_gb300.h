@@ -31,13 +31,19 @@ extern "C" {
  *                        order ("plain FP64 GPU form").
  *  FEDM_PRECISION_MIXED: FP32 candidate distances with a proven error margin,
  *                        then an FP64 re-rank of every candidate inside the
- *                        margin, so neighbour sets and distances are the same
- *                        bits as FP64; the FP64 S-map solve uses a faster
- *                        normal-equation path when it is well conditioned.
- *                        Falls back to FP64 where its preconditions (no
- *                        missing values, no panels, L2) do not hold. */
+ *                        margin, so neighbour sets, distances and forecasts
+ *                        are the same bits as FP64.  Falls back to FP64
+ *                        where its preconditions (no missing values, L2
+ *                        distances, no panel weights) do not hold.
+ *  FEDM_PRECISION_FAST:  MIXED, and the S-map with every library row as a
+ *                        neighbour (k = all, E_actual <= 8, no missing
+ *                        values) takes its weights in FP32 and accumulates
+ *                        its normal equations in double-float arithmetic
+ *                        before the FP64 solve: forecasts agree with FP64 to
+ *                        about 1e-7 relative instead of bit for bit. */
 #define FEDM_PRECISION_FP64 0
 #define FEDM_PRECISION_MIXED 1
+#define FEDM_PRECISION_FAST 2
 
 typedef struct fedm_ctx fedm_ctx;
 

@@ -108,6 +108,38 @@ def test_smap_theta0_is_least_squares_full_size(ctx):
     assert np.allclose(got, want, rtol=1e-7, atol=1e-9)
 
 
+@pytest.mark.parametrize("T", [1600, 20000], ids=["reduced", "full_size"])
+def test_fast_precision_smap_all_neighbours(T):
+    """FEDM_PRECISION_FAST (config 2 shape: E = 5, k = all, a theta sweep
+    with theta = 0..8): FP32 weights and double-float normal equations, then
+    the FP64 solve.  Against the bit-exact FP64 path the forecasts agree to
+    the FP32 weights' rounding and rho to 1e-6; theta = 0 (every weight 1) is
+    exact up to the double-float sums."""
+    w = workloads.smap_config(T=T)
+    thetas = [0.0, 0.5, 1.0, 2.0, 4.0, 8.0]
+    kw = dict(E=5, k=float("inf"), theta=thetas, algorithm="smap", savePredictions=True)
+    fast = fedm.Context(0, precision=fedm.PRECISION_FAST)
+    exact = fedm.Context(0, precision=fedm.PRECISION_MIXED)
+    try:
+        f = fedm.edm(w["t"], w["x"], ctx=fast, **kw)
+        tf = fast.timing()
+        e = fedm.edm(w["t"], w["x"], ctx=exact, **kw)
+        te = exact.timing()
+    finally:
+        fast.close()
+        exact.close()
+    assert f["rc"] == e["rc"] == 0
+    pf, pe = np.asarray(f["predictions"], float), np.asarray(e["predictions"], float)
+    assert np.array_equal(np.isnan(pf), np.isnan(pe))
+    m = ~np.isnan(pe)
+    scale = np.max(np.abs(pe[m]))
+    err = np.max(np.abs(pf[m] - pe[m])) / scale
+    assert err < 1e-5, err
+    assert np.max(np.abs(np.asarray(f["stats"]["rho"]) - np.asarray(e["stats"]["rho"]))) <= 1e-6
+    print(f"T={T}: max |forecast difference| / max |forecast| = {err:.2e}; device ms fast {tf['device_ms']:.1f}, "
+          f"exact {te['device_ms']:.1f}")
+
+
 def test_mixed_fp64_operation_count(ctx):
     """The mixed kernel counts the FP64 arithmetic of its re-rank and forecast
     stage (the roofline's numerator); the exact FP64 path reports none."""
