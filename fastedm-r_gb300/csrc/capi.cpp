@@ -139,6 +139,12 @@ int fedm_run_command(fedm_ctx* ctx, const fedm_args* args, fedm_result** out)
   r.coeffs = (args->save_smap_coeffs && !d.coeffs.empty()) ? d.coeffs.data() : nullptr;
   r.missing_distance = d.has_missing_distance ? d.missing_distance : NAN;
   r.dt_weight = d.has_dt_weight ? d.dt_weight : NAN;
+  r.n_manifolds = (int)d.man_rows.size();
+  r.manifold_rows = d.man_rows.data();
+  r.pred_manifold_rows = d.pman_rows.data();
+  r.manifold_cols = d.man_cols.data();
+  r.manifolds = d.man.data();
+  r.pred_manifolds = d.pman.data();
   *out = &r;
   return rc;
 }

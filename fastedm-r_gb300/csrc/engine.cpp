@@ -1158,6 +1158,21 @@ CommandResult run_command(Context& ctx, const fedm_args& a)
       R.coeff_rows = nrow;
       R.coeff_cols = Ea + 1;
     }
+    if (a.save_manifolds) {
+      // src/edm.cpp:473-475, src/r.cpp:406-409: the task's library manifold
+      // (library rows whose target is observed) and prediction manifold
+      // (co_x lags for coprediction), row-major, MISSING as NA
+      auto append = [&](const std::vector<double>& F, const std::vector<int>& rows, std::vector<double>& out) {
+        for (int r : rows)
+          for (int j = 0; j < Ea; j++)
+            out.push_back(na(F[(size_t)r * Ea + j]));
+      };
+      append(M.host[std::make_pair(t.E, false)], lib_lists[t.lib_mask], R.man);
+      append(M.host[std::make_pair(t.E, t.copredict)], pred_lists[t.pred_mask], R.pman);
+      R.man_rows.push_back((int)lib_lists[t.lib_mask].size());
+      R.pman_rows.push_back((int)pred_lists[t.pred_mask].size());
+      R.man_cols.push_back(Ea);
+    }
     npred += (long long)pred_lists[t.pred_mask].size() * (long long)o.thetas.size();
     pairs += (long long)pred_lists[t.pred_mask].size() * (long long)lib_lists[t.lib_mask].size();
   }

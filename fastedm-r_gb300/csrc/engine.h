@@ -59,6 +59,10 @@ struct CommandResult
   std::vector<double> sT, sR, sM, cT, cR, cM;
   int kmin = MISSING_I, kmax = MISSING_I;
   std::vector<double> preds, copreds, coeffs;  // R matrices (column-major)
+  // saveManifolds: per task in task order, the library and prediction
+  // manifolds, row-major and concatenated
+  std::vector<int> man_rows, pman_rows, man_cols;
+  std::vector<double> man, pman;
   int pred_rows = 0, pred_cols = 0, copred_rows = 0, copred_cols = 0, coeff_rows = 0, coeff_cols = 0;
   double missing_distance = 0, dt_weight = 0;
   bool has_missing_distance = false, has_dt_weight = false;

@@ -49,6 +49,9 @@ class Result(C.Structure):
         ("copred_rows", C.c_int), ("copred_cols", C.c_int), ("copredictions", C.POINTER(C.c_double)),
         ("coeff_rows", C.c_int), ("coeff_cols", C.c_int), ("coeffs", C.POINTER(C.c_double)),
         ("missing_distance", C.c_double), ("dt_weight", C.c_double), ("internal", C.c_void_p),
+        ("n_manifolds", C.c_int), ("manifold_rows", C.POINTER(C.c_int)),
+        ("pred_manifold_rows", C.POINTER(C.c_int)), ("manifold_cols", C.POINTER(C.c_int)),
+        ("manifolds", C.POINTER(C.c_double)), ("pred_manifolds", C.POINTER(C.c_double)),
     ]
 
 
@@ -391,6 +394,20 @@ def result_to_dict(r):
             r.copred_cols, r.copred_rows).T
     if r.coeffs:
         out["coeffs"] = _arr(r.coeffs, r.coeff_rows * r.coeff_cols).reshape(r.coeff_cols, r.coeff_rows).T
+    if r.n_manifolds:
+        # saveManifolds: per task the library (Ms) and prediction (Mps)
+        # manifolds, row-major blocks in task order
+        rows, prows, cols = (_arr(v, r.n_manifolds) for v in (r.manifold_rows, r.pred_manifold_rows,
+                                                              r.manifold_cols))
+        man = _arr(r.manifolds, int(np.sum(rows * cols)))
+        pman = _arr(r.pred_manifolds, int(np.sum(prows * cols)))
+        out["Ms"], out["Mps"] = [], []
+        o1 = o2 = 0
+        for nr, npr, nc in zip(rows, prows, cols):
+            out["Ms"].append(man[o1:o1 + nr * nc].reshape(nr, nc))
+            out["Mps"].append(pman[o2:o2 + npr * nc].reshape(npr, nc))
+            o1 += nr * nc
+            o2 += npr * nc
     if not math.isnan(r.missing_distance):
         out["missingdistance"] = r.missing_distance
     if not math.isnan(r.dt_weight):

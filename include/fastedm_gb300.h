@@ -130,6 +130,18 @@ typedef struct fedm_result {
   double missing_distance;  /* NaN unless allow_missing                       */
   double dt_weight;         /* NaN unless dt or reldt                         */
   void* internal;
+  /* save_manifolds (src/r.cpp:406-409, 440-443): per task, in task order,
+   * the library manifold (manifold_rows[f] x manifold_cols[f]: the task's
+   * library rows whose target is observed) and the prediction manifold
+   * (pred_manifold_rows[f] x manifold_cols[f]), each row-major with NA as
+   * NaN, concatenated in task order in manifolds / pred_manifolds.
+   * n_manifolds is 0 without save_manifolds. */
+  int n_manifolds;
+  const int* manifold_rows;
+  const int* pred_manifold_rows;
+  const int* manifold_cols;
+  const double* manifolds;
+  const double* pred_manifolds;
 } fedm_result;
 
 /* Replaces run_command -> launch_tasks -> edm_task (src/r.cpp:107-468,

@@ -254,6 +254,42 @@ def test_wide_embedding_task_bit_exact(ctx, E, algorithm):
     assert np.array_equal(g["predictions"], o["predictions"], equal_nan=True)
 
 
+@pytest.mark.parametrize("case", ["explore_dt_missing", "ccm_copredict"])
+def test_save_manifolds(ctx, case):
+    """saveManifolds (src/edm.cpp:473-475, src/r.cpp:406-409, 440-443): per
+    task in task order, the library manifold (the task's library rows whose
+    target is observed) and the prediction manifold (co_x lags for a
+    coprediction task), missing values as NA.  easy_edm() reads
+    nrow(res$Ms[[1]]) as its largest library (R/easy_edm.R:297-312).  Each
+    must be the oracle's manifold for the task's masks from the task plan."""
+    if case == "explore_dt_missing":
+        t, x, _ = workloads.coupled_logistic(400, seed=3)
+        x = x.copy()
+        x[::37] = np.nan
+        t = t.astype(float).copy()
+        t[5::50] += 0.5  # uneven times: dt columns
+        kw = dict(E=[2, 3], dt=True, allowMissing=True, saveManifolds=True, full=True)
+        y = co = None
+    else:
+        t, x, y = workloads.coupled_logistic(600, seed=4)
+        co = np.roll(x, 7)
+        kw = dict(E=3, library=[50, 200], numReps=2, seed=9, copredict=co, saveManifolds=True)
+    g = fedm.edm(t, x, y, ctx=ctx, **kw)
+    assert g["rc"] == 0
+    a = edm_oracle.normalise(t, x, y, **kw)
+    plan = fedm.host_plan(a)
+    assert len(g["Ms"]) == len(g["Mps"]) == len(plan["E"]) > 1
+    for f in range(len(plan["E"])):
+        o = edm_oracle.oracle_task(a, plan["lib"][f], plan["pred"][f], int(plan["E"][f]), int(plan["k"][f]),
+                                   copredict=bool(plan["copredict"][f]))
+        for got, want in ((g["Ms"][f], o["lib_manifold"]), (g["Mps"][f], o["pred_manifold"])):
+            want = np.where(want == 1e100, np.nan, want)
+            assert got.shape == want.shape, (f, got.shape, want.shape)
+            assert np.array_equal(got, want, equal_nan=True), f
+    if case == "ccm_copredict":
+        assert any(plan["copredict"]) and not all(plan["copredict"])
+
+
 def test_keep_going_stops_between_batches():
     """keep_going() (src/edm.cpp:572-591) is polled before every task batch:
     returning false stops the run with rc 1 (BREAK_HIT).  The context (its
