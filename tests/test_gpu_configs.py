@@ -290,6 +290,40 @@ def test_save_manifolds(ctx, case):
         assert any(plan["copredict"]) and not all(plan["copredict"])
 
 
+def test_easy_edm_call_sequence(ctx):
+    """The edm() calls easy_edm() makes (R/easy_edm.R:160-410), in order, on a
+    coupled logistic pair: explore E = 3..10; an S-map theta sweep with
+    k = Inf; S-map k = 20 with replicates; saveManifolds with full for the
+    largest library; CCM over 25 library sizes with k = Inf and shuffle; a
+    replicate distribution at a small library and the final library.  Replicate
+    counts are reduced from easy_edm's (1000) to keep the oracle quick.  Every
+    call's statistics must be the oracle's."""
+    t, x, y = workloads.coupled_logistic(500, seed=21)
+
+    def both(first, second=None, **kw):
+        g = fedm.edm(t, first, second, ctx=ctx, **kw)
+        o = edm_oracle.oracle_edm(t, first, second, numThreads=16, **kw)
+        _stats_close(g, o)
+        return g
+
+    r = both(x, E=list(range(3, 11)))
+    E_best = int(r["stats"]["E"][int(np.nanargmax(r["stats"]["rho"]))])
+    thetas = list(np.linspace(0, 8, 9))
+    r = both(x, E=E_best, theta=thetas, algorithm="smap", k=float("inf"))
+    opt_theta = float(r["stats"]["theta"][int(np.nanargmax(r["stats"]["rho"]))])
+    both(x, E=E_best, theta=0.0, numReps=8, k=20, algorithm="smap")
+    both(x, E=E_best, theta=opt_theta, numReps=8, k=20, algorithm="smap")
+    m = fedm.edm(t, y, ctx=ctx, E=E_best, algorithm="simplex", full=True, saveManifolds=True)
+    lib_max = m["Ms"][0].shape[0]
+    assert m["rc"] == 0 and lib_max > 400 and m["Ms"][0].shape[1] == E_best
+    libraries = [int(v) for v in np.ceil(np.linspace(10, lib_max, 25))]
+    both(y, x, E=E_best, library=libraries, algorithm="simplex", k=float("inf"), shuffle=True)
+    small = max(E_best + 2, lib_max // 10)
+    both(y, x, E=E_best, library=small, numReps=20, theta=opt_theta, algorithm="simplex", k=float("inf"),
+         shuffle=True)
+    both(y, x, E=E_best, library=lib_max, theta=opt_theta, algorithm="simplex", k=float("inf"), shuffle=True)
+
+
 def test_keep_going_stops_between_batches():
     """keep_going() (src/edm.cpp:572-591) is polled before every task batch:
     returning false stops the run with rc 1 (BREAK_HIT).  The context (its
