@@ -613,9 +613,15 @@ void run_group(Context& ctx, const Options& o, const std::vector<Task>& tasks, c
       ctx.timing.kernel_launches += 1;
     }
     if (with_all) {
-      launch_all_mode(g, c, ctx.num_sms, max_nlib_all, s, gram_terms);
+      float* rdist = nullptr;
+      double* means = nullptr;
+      if (gram_terms) {
+        rdist = (float*)ctx.buf("df_rdist", (size_t)(c.p_end - c.p_begin) * max_nlib_all * 4);
+        means = (double*)ctx.buf("df_means", (size_t)(c.p_end - c.p_begin) * 8);
+      }
+      launch_all_mode(g, c, ctx.num_sms, max_nlib_all, s, gram_terms, rdist, means);
       ctx.check("all_mode");
-      ctx.timing.kernel_launches += o.algorithm == 1 ? 2 : 1;
+      ctx.timing.kernel_launches += o.algorithm == 1 ? (gram_terms ? 3 : 2) : 1;
     }
   };
 

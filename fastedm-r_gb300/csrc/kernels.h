@@ -103,10 +103,11 @@ void launch_knn_exact(const GroupParams& g, const ChunkBuffers& c, int num_sms, 
 void launch_simplex_nn(const GroupParams& g, const ChunkBuffers& c, cudaStream_t s);
 void launch_smap_nn(const GroupParams& g, const ChunkBuffers& c, int num_sms, cudaStream_t s);
 void launch_all_mode(const GroupParams& g, const ChunkBuffers& c, int num_sms, long long max_nlib, cudaStream_t s,
-                     const float2* gram_terms = nullptr);
+                     const float2* gram_terms = nullptr, float* rdist = nullptr, double* means = nullptr);
 // FAST precision, k = all S-map (E_a <= 8): per library-pool row the
 // n(n+1)/2 + n Gram and right-hand-side products as float pairs; *bad is set
-// when a product is not below 1e30 in magnitude.
+// when a product is not below 1e30 in magnitude.  launch_all_mode then also
+// takes rdist [chunk x max_nlib] floats and means [chunk] doubles of scratch.
 int gram_terms_per_row(int Ea);
 void launch_gram_terms(const GroupParams& g, long long pool_size, float2* P, int* bad, cudaStream_t s);
 void launch_stats(const GroupParams& g, const DevTask* tasks_host_unused, int n_tasks, double* rho, double* mae,

@@ -764,9 +764,38 @@ __global__ void gram_terms_kernel(GroupParams g, long long pool_size, float2* P,
     atomicExch(bad, 1);
 }
 
+// Once per point for every theta: the mean distance (a warp reduction, not
+// the reference's sequential sum: this path is not bit-exact anyway) and the
+// distances in FP32 (-1: not a neighbour).
+__global__ void all_df_prep_kernel(GroupParams g, ChunkBuffers c, long long max_nlib, float* rdist, double* means)
+{
+  const int lane = threadIdx.x & 31;
+  const long long q = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const long long chunk = c.p_end - c.p_begin;
+  if (q >= chunk)
+    return;
+  const long long p = point_of(c, q);
+  const DevTask T = g.tasks[find_task(g, p)];
+  if (!T.all_mode || c.status[q] != PT_OK)
+    return;
+  const double* dq = c.scratch + q * max_nlib;
+  float* rq = rdist + q * max_nlib;
+  double sum = 0;
+  for (int i = lane; i < T.n_lib; i += 32) {
+    const double d = dq[i];
+    rq[i] = d >= 0 ? (float)d : -1.f;
+    if (d >= 0)
+      sum += d;
+  }
+  for (int o = 16; o > 0; o >>= 1)
+    sum += __shfl_xor_sync(FULL, sum, o);
+  if (lane == 0)
+    means[q] = sum / (double)c.nn_count[q];
+}
+
 template<int EA>
 __global__ void __launch_bounds__(128) all_smap_df_kernel(GroupParams g, ChunkBuffers c, long long max_nlib,
-                                                           const float2* P)
+                                                           const float2* P, const float* rdist, const double* means)
 {
   constexpr int n = EA + 1, NA = n * (n + 1) / 2, NP = NA + n;
   const long long chunk = c.p_end - c.p_begin;
@@ -784,24 +813,18 @@ __global__ void __launch_bounds__(128) all_smap_df_kernel(GroupParams g, ChunkBu
     early_rc(g, T.task, st, t);
     return;
   }
-  const double* dq = c.scratch + q * max_nlib;
-  const int ke = c.nn_count[q];
-  double mean = 0;
-  for (int i = 0; i < T.n_lib; i++)
-    if (dq[i] >= 0)
-      mean += dq[i];
-  mean /= (double)ke;
-  const float c2 = (float)(-2.0 * g.thetas[t] / mean);
+  const float* rq = rdist + q * max_nlib;
+  const float c2 = (float)(-2.0 * g.thetas[t] / means[q]);
   float S[NP], Cr[NP];
 #pragma unroll
   for (int e = 0; e < NP; e++)
     S[e] = Cr[e] = 0.f;
   const float2* pool = P + (size_t)T.lib_off * NP;
   for (int i = 0; i < T.n_lib; i++) {
-    const double d = dq[i];
-    if (d < 0)
+    const float d = rq[i];
+    if (d < 0.f)
       continue;
-    const float om = expf(__fmul_rn(c2, (float)d));
+    const float om = expf(__fmul_rn(c2, d));
     const float2* pr = pool + (size_t)i * NP;
 #pragma unroll
     for (int e = 0; e < NP; e++) {
@@ -1035,7 +1058,7 @@ void launch_gram_terms(const GroupParams& g, long long pool_size, float2* P, int
 }
 
 void launch_all_mode(const GroupParams& g, const ChunkBuffers& c, int num_sms, long long max_nlib, cudaStream_t s,
-                     const float2* gram_terms)
+                     const float2* gram_terms, float* rdist, double* means)
 {
   int per_warp;
   const int w = all_warps_per_block(g.Ea, per_warp);
@@ -1050,16 +1073,17 @@ void launch_all_mode(const GroupParams& g, const ChunkBuffers& c, int num_sms, l
   if (total <= 0)
     return;
   const int fb = (int)((total + 127) / 128);
-  if (g.algorithm == 1 && g.Ea <= 8 && gram_terms) {
+  if (g.algorithm == 1 && g.Ea <= 8 && gram_terms && rdist && means) {
+    all_df_prep_kernel<<<(int)((chunk * 32 + 127) / 128), 128, 0, s>>>(g, c, max_nlib, rdist, means);
     switch (g.Ea) {
-      case 1: all_smap_df_kernel<1><<<fb, 128, 0, s>>>(g, c, max_nlib, gram_terms); return;
-      case 2: all_smap_df_kernel<2><<<fb, 128, 0, s>>>(g, c, max_nlib, gram_terms); return;
-      case 3: all_smap_df_kernel<3><<<fb, 128, 0, s>>>(g, c, max_nlib, gram_terms); return;
-      case 4: all_smap_df_kernel<4><<<fb, 128, 0, s>>>(g, c, max_nlib, gram_terms); return;
-      case 5: all_smap_df_kernel<5><<<fb, 128, 0, s>>>(g, c, max_nlib, gram_terms); return;
-      case 6: all_smap_df_kernel<6><<<fb, 128, 0, s>>>(g, c, max_nlib, gram_terms); return;
-      case 7: all_smap_df_kernel<7><<<fb, 128, 0, s>>>(g, c, max_nlib, gram_terms); return;
-      case 8: all_smap_df_kernel<8><<<fb, 128, 0, s>>>(g, c, max_nlib, gram_terms); return;
+      case 1: all_smap_df_kernel<1><<<fb, 128, 0, s>>>(g, c, max_nlib, gram_terms, rdist, means); return;
+      case 2: all_smap_df_kernel<2><<<fb, 128, 0, s>>>(g, c, max_nlib, gram_terms, rdist, means); return;
+      case 3: all_smap_df_kernel<3><<<fb, 128, 0, s>>>(g, c, max_nlib, gram_terms, rdist, means); return;
+      case 4: all_smap_df_kernel<4><<<fb, 128, 0, s>>>(g, c, max_nlib, gram_terms, rdist, means); return;
+      case 5: all_smap_df_kernel<5><<<fb, 128, 0, s>>>(g, c, max_nlib, gram_terms, rdist, means); return;
+      case 6: all_smap_df_kernel<6><<<fb, 128, 0, s>>>(g, c, max_nlib, gram_terms, rdist, means); return;
+      case 7: all_smap_df_kernel<7><<<fb, 128, 0, s>>>(g, c, max_nlib, gram_terms, rdist, means); return;
+      case 8: all_smap_df_kernel<8><<<fb, 128, 0, s>>>(g, c, max_nlib, gram_terms, rdist, means); return;
       default: break;
     }
   }
