@@ -74,11 +74,35 @@ void Context::reset_timing()
 Context::~Context()
 {
   cudaSetDevice(device);
+  if (stream)
+    cudaStreamSynchronize(stream);
   for (auto& kv : bufs_)
     if (kv.second.p)
       cudaFree(kv.second.p);
+  for (auto& kv : host_bufs_)
+    if (kv.second.p)
+      cudaFreeHost(kv.second.p);
   if (stream)
     cudaStreamDestroy(stream);
+}
+
+void* Context::host_buf(const std::string& name, size_t bytes)
+{
+  DevBuf& b = host_bufs_[name];
+  if (bytes == 0)
+    bytes = 16;
+  if (b.cap < bytes) {
+    if (b.p) {
+      ck(cudaStreamSynchronize(stream), "sync before realloc");
+      ck(cudaFreeHost(b.p), "cudaFreeHost");
+      b.p = nullptr;
+      b.cap = 0;
+    }
+    size_t want = bytes + bytes / 8;
+    ck(cudaHostAlloc(&b.p, want, cudaHostAllocDefault), ("cudaHostAlloc " + name).c_str());
+    b.cap = want;
+  }
+  return b.p;
 }
 
 void* Context::buf(const std::string& name, size_t bytes)
@@ -377,10 +401,12 @@ void run_group(Context& ctx, const Options& o, const std::vector<Task>& tasks, c
   double R = 0;
   const bool mixed_group = mixed_eligible(ctx, o, job, center, R);
 
-  // task table and row pools
+  // task table and row pools: offsets first, then the distinct lists copied
+  // in parallel into pinned host buffers, uploaded without staging
   std::vector<DevTask> dt(nT);
   std::unordered_map<const std::vector<int>*, int> lib_off, pred_off;
-  std::vector<int> lib_pool, pred_pool;
+  std::vector<const std::vector<int>*> lib_src, pred_src;
+  long long lib_total = 0, pred_total = 0;
   long long P = 0, max_nlib_all = 1;
   int kcap = 1, kmix = 0;
   bool any_finite = false, any_all = false, any_coeffs = false, any_mixed = false;
@@ -390,13 +416,15 @@ void run_group(Context& ctx, const Options& o, const std::vector<Task>& tasks, c
     const std::vector<int>* Pl = job.pred_lists[j];
     auto it = lib_off.find(L);
     if (it == lib_off.end()) {
-      it = lib_off.emplace(L, (int)lib_pool.size()).first;
-      lib_pool.insert(lib_pool.end(), L->begin(), L->end());
+      it = lib_off.emplace(L, (int)lib_total).first;
+      lib_src.push_back(L);
+      lib_total += (long long)L->size();
     }
     auto it2 = pred_off.find(Pl);
     if (it2 == pred_off.end()) {
-      it2 = pred_off.emplace(Pl, (int)pred_pool.size()).first;
-      pred_pool.insert(pred_pool.end(), Pl->begin(), Pl->end());
+      it2 = pred_off.emplace(Pl, (int)pred_total).first;
+      pred_src.push_back(Pl);
+      pred_total += (long long)Pl->size();
     }
     DevTask& d = dt[j];
     d.point_base = P;
@@ -434,12 +462,35 @@ void run_group(Context& ctx, const Options& o, const std::vector<Task>& tasks, c
     throw Error{ RC_NOT_IMPLEMENTED, "embedding too wide for the all-neighbour S-map" };
 
   DevTask* d_tasks = (DevTask*)ctx.buf("tasks", dt.size() * sizeof(DevTask));
-  int* d_lib = (int*)ctx.buf("lib_pool", std::max<size_t>(lib_pool.size(), 1) * 4);
-  int* d_pred = (int*)ctx.buf("pred_pool", std::max<size_t>(pred_pool.size(), 1) * 4);
+  if (lib_total > INT_MAX || pred_total > INT_MAX)
+    throw Error{ RC_NOT_IMPLEMENTED, "row pool of a task batch above 2^31 rows" };
+  auto fill_pool = [&](const std::vector<const std::vector<int>*>& src, long long total, const char* name) {
+    int* h = (int*)ctx.host_buf(name, (size_t)std::max<long long>(total, 1) * 4);
+    const int nth_copy = (int)std::min<long long>(8, std::max<long long>(1, total >> 20));
+    auto copy_range = [&](int w) {
+      long long off = 0;
+      for (size_t l = 0; l < src.size(); l++) {
+        if ((int)(l % nth_copy) == w && !src[l]->empty())
+          std::memcpy(h + off, src[l]->data(), src[l]->size() * 4);
+        off += (long long)src[l]->size();
+      }
+    };
+    std::vector<std::thread> pool;
+    for (int w = 1; w < nth_copy; w++)
+      pool.emplace_back(copy_range, w);
+    copy_range(0);
+    for (auto& th : pool)
+      th.join();
+    return h;
+  };
+  const int* h_lib = fill_pool(lib_src, lib_total, "lib_pool");
+  const int* h_pred = fill_pool(pred_src, pred_total, "pred_pool");
+  int* d_lib = (int*)ctx.buf("lib_pool", (size_t)std::max<long long>(lib_total, 1) * 4);
+  int* d_pred = (int*)ctx.buf("pred_pool", (size_t)std::max<long long>(pred_total, 1) * 4);
   double* d_thetas = (double*)ctx.buf("thetas", nth * 8);
   ctx.upload(d_tasks, dt.data(), dt.size() * sizeof(DevTask));
-  ctx.upload(d_lib, lib_pool.data(), lib_pool.size() * 4);
-  ctx.upload(d_pred, pred_pool.data(), pred_pool.size() * 4);
+  ctx.upload(d_lib, h_lib, (size_t)lib_total * 4);
+  ctx.upload(d_pred, h_pred, (size_t)pred_total * 4);
   ctx.upload(d_thetas, o.thetas.data(), nth * 8);
 
   GroupParams g{};
@@ -504,7 +555,7 @@ void run_group(Context& ctx, const Options& o, const std::vector<Task>& tasks, c
   const float2* gram_terms = nullptr;
   if (ctx.precision == FEDM_PRECISION_FAST && any_all && o.algorithm == 1 && Ea <= 8 && !o.has_missing &&
       !o.low_memory) {
-    const long long pool = (long long)lib_pool.size();
+    const long long pool = lib_total;
     const long long bytes = pool * gram_terms_per_row(Ea) * (long long)sizeof(float2);
     if (pool > 0 && bytes <= (2LL << 30)) {
       float2* P = (float2*)ctx.buf("gram_terms", (size_t)bytes);

@@ -43,12 +43,15 @@ public:
   void reset_timing();
   // Grow-only named device buffers (the context's memory pool).
   void* buf(const std::string& name, size_t bytes);
+  // Grow-only named pinned host buffers, for uploads that need no staging;
+  // the caller must not refill one while a copy from it is in flight.
+  void* host_buf(const std::string& name, size_t bytes);
   void upload(void* dst, const void* src, size_t bytes);
   void download(void* dst, const void* src, size_t bytes);
   void check(const char* what);
 
 private:
-  std::map<std::string, DevBuf> bufs_;
+  std::map<std::string, DevBuf> bufs_, host_bufs_;
 };
 
 // Everything run_command returns, in host memory.
