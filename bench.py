@@ -183,7 +183,8 @@ def run_ours(a):
     def step():
         tot = dict(device_ms=0.0, knn_kernel_ms=0.0, knn_launches=0, predictions=0, distance_pairs=0,
                    h2d_bytes=0, d2h_bytes=0, fallback_points=0, kernel_launches=0, fp64_ops=0, host_ms=0.0,
-                   list_wait_ms=0.0, setup_ms=0.0, finish_ms=0.0, exact_points=0, autotune_probes=0, wall_ms=0.0)
+                   list_wait_ms=0.0, setup_ms=0.0, finish_ms=0.0, exact_points=0, autotune_probes=0, prep_ms=0.0,
+                   manifold_ms=0.0, wall_ms=0.0)
         base_keys = [k for k in tot if k != "wall_ms"]
         rhos = []
         for args, alg in zip(calls, ("simplex", "smap")):
@@ -282,7 +283,8 @@ def run_ours(a):
         },
         "e2e": {"value": e2e, "unit": "predictions/s", "h2d_bytes_per_step": int(s0["h2d_bytes"]),
                 "d2h_bytes_per_step": int(s0["d2h_bytes"]), "wall_ms_per_step": wall_s_max / a.steps * 1e3,
-                "host_ms_per_step": {k: mean_of(k) for k in ("host_ms", "list_wait_ms", "setup_ms", "finish_ms")}},
+                "host_ms_per_step": {k: mean_of(k) for k in ("host_ms", "prep_ms", "manifold_ms", "list_wait_ms",
+                                                             "setup_ms", "finish_ms")}},
         "gpu_launches": int(sum(s["kernel_launches"] for s in per_step)),
         "roofline": {
             "kernel": form_kernel(s0["smap_mixed_form"], "smap") + " (FP32 scan + FP64 re-rank + JacobiSVD solve)",
@@ -421,6 +423,7 @@ def run_config(a):
     barrier(world)
     dev = wall = 0.0
     preds = launches = fallback = exact = 0
+    host = {k: 0.0 for k in ("host_ms", "prep_ms", "manifold_ms", "list_wait_ms", "setup_ms", "finish_ms")}
     with Clocks(local) as clk:
         for _ in range(a.steps):
             for tm, ws in step():
@@ -430,6 +433,8 @@ def run_config(a):
                 launches += tm["kernel_launches"]
                 fallback += tm.get("fallback_points", 0)
                 exact += tm.get("exact_points", 0)
+                for k in host:
+                    host[k] += tm.get(k, 0.0)
             flush_l2(local)
     dev = allreduce_max(world, dev)
     wall = allreduce_max(world, wall)
@@ -442,7 +447,8 @@ def run_config(a):
         preds * world / dev, "unit": "predictions/s", "n_gpus": world, "steps": a.steps, "warmup": max(3, a.warmup),
         "ms_per_step": dev / a.steps * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "fp32+fp64", "data": "synthetic (seeded generators)", "config": cfg,
-        "e2e": {"value": preds * world / wall, "unit": "predictions/s", "wall_ms_per_step": wall / a.steps * 1e3},
+        "e2e": {"value": preds * world / wall, "unit": "predictions/s", "wall_ms_per_step": wall / a.steps * 1e3,
+                "host_ms_per_step": {k: v / a.steps for k, v in host.items()}},
         "gpu_launches": launches, "predictions_per_step": preds // a.steps,
         "fallback_points_per_step": fallback // a.steps, "exact_points_per_step": exact // a.steps,
         "roofline": None, "cpu_baseline": None,

@@ -347,15 +347,42 @@ bool mixed_eligible(const Context& ctx, const Options& o, const GroupJob& job, s
     return false;
   const int Ea = job.Ea;
   std::vector<double> lo(Ea, INFINITY), hi(Ea, -INFINITY);
+  // bounding box of the listed rows, split over host threads for long lists
+  // (minimum and maximum do not depend on the split)
+  const int hw = std::max(1, std::min(16, (int)std::thread::hardware_concurrency()));
   auto scan = [&](const std::vector<double>& F, const std::vector<int>& rows) {
-    for (int r : rows)
-      for (int j = 0; j < Ea; j++) {
-        const double v = F[(size_t)r * Ea + j];
-        if (v == MISSING_D || !std::isfinite(v))
-          return false;
-        lo[j] = std::min(lo[j], v);
-        hi[j] = std::max(hi[j], v);
+    const long long n = (long long)rows.size();
+    const int nt = (int)std::max<long long>(1, std::min<long long>(hw, n / 16384));
+    std::vector<std::vector<double>> tlo(nt, lo), thi(nt, hi);
+    std::vector<uint8_t> ok(nt, 1);
+    auto work = [&](int w) {
+      for (long long q = n * w / nt; q < n * (w + 1) / nt; q++) {
+        const double* row = &F[(size_t)rows[q] * Ea];
+        for (int j = 0; j < Ea; j++) {
+          const double v = row[j];
+          if (v == MISSING_D || !std::isfinite(v)) {
+            ok[w] = 0;
+            return;
+          }
+          tlo[w][j] = std::min(tlo[w][j], v);
+          thi[w][j] = std::max(thi[w][j], v);
+        }
       }
+    };
+    std::vector<std::thread> pool;
+    for (int w = 1; w < nt; w++)
+      pool.emplace_back(work, w);
+    work(0);
+    for (auto& th : pool)
+      th.join();
+    for (int w = 0; w < nt; w++) {
+      if (!ok[w])
+        return false;
+      for (int j = 0; j < Ea; j++) {
+        lo[j] = std::min(lo[j], tlo[w][j]);
+        hi[j] = std::max(hi[j], thi[w][j]);
+      }
+    }
     return true;
   };
   std::vector<const std::vector<int>*> seen_l, seen_p;
@@ -1045,11 +1072,13 @@ double* device_manifold(Context& ctx, Manifolds& M, const Generator& g, const Ro
   auto it = M.dev.find(key);
   if (it != M.dev.end())
     return it->second;
+  const double t0 = now_ms();
   auto& h = M.host[key];
   h = build_manifold(g, rt, E, co, threads);
   double* d = (double*)ctx.buf("F_" + std::to_string(E) + (co ? "_co" : ""), std::max<size_t>(h.size(), 1) * 8);
   ctx.upload(d, h.data(), h.size() * 8);
   M.dev[key] = d;
+  ctx.timing.manifold_ms += now_ms() - t0;
   return d;
 }
 
@@ -1091,6 +1120,7 @@ CommandResult run_command(Context& ctx, const fedm_args& a)
   if (plan.lazy.active)
     producer = std::make_unique<SplitProducer>(plan, rt.lib_target, threads);
   DevRows drows = upload_rows(ctx, gen, rt, o);
+  ctx.timing.prep_ms += now_ms() - t0;
 
   // row lists per mask (shared by every task that uses the mask); lazy
   // library lists are taken when their batch runs

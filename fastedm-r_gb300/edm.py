@@ -73,7 +73,8 @@ class Timing(C.Structure):
         ("h2d_bytes", C.c_longlong), ("d2h_bytes", C.c_longlong), ("fallback_points", C.c_int),
         ("kernel_launches", C.c_int), ("fp64_ops", C.c_longlong), ("list_wait_ms", C.c_double),
         ("setup_ms", C.c_double), ("finish_ms", C.c_double), ("exact_points", C.c_int),
-        ("mixed_form", C.c_int), ("autotune_probes", C.c_int),
+        ("mixed_form", C.c_int), ("autotune_probes", C.c_int), ("prep_ms", C.c_double),
+        ("manifold_ms", C.c_double),
     ]
 
 

@@ -220,6 +220,9 @@ typedef struct fedm_timing {
                                 specialised S-map (4 / 8 solver warps),
                                 4 the wide form (E_actual 9..16); -1 none    */
   int autotune_probes;       /* timed form probes of the autotuner          */
+  double prep_ms;            /* host time before the first batch: argument
+                                handling, usable rows, task plan, row tables */
+  double manifold_ms;        /* host time building and uploading manifolds  */
 } fedm_timing;
 
 int fedm_last_timing(const fedm_ctx* ctx, fedm_timing* out);

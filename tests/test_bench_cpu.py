@@ -35,7 +35,7 @@ class FakeContext:
         return dict(device_ms=100.0, knn_kernel_ms=90.0, knn_launches=1, host_ms=101.0, distance_pairs=10**9,
                     predictions=10**6, h2d_bytes=1000, d2h_bytes=100, fallback_points=3, kernel_launches=10,
                     fp64_ops=10**10, list_wait_ms=1.0, setup_ms=2.0, finish_ms=0.5, exact_points=1, mixed_form=1,
-                    autotune_probes=0)
+                    autotune_probes=0, prep_ms=0.3, manifold_ms=0.2)
 
     def close(self):
         pass
