@@ -19,7 +19,9 @@
 // The k-th true distance is at most hi = sqrt(s_k)/sqrt(1-g) + e, so every
 // true neighbour has s <= T = ((hi + e) * sqrt(1+g))^2 (widened by 1e-14).
 // If the C-th kept value exceeds T, every entry at or under T is in the list;
-// otherwise the point is handed to the exact kernels.  Entries under T are
+// otherwise the point goes on a fallback list with its T, and
+// knn_refine_kernel re-scans the library for the rows under T (the exact
+// kernels take a point with more than 1024 of them).  Entries under T are
 // re-scored in FP64 with the reference's operation order
 // (src/distances.cpp:194-225), so neighbour distances and their
 // (distance, index) order are the FP64 bits.  A positive FP32 distance implies

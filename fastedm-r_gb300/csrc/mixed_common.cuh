@@ -84,13 +84,13 @@ struct Cand
 };
 
 // Settles one point's neighbour list from its FP32 candidates: certifies the
-// list against the error margin (else queues the point for the exact
-// kernels), re-scores the candidates in FP64 in the reference's operation
+// list against the error margin (else queues the point and its bound for
+// knn_refine_kernel), re-scores the candidates in FP64 in the reference's operation
 // order, orders them by (distance, library index) -- library order when
 // every valid neighbour is used -- and applies the k rules of
 // src/edm.cpp:565-639.  Returns true with keff, rows (library manifold rows)
 // and cd (their FP64 distances) set when a forecast follows; false when the
-// point was handed to the exact kernels or has no valid neighbour.  ops
+// point went on the fallback list or has no valid neighbour.  ops
 // accumulates the FP64 operations.
 template<int EA, int C>
 __device__ __forceinline__ bool prepare_point(const GroupParams& g, const MixedRun& m, const DevTask& T, long long p,
