@@ -48,7 +48,8 @@ def form_kernel(form, alg):
             1: f"knn_one_kernel<E=4,C=8,{alg},6 CTAs/SM>",
             2: "knn_smap_ws_kernel<E=4,C=8,4 solver warps>",
             3: "knn_smap_ws_kernel<E=4,C=8,8 solver warps>",
-            4: f"knn_one_kernel wide form ({alg})"}.get(int(form), "none")
+            4: f"knn_one_kernel wide form ({alg})",
+            5: f"knn_one_kernel<E=4,C=16,{alg},4 CTAs/SM>"}.get(int(form), "none")
 
 
 def hbm_peak():

@@ -25,6 +25,7 @@ CU_FLAGS = {
     "kernels_util.cu": [],
     "kernels_mixed.cu": [],
     "kernels_wide.cu": [],
+    "kernels_one16.cu": [],
     "static_entry.cu": [],
     "kernels_adjoint.cu": [],
 }

@@ -51,12 +51,18 @@ Context::Context(int dev) : device(dev)
   ck(cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, dev), "cudaDeviceGetAttribute");
   if (const char* v = std::getenv("FEDM_MIXED_KERNEL")) {
     static const std::pair<const char*, int> forms[] = {
-      { "one6", MIXED_ONE6 }, { "fused2", MIXED_FUSED2 }, { "ws4", MIXED_WS4 }, { "ws8", MIXED_WS8 }
+      { "one6", MIXED_ONE6 }, { "fused2", MIXED_FUSED2 }, { "ws4", MIXED_WS4 }, { "ws8", MIXED_WS8 },
+      { "one16", MIXED_ONE16 }
     };
     for (const auto& f : forms)
       if (std::strcmp(v, f.first) == 0) {
-        mixed_form = f.second;
-        autotune = false;  // a named form is used as given
+        // a named form is used as given: one16 names the 7 <= k <= 14 form,
+        // fused2 both, the others the k <= 6 form
+        if (f.second == MIXED_ONE16 || f.second == MIXED_FUSED2)
+          mixed_form16 = f.second;
+        if (f.second != MIXED_ONE16)
+          mixed_form = f.second;
+        autotune = false;
       }
   }
   if (const char* v = std::getenv("FEDM_AUTOTUNE"))
@@ -708,11 +714,16 @@ void run_group(Context& ctx, const Options& o, const std::vector<Task>& tasks, c
     const bool wide = Ea > 8;
     const int S = Ea <= 4 ? 4 : (Ea <= 8 ? 8 : 16);
     const int C = wide ? 32 : (kmix <= 6 ? 8 : 16);
-    // one point per thread for k <= 6: the default form, and the simplex's
-    // when the S-map uses the warp-specialised kernel
+    // one point per thread: for k <= 6 the default form (and the simplex's
+    // when the S-map uses the warp-specialised kernel); for 7 <= k <= 14 the
+    // MIXED_ONE16 form
     auto is_one = [&](int form) {
+      if (wide)
+        return false;
+      if (C == 16)
+        return form == MIXED_ONE16;
       const bool ws = o.algorithm == 1 && (form == MIXED_WS4 || form == MIXED_WS8);
-      return !wide && C == 8 && form != MIXED_FUSED2 && !ws;
+      return form != MIXED_FUSED2 && form != MIXED_ONE16 && !ws;
     };
     auto points_per_item = [&](int form) { return (wide || is_one(form)) ? WIDE_POINTS : MIX_POINTS; };
     const long long nrows = (long long)rows.n_rows;
@@ -779,6 +790,8 @@ void run_group(Context& ctx, const Options& o, const std::vector<Task>& tasks, c
       m.form = form;
       if (wide)
         launch_knn_wide(g, m, ctx.num_sms, s);
+      else if (is_one(form) && C == 16)
+        launch_mixed_one16(g, m, ctx.num_sms, s);
       else if (is_one(form))
         launch_mixed_one(g, m, ctx.num_sms, s);
       else
@@ -790,8 +803,8 @@ void run_group(Context& ctx, const Options& o, const std::vector<Task>& tasks, c
       m.item_begin = 0;
       m.item_end = m.n_items;
     };
-    int form = ctx.mixed_form;
-    if (!wide && C == 8 && ctx.autotune) {
+    int form = C == 16 ? ctx.mixed_form16 : ctx.mixed_form;
+    if (!wide && ctx.autotune) {
       // Autotuner: every form gives the same bits, so the first batch of
       // each (algorithm, E_a, k) with enough points times each candidate
       // form on the same leading tasks (about two waves of the default
@@ -808,7 +821,9 @@ void run_group(Context& ctx, const Options& o, const std::vector<Task>& tasks, c
         form = hit->second;
       } else if (mixed_points >= probe_points) {
         std::vector<int> cands{ MIXED_ONE6, MIXED_FUSED2 };
-        if (o.algorithm == 1)
+        if (C == 16)
+          cands = { MIXED_ONE16, MIXED_FUSED2 };
+        else if (o.algorithm == 1)
           cands.push_back(MIXED_WS8);
         std::vector<float> best(cands.size(), INFINITY);
         for (int f : cands) {
@@ -858,7 +873,7 @@ void run_group(Context& ctx, const Options& o, const std::vector<Task>& tasks, c
     if (wide)
       ctx.timing.mixed_form = MIXED_WIDE;
     else if (is_one(form))
-      ctx.timing.mixed_form = MIXED_ONE6;
+      ctx.timing.mixed_form = C == 16 ? MIXED_ONE16 : MIXED_ONE6;
     else
       ctx.timing.mixed_form = (o.algorithm == 1 && (form == MIXED_WS4 || form == MIXED_WS8)) ? form : MIXED_FUSED2;
     run_items(items_of(points_per_item(form), LLONG_MAX));

@@ -29,9 +29,10 @@ public:
   // Kernel form of the mixed path (MixedForm in kernels.h); the environment
   // variable FEDM_MIXED_KERNEL (one6, fused2, ws4, ws8) overrides it when
   // the context is created.
-  int mixed_form = MIXED_ONE6;
+  int mixed_form = MIXED_ONE6;     // for k <= 6
+  int mixed_form16 = MIXED_ONE16;  // for 7 <= k <= 14
   // With autotune on (the default; FEDM_AUTOTUNE=0 or a named form turns it
-  // off) the form for E_a <= 8, k <= 6 is chosen per (algorithm, E_a, k) by
+  // off) the form for E_a <= 8, k <= 14 is chosen per (algorithm, E_a, k) by
   // timing the candidates on the first batch large enough to measure.
   bool autotune = true;
   std::map<std::array<int, 3>, int> tuned_forms;

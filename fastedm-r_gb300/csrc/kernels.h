@@ -124,7 +124,8 @@ enum MixedForm
   MIXED_ONE6 = 1,    // knn_one_kernel: one point per thread, six CTAs per SM (40 registers)
   MIXED_WS4 = 2,     // S-map: knn_smap_ws_kernel, 8 scan warps, 4 FP64 solver warps
   MIXED_WS8 = 3,     // S-map: knn_smap_ws_kernel, 8 scan warps, 8 FP64 solver warps
-  MIXED_WIDE = 4     // knn_one_kernel's wide form (E_a 9..16), chosen by E_a; reported in timings only
+  MIXED_WIDE = 4,    // knn_one_kernel's wide form (E_a 9..16), chosen by E_a; reported in timings only
+  MIXED_ONE16 = 5    // 7 <= k <= 14: knn_one_kernel with 16 candidate slots, four CTAs per SM
 };
 
 // Mixed-precision neighbour scan for the common case (L2, no missing values,
@@ -179,6 +180,9 @@ void launch_knn_wide(const GroupParams& g, const MixedRun& m, int num_sms, cudaS
 // Simplex or S-map (E_a <= 8, k <= 6) in the MIXED_ONE6 form; work items of
 // 256 points.
 void launch_mixed_one(const GroupParams& g, const MixedRun& m, int num_sms, cudaStream_t s);
+
+// The same for 7 <= k <= 14 (MIXED_ONE16, kernels_one16.cu).
+void launch_mixed_one16(const GroupParams& g, const MixedRun& m, int num_sms, cudaStream_t s);
 
 // Differentiable S-map over every library neighbour (kernels_adjoint.cu).
 struct AdjointParams

@@ -1,0 +1,139 @@
+// One prediction point per thread: the scan, the work-item kernel and its
+// launcher, shared by kernels_wide.cu (k <= 6 at E_a <= 8, and the wide
+// embeddings) and kernels_one16.cu (7 <= k <= 14 at E_a <= 8).
+// A 256-thread CTA takes a work item of 256 points, stages library rows of
+// the centred FP32 manifold per tile as interleaved pairs, and every thread
+// scores two rows against its point per packed step.  Certification, the
+// FP64 re-rank in the reference's operation order and the forecast are
+// finalize_point's, so neighbours and forecasts are the FP64 path's bits.
+#pragma once
+
+#include "mixed_common.cuh"
+
+namespace fedm {
+
+namespace {
+
+// One point per thread: C candidate slots, float manifold row stride RS,
+// TR library rows per shared-memory tile, NT threads per CTA.
+template<int EA, int C, int RS, int TR, int NT>
+__device__ __forceinline__ void scan_item_one(const GroupParams& g, const MixedRun& m, const DevTask& T, int first,
+                                              int tid, float2* tile, Cand<C>& c0, int& prow0, bool& a0)
+{
+  const int pi0 = first + tid;
+  a0 = pi0 < T.n_pred;
+  prow0 = a0 ? g.pred_rows[T.pred_off + pi0] : 0;
+  // negated prediction coordinates, duplicated in both halves; an idle slot
+  // sits at 1e30 so its squared distances overflow to +inf and never enter
+  float2 na[EA];
+#pragma unroll
+  for (int j = 0; j < EA; j++) {
+    const float va = a0 ? -m.Fp32[(size_t)prow0 * RS + j] : -1e30f;
+    na[j] = make_float2(va, va);
+  }
+  float D0[C];
+  int I0[C];
+#pragma unroll
+  for (int j = 0; j < C; j++) {
+    D0[j] = INFINITY;
+    I0[j] = -1;
+  }
+  int z0 = 0;
+  int zi0[ZCAP];
+#pragma unroll
+  for (int j = 0; j < ZCAP; j++)
+    zi0[j] = -1;
+  for (int t0 = 0; t0 < T.n_lib; t0 += TR) {
+    const int cnt = min(TR, T.n_lib - t0);
+    const int npairs = (cnt + 1) >> 1;
+    __syncthreads();
+    for (int i = tid; i < 2 * npairs; i += NT) {
+      float* dst = reinterpret_cast<float*>(tile + (i >> 1) * EA) + (i & 1);
+      if (i < cnt) {
+        const float* src = m.F32 + (size_t)g.lib_rows[T.lib_off + t0 + i] * RS;
+#pragma unroll
+        for (int j = 0; j < EA; j++)
+          dst[2 * j] = src[j];
+      } else {
+#pragma unroll
+        for (int j = 0; j < EA; j++)
+          dst[2 * j] = 1e30f;  // padding row: never a candidate
+      }
+    }
+    __syncthreads();
+#pragma unroll 2
+    for (int ip = 0; ip < npairs; ip++) {
+      const float2* xr = tile + ip * EA;
+      float2 d = __fadd2_rn(xr[0], na[0]);
+      float2 sa = __fmul2_rn(d, d);
+#pragma unroll
+      for (int j = 1; j < EA; j++) {
+        d = __fadd2_rn(xr[j], na[j]);
+        sa = __ffma2_rn(d, d, sa);
+      }
+      if (fminf(sa.x, sa.y) < D0[C - 1]) {
+        const int li = t0 + 2 * ip;
+        offer<C>(D0, I0, z0, zi0, sa.x, li);
+        offer<C>(D0, I0, z0, zi0, sa.y, li + 1);
+      }
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < C; j++) {
+    c0.D[j] = D0[j];
+    c0.I[j] = I0[j];
+  }
+  c0.z = z0;
+#pragma unroll
+  for (int j = 0; j < ZCAP; j++)
+    c0.zi[j] = zi0[j];
+}
+
+template<int EA, int C, int RS, int TR, int ALG, int OCC, int NT = TPB>
+__global__ void __launch_bounds__(NT, OCC) knn_one_kernel(GroupParams g, MixedRun m)
+{
+  __shared__ __align__(16) float2 tile[(TR / 2) * EA];
+  __shared__ int s_item;
+  const int tid = threadIdx.x;
+  unsigned long long ops = 0;
+  for (;;) {
+    __syncthreads();
+    if (tid == 0)
+      s_item = m.item_begin + atomicAdd(m.counter, 1);
+    __syncthreads();
+    const int item = s_item;
+    if (item >= m.item_end) {
+      add_ops(m, ops);  // every thread of the CTA leaves here together
+      return;
+    }
+    const int2 it = m.items[item];
+    const DevTask T = g.tasks[it.x];
+    Cand<C> c0;
+    int prow0;
+    bool a0;
+    scan_item_one<EA, C, RS, TR, NT>(g, m, T, it.y, tid, tile, c0, prow0, a0);
+    if (a0) {
+      const Cand<C> c = c0;
+      ops += finalize_point<EA, C, ALG>(g, m, T, T.point_base + it.y + tid, prow0, c);
+    }
+  }
+}
+
+template<int EA, int C, int RS, int TR, int ALG, int OCC, int NT = TPB>
+void launch_one(const GroupParams& g, const MixedRun& m, int num_sms, cudaStream_t s)
+{
+  int per_sm = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, knn_one_kernel<EA, C, RS, TR, ALG, OCC, NT>, NT, 0);
+  if (per_sm < 1)
+    per_sm = 1;
+  long long blocks = (long long)num_sms * per_sm;
+  if (blocks > m.item_end - m.item_begin)
+    blocks = m.item_end - m.item_begin;
+  if (blocks < 1)
+    blocks = 1;
+  knn_one_kernel<EA, C, RS, TR, ALG, OCC, NT><<<(int)blocks, NT, 0, s>>>(g, m);
+}
+
+} // namespace
+
+} // namespace fedm

@@ -218,7 +218,9 @@ typedef struct fedm_timing {
                                 two points per thread, 1 one point per
                                 thread at six CTAs per SM, 2 / 3 warp-
                                 specialised S-map (4 / 8 solver warps),
-                                4 the wide form (E_actual 9..16); -1 none    */
+                                4 the wide form (E_actual 9..16), 5 one
+                                point per thread with 16 candidate slots
+                                (7 <= k <= 14); -1 none                      */
   int autotune_probes;       /* timed form probes of the autotuner          */
   double prep_ms;            /* host time before the first batch: argument
                                 handling, usable rows, task plan, row tables */

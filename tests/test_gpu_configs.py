@@ -188,6 +188,34 @@ def test_mixed_kernel_forms_agree(form, algorithm, monkeypatch):
 
 
 @pytest.mark.parametrize("algorithm", ["simplex", "smap"])
+@pytest.mark.parametrize("form", ["one16", "fused2"])
+def test_k_up_to_16_forms_agree(form, algorithm, monkeypatch):
+    """For 7 <= k <= 14 the mixed path has two forms: one point per thread
+    with 16 candidate slots at four CTAs per SM, or two points per thread.
+    Both give the FP64 path's bits (k = 10 and k = 14, CCM replicates)."""
+    monkeypatch.setenv("FEDM_MIXED_KERNEL", form)
+    w = workloads.ccm_config(T=6000, reps=3, n_libs=5, hi=5000)
+    cm = fedm.Context(0, precision=fedm.PRECISION_MIXED)
+    c64 = fedm.Context(0, precision=fedm.PRECISION_FP64)
+    try:
+        for k in (10, 14):
+            kw = dict(E=4, k=k, library=w["libraries"], numReps=3, seed=w["seed"], algorithm=algorithm,
+                      theta=2.0 if algorithm == "smap" else 1.0, savePredictions=True,
+                      saveSMAPCoeffs=algorithm == "smap")
+            g = fedm.edm(w["t"], w["x"], w["y"], ctx=cm, **kw)
+            assert cm.timing()["mixed_form"] == (5 if form == "one16" else 0)
+            f = fedm.edm(w["t"], w["x"], w["y"], ctx=c64, **kw)
+            assert g["rc"] == f["rc"] == 0
+            assert np.array_equal(g["stats"]["rho"], f["stats"]["rho"], equal_nan=True)
+            assert np.array_equal(g["predictions"], f["predictions"], equal_nan=True)
+            if algorithm == "smap":
+                assert np.array_equal(g["coeffs"], f["coeffs"], equal_nan=True)
+    finally:
+        cm.close()
+        c64.close()
+
+
+@pytest.mark.parametrize("algorithm", ["simplex", "smap"])
 def test_autotuner_keeps_bits_and_its_choice(algorithm, monkeypatch):
     """With autotuning on (the default), the first batch of an (algorithm,
     E_a, k) large enough to measure times each candidate form on the same
@@ -223,6 +251,16 @@ def test_autotuner_keeps_bits_and_its_choice(algorithm, monkeypatch):
         assert np.array_equal(r["predictions"], f["predictions"], equal_nan=True)
         if algorithm == "smap":
             assert np.array_equal(r["coeffs"], f["coeffs"], equal_nan=True)
+    # k = 10: the 7 <= k <= 14 candidates (two points per thread, or one with
+    # 16 slots), tuned separately
+    monkeypatch.delenv("FEDM_MIXED_KERNEL", raising=False)
+    tuned = fedm.Context(0, precision=fedm.PRECISION_MIXED)
+    try:
+        fedm.edm(w["t"], w["x"], w["y"], ctx=tuned, **dict(kw, k=10))
+        t3 = tuned.timing()
+    finally:
+        tuned.close()
+    assert t3["autotune_probes"] == 4 and t3["mixed_form"] in (0, 5)
 
 
 @pytest.mark.parametrize("E", [5, 8])
