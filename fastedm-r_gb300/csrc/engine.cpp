@@ -497,6 +497,9 @@ void run_group(Context& ctx, const Options& o, const std::vector<Task>& tasks, c
   DevTask* d_tasks = (DevTask*)ctx.buf("tasks", dt.size() * sizeof(DevTask));
   if (lib_total > INT_MAX || pred_total > INT_MAX)
     throw Error{ RC_NOT_IMPLEMENTED, "row pool of a task batch above 2^31 rows" };
+  // an upload from these buffers by an earlier call that ended in an error
+  // may still be queued; normally the stream is idle here
+  ck(cudaStreamSynchronize(s), "sync");
   auto fill_pool = [&](const std::vector<const std::vector<int>*>& src, long long total, const char* name) {
     int* h = (int*)ctx.host_buf(name, (size_t)std::max<long long>(total, 1) * 4);
     const int nth_copy = (int)std::min<long long>(8, std::max<long long>(1, total >> 20));
