@@ -140,6 +140,38 @@ def test_fast_precision_smap_all_neighbours(T):
           f"exact {te['device_ms']:.1f}")
 
 
+@pytest.mark.parametrize("case", ["missing", "simplex_k_all", "wide_dt", "finite_k"])
+def test_fast_precision_elsewhere_is_mixed(case):
+    """FEDM_PRECISION_FAST changes only the S-map with every library row as a
+    neighbour, E_actual <= 8, no missing values.  Elsewhere (missing values,
+    simplex, dt embeddings wider than 8, a finite k) it gives MIXED's bits."""
+    t, x, _ = workloads.coupled_logistic(1500, seed=8)
+    x = x.copy()
+    kw = dict(E=3, k=float("inf"), theta=[0.0, 2.0], algorithm="smap", savePredictions=True)
+    if case == "missing":
+        x[::41] = np.nan
+        kw.update(allowMissing=True)
+    elif case == "simplex_k_all":
+        kw.update(algorithm="simplex")
+    elif case == "wide_dt":
+        t = t.astype(float).copy()
+        t[7::60] += 0.5
+        kw.update(E=5, dt=True)
+    else:
+        kw.update(k=12)
+    fast = fedm.Context(0, precision=fedm.PRECISION_FAST)
+    mixed = fedm.Context(0, precision=fedm.PRECISION_MIXED)
+    try:
+        f = fedm.edm(t, x, ctx=fast, **kw)
+        m = fedm.edm(t, x, ctx=mixed, **kw)
+    finally:
+        fast.close()
+        mixed.close()
+    assert f["rc"] == m["rc"] == 0
+    assert np.array_equal(f["stats"]["rho"], m["stats"]["rho"], equal_nan=True)
+    assert np.array_equal(f["predictions"], m["predictions"], equal_nan=True)
+
+
 def test_mixed_fp64_operation_count(ctx):
     """The mixed kernel counts the FP64 arithmetic of its re-rank and forecast
     stage (the roofline's numerator); the exact FP64 path reports none."""
