@@ -676,6 +676,7 @@ __global__ void __launch_bounds__(128) all_smap_kernel(GroupParams g, ChunkBuffe
     if (dq[i] >= 0)
       mean += dq[i];
   mean /= (double)ke;
+  const double ymean = rcp(mean);
   double W[n][n], bv[n];
 #pragma unroll
   for (int a = 0; a < n; a++) {
@@ -688,7 +689,7 @@ __global__ void __launch_bounds__(128) all_smap_kernel(GroupParams g, ChunkBuffe
     const double d = dq[i];
     if (d < 0)
       continue;
-    const double w = exp_rn(-theta * (d / mean));
+    const double w = exp_rn(-theta * dvd_r(d, mean, ymean));
     const int row = g.lib_rows[T.lib_off + i];
     const double* fr = g.F + (size_t)row * EA;
     const double yl = w * g.lib_target[row];

@@ -208,6 +208,7 @@ __device__ __noinline__ int smap_point_sm(const GroupParams& g, long long p, int
   for (int j = 0; j < keff; j++)
     mean = add(mean, cd[j]);
   mean = dvd(mean, (double)keff);
+  const double ymean = rcp(mean);
   const StridedMat<n> U{ uv, uv_stride }, V{ uv + n * n * uv_stride, uv_stride };
   for (int t = 0; t < g.n_thetas; t++) {
     const double theta = g.thetas[t];
@@ -220,7 +221,7 @@ __device__ __noinline__ int smap_point_sm(const GroupParams& g, long long p, int
         W[a][b] = 0;
     }
     for (int i = 0; i < keff; i++) {
-      const double w = exp_rn(mul(-theta, dvd(cd[i], mean)));
+      const double w = exp_rn(mul(-theta, dvd_r(cd[i], mean, ymean)));
       const int row = rows[i];
       double xr[n];
       xr[0] = w;

@@ -445,8 +445,9 @@ __device__ __noinline__ int finalize_point(const GroupParams& g, const MixedRun&
     for (int j = 1; j < keff; j++)
       minD = cd[j] < minD ? cd[j] : minD;
     double rel[C + ZCAP], tg[C + ZCAP];
+    const double ymin = rcp(minD);
     for (int j = 0; j < keff; j++) {
-      rel[j] = dvd(cd[j], minD);
+      rel[j] = dvd_r(cd[j], minD, ymin);
       tg[j] = g.lib_target[rows[j]];
     }
     for (int t = 0; t < g.n_thetas; t++) {
@@ -458,8 +459,9 @@ __device__ __noinline__ int finalize_point(const GroupParams& g, const MixedRun&
         sumw = add(sumw, w[j]);
       }
       double r = 0.0;
+      const double ysum = rcp(sumw);
       for (int j = 0; j < keff; j++)
-        r = add(r, mul(tg[j], dvd(w[j], sumw)));
+        r = add(r, mul(tg[j], dvd_r(w[j], sumw, ysum)));
       g.pred[(size_t)t * g.total_points + p] = r;
     }
     return ops + keff + g.n_thetas * keff * (EXP_OPS + 5);
@@ -491,6 +493,7 @@ __device__ __noinline__ int smap_point_local(const GroupParams& g, long long p, 
   for (int j = 0; j < keff; j++)
     mean = add(mean, cd[j]);
   mean = dvd(mean, (double)keff);
+  const double ymean = rcp(mean);
   for (int t = 0; t < g.n_thetas; t++) {
     const double theta = g.thetas[t];
     double W[n * n], bv[n], xs[n], U[n * n], V[n * n], sv[n], tmp[n];
@@ -499,7 +502,7 @@ __device__ __noinline__ int smap_point_local(const GroupParams& g, long long p, 
     for (int a = 0; a < n; a++)
       bv[a] = 0;
     for (int i = 0; i < keff; i++) {
-      const double w = exp_rn(mul(-theta, dvd(cd[i], mean)));
+      const double w = exp_rn(mul(-theta, dvd_r(cd[i], mean, ymean)));
       const int row = rows[i];
       double xr[n];
       xr[0] = w;

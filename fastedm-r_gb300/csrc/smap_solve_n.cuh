@@ -43,11 +43,12 @@ __device__ __forceinline__ void svd_solve_nm(double (&W)[N][N], const double (&b
   }
   if (scale == 0)
     scale = 1;
+  const double yscale = rcp(scale);
 #pragma unroll
   for (int i = 0; i < N; i++)
 #pragma unroll
     for (int j = 0; j < N; j++) {
-      W[i][j] = dvd(W[i][j], scale);
+      W[i][j] = dvd_r(W[i][j], scale, yscale);
       U(i, j) = i == j ? 1.0 : 0.0;
       V(i, j) = i == j ? 1.0 : 0.0;
     }
@@ -81,7 +82,7 @@ __device__ __forceinline__ void svd_solve_nm(double (&W)[N][N], const double (&b
             const double u = dvd(t, d);
             const double tmp = __dsqrt_rn(add(1.0, mul(u, u)));
             r1s = rcp(tmp);
-            r1c = dvd(u, tmp);
+            r1c = dvd_r(u, tmp, r1s);
             ops += 6;
           }
           const double n00 = add(mul(r1c, m00), mul(r1s, m10));
