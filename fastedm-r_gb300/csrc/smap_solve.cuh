@@ -31,8 +31,9 @@ __device__ __forceinline__ double rcp(double a) { return __drcp_rn(a); }
 // rounds to a/b (Markstein's theorem, y being within half an ulp of 1/b).
 // All products and remainders stay normal while both exponents lie within
 // +-500; other operands (zero, tiny, huge, not finite) take the division.
-// One multiply and four FMAs against the division's longer sequence; no
-// difference from dvd in 3.4e10 random pairs over every exponent range.
+// One multiply and four FMAs against the division's longer sequence;
+// tests/division_check.cu compares it with dvd on random pairs over every
+// exponent range.
 __device__ __forceinline__ double dvd_r(double a, double b, double y)
 {
   const unsigned ea = (unsigned)(__double2hiint(a) >> 20) & 0x7ffu;
