@@ -42,6 +42,65 @@ METRIC = "CCM S-map predictions/s: batched FP32+FP64-fix vs plain FP64 GPU @|Î”Ï
 SMAP_DRAM_BYTES_PER_POINT = 6428.5
 
 
+def concurrent_calls(fedm, w, a, local, rhos, steps=2):
+    """The step's two calls from two host threads on two contexts whose mixed
+    kernels share the SMs: the FP64-bound S-map capped at five resident CTAs
+    per SM, the FP32-bound simplex at one (fedm_set_ctas_per_sm).  The forms
+    are fixed (no autotuning: the two calls would disturb each other's
+    probes).  Reports the throughput and whether rho equals the sequential
+    run's."""
+    saved = os.environ.get("FEDM_AUTOTUNE")
+    os.environ["FEDM_AUTOTUNE"] = "0"
+    try:
+        ctxs = {}
+        for alg, cap in (("simplex", 1), ("smap", 5)):
+            ctxs[alg] = fedm.Context(local, precision=fedm.PRECISION_MIXED)
+            ctxs[alg].set_ctas_per_sm(cap)
+    finally:
+        if saved is None:
+            os.environ.pop("FEDM_AUTOTUNE", None)
+        else:
+            os.environ["FEDM_AUTOTUNE"] = saved
+    calls = {alg: ccm_args(fedm, w, alg, a.reps) for alg in ctxs}
+
+    def step():
+        out = {}
+
+        def run(alg):
+            out[alg] = ctxs[alg].run_command(calls[alg])
+
+        threads = [threading.Thread(target=run, args=(alg,)) for alg in ctxs]
+        t0 = time.perf_counter()
+        for th in threads:
+            th.start()
+        for th in threads:
+            th.join()
+        dt = time.perf_counter() - t0
+        for alg in ctxs:
+            if out[alg]["rc"] != 0:
+                raise RuntimeError(f"concurrent {alg} call rc={out[alg]['rc']}")
+        return dt, out
+
+    for _ in range(3):
+        step()
+        flush_l2(local)
+    times, out = [], None
+    for _ in range(steps):
+        dt, out = step()
+        times.append(dt)
+        flush_l2(local)
+    preds = sum(ctxs[alg].timing()["predictions"] for alg in ctxs)
+    same = all(np.array_equal(np.asarray(out[alg]["stats"]["rho"]), np.asarray(r), equal_nan=True)
+               for alg, r in zip(("simplex", "smap"), rhos))
+    for c in ctxs.values():
+        c.close()
+    wall = statistics.mean(times)
+    return {"value": preds / wall, "unit": "predictions/s", "wall_ms_per_step": wall * 1e3, "steps": steps,
+            "how": "simplex and S-map fedm_run_command calls from two host threads on two contexts, "
+                   "CTAs per SM capped at 1 (simplex) and 5 (S-map); wall time of both calls",
+            "rho_identical_to_sequential": bool(same)}
+
+
 def form_kernel(form, alg):
     """The kernel a mixed run used (fedm_timing.mixed_form), for the E = 4, k <= 6 benchmark."""
     return {0: f"knn_mixed_kernel<E=4,C=8,{alg},2 points per thread>",
@@ -267,6 +326,10 @@ def run_ours(a):
                 "sample": f"{sample_reps} replicates, both algorithms", "mixed_over_fp64": value / (p_fp64 / t_fp64),
                 "max_abs_drho_vs_fp64": drho}
 
+    concurrent = None
+    if world == 1 and not a.no_concurrent:
+        concurrent = concurrent_calls(fedm, w, a, local, rhos)
+
     cpu = None
     if world == 1 and not a.no_cpu:
         cpu = cpu_baseline(fedm, w, a)
@@ -308,6 +371,7 @@ def run_ours(a):
                     "frac": alg_bytes / (knn_ms_step * 1e-3) / 1e9 / hbm_gbs, "peak_source": hbm_src},
         },
         "fp64_plain": fp64,
+        "concurrent_calls": concurrent,
         "fallback_points_per_step": int(s0["fallback_points"]),
         "exact_points_per_step": int(s0["exact_points"]),
         "autotune": {"smap_form": form_kernel(s0["smap_mixed_form"], "smap"),
@@ -500,6 +564,8 @@ def main():
     ap.add_argument("--ref-libs", dest="ref_libs", type=int, default=None,
                     help="library sizes in each CPU reference sample (default: all)")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-concurrent", dest="no_concurrent", action="store_true",
+                    help="skip the concurrent two-context measurement of the headline workload")
     ap.add_argument("--no-fp64", dest="no_fp64", action="store_true",
                     help="skip the plain FP64 sample (profiling runs)")
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fast"],

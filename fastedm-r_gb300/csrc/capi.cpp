@@ -85,6 +85,14 @@ int fedm_set_precision(fedm_ctx* ctx, int precision)
   return FEDM_SUCCESS;
 }
 
+int fedm_set_ctas_per_sm(fedm_ctx* ctx, int ctas)
+{
+  if (!ctx || ctas < 0)
+    return FEDM_UNKNOWN_ERROR;
+  ctx->c->ctas_per_sm = ctas;
+  return FEDM_SUCCESS;
+}
+
 int fedm_set_keep_going(fedm_ctx* ctx, int (*keep_going)(void))
 {
   if (!ctx)

@@ -68,6 +68,8 @@ Context::Context(int dev) : device(dev)
   if (const char* v = std::getenv("FEDM_AUTOTUNE"))
     if (std::strcmp(v, "0") == 0)
       autotune = false;
+  if (const char* v = std::getenv("FEDM_CTAS_PER_SM"))
+    ctas_per_sm = std::max(0, std::atoi(v));
   reset_timing();
 }
 
@@ -789,6 +791,7 @@ void run_group(Context& ctx, const Options& o, const std::vector<Task>& tasks, c
     }
     ctx.timing.kernel_launches += (job.dFp != job.dF ? 2 : 1) + 1;  // centring, counter fill
     m.kslots = C;
+    m.ctas_per_sm = ctx.ctas_per_sm;
     auto launch_form = [&](int form) {
       m.form = form;
       if (wide)

@@ -35,6 +35,10 @@ public:
   // off) the form for E_a <= 8, k <= 14 is chosen per (algorithm, E_a, k) by
   // timing the candidates on the first batch large enough to measure.
   bool autotune = true;
+  // Cap on resident CTAs per SM of the mixed kernels' persistent grids (0:
+  // as many as fit), so that calls from other contexts can share the SMs;
+  // FEDM_CTAS_PER_SM sets it when the context is created.
+  int ctas_per_sm = 0;
   std::map<std::array<int, 3>, int> tuned_forms;
   std::string last_error;
   fedm_timing timing{};

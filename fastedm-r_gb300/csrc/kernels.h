@@ -153,6 +153,7 @@ struct MixedRun
   unsigned long long* fp64_ops;  // optional: FP64 operations of the re-rank and forecast stage
   int* error;          // set when a bounded wait of the warp-specialised kernel ran out
   int form;            // kernel form (MixedForm)
+  int ctas_per_sm;     // cap on resident CTAs per SM for the persistent grid (0: as many as fit)
   int item_begin;      // first item of this launch (the queue head starts here)
   int item_end;        // one past the last item of this launch
 };

@@ -262,6 +262,8 @@ void launch_one(const GroupParams& g, const MixedRun& m, int num_sms, cudaStream
 {
   int per_sm = 0;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, knn_mixed_kernel<EA, C, ALG>, TPB, 0);
+  if (m.ctas_per_sm > 0 && per_sm > m.ctas_per_sm)
+    per_sm = m.ctas_per_sm;
   if (per_sm < 1)
     per_sm = 1;
   long long blocks = (long long)num_sms * per_sm;

@@ -79,7 +79,8 @@ class Timing(C.Structure):
 
 
 EXPORTS = [
-    "fedm_create", "fedm_destroy", "fedm_last_error", "fedm_set_precision", "fedm_set_keep_going",
+    "fedm_create", "fedm_destroy", "fedm_last_error", "fedm_set_precision", "fedm_set_ctas_per_sm",
+    "fedm_set_keep_going",
     "fedm_run_command", "fedm_free_result", "fedm_run_task", "fedm_last_timing", "fedm_measure_peak",
     "fedm_host_usable", "fedm_host_manifold", "fedm_host_mt_real2", "fedm_host_plan",
     "fedm_smap_fwd", "fedm_smap_bwd", "fedm_smap_grad", "fedm_predict_static",
@@ -100,6 +101,7 @@ def load():
         lib.fedm_last_error.argtypes = [C.c_void_p]
         lib.fedm_last_error.restype = C.c_char_p
         lib.fedm_set_precision.argtypes = [C.c_void_p, C.c_int]
+        lib.fedm_set_ctas_per_sm.argtypes = [C.c_void_p, C.c_int]
         lib.fedm_set_keep_going.argtypes = [C.c_void_p, C.CFUNCTYPE(C.c_int)]
         lib.fedm_run_command.argtypes = [C.c_void_p, C.POINTER(Args), C.POINTER(C.POINTER(Result))]
         lib.fedm_free_result.argtypes = [C.POINTER(Result)]
@@ -144,6 +146,12 @@ class Context:
         if self.lib.fedm_set_precision(self.h, precision) != 0:
             raise ValueError("bad precision")
         self.precision = precision
+
+    def set_ctas_per_sm(self, ctas):
+        """Caps the mixed kernels' resident CTAs per SM (0: no cap), so that
+        calls on other contexts from other threads can share the SMs."""
+        if self.lib.fedm_set_ctas_per_sm(self.h, int(ctas)) != 0:
+            raise ValueError("bad CTA count")
 
     def close(self):
         if self.h:

@@ -54,6 +54,12 @@ void fedm_destroy(fedm_ctx* ctx);
 const char* fedm_last_error(const fedm_ctx* ctx);
 /* Selects FEDM_PRECISION_*; the default is FEDM_PRECISION_MIXED. */
 int fedm_set_precision(fedm_ctx* ctx, int precision);
+/* Caps the resident CTAs per SM of the context's persistent mixed-path
+ * kernels (0, the default: as many as fit).  Contexts used from concurrent
+ * host threads can then share the SMs: an FP64-bound S-map call leaves most
+ * issue slots idle, which a concurrent FP32-bound simplex call can fill
+ * (e.g. S-map 5 and simplex 1 of the six CTAs per SM). */
+int fedm_set_ctas_per_sm(fedm_ctx* ctx, int ctas);
 /* Optional cancellation callback, polled between GPU chunks (the
  * reference's keep_going(), src/edm.cpp:572-591).  Returning 0 stops the run
  * with FEDM_BREAK_HIT. */

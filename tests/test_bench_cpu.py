@@ -19,6 +19,9 @@ class FakeContext:
     def __init__(self, device=0, precision=1):
         self.precision = precision
 
+    def set_ctas_per_sm(self, ctas):
+        self.ctas = ctas
+
     def measure_peak(self, kind):
         return {0: 78.0, 1: 1.05, 2: 65.0, 3: 0.53}[kind]
 
@@ -88,7 +91,8 @@ BASE_KEYS = ["metric", "value", "unit", "n_gpus", "steps", "warmup", "higher_is_
 
 def test_headline_line(bench, monkeypatch):
     d = run(bench, monkeypatch, "--reps", "2", "--steps", "1", "--warmup", "3")
-    for k in BASE_KEYS + ["ms_per_step", "gpu_launches", "roofline", "cpu_baseline", "clocks", "fp64_plain"]:
+    for k in BASE_KEYS + ["ms_per_step", "gpu_launches", "roofline", "cpu_baseline", "clocks", "fp64_plain",
+                          "concurrent_calls"]:
         assert k in d, k
     assert d["warmup"] >= 3 and d["n_gpus"] == 1 and "workload" in d["config"]
     for k in ("value", "unit", "h2d_bytes_per_step", "d2h_bytes_per_step"):
@@ -99,6 +103,7 @@ def test_headline_line(bench, monkeypatch):
     for k in ("value", "unit", "cores", "kind", "sample"):
         assert k in d["cpu_baseline"], k
     assert {"sm_mhz", "sm_max_mhz", "reasons"} <= set(d["clocks"])
+    assert d["concurrent_calls"]["value"] > 0 and d["concurrent_calls"]["rho_identical_to_sequential"]
 
 
 @pytest.mark.parametrize("workload", ["simplex_explore", "smap_sweep", "panels", "adjoint"])

@@ -394,6 +394,41 @@ def test_easy_edm_call_sequence(ctx):
     both(y, x, E=E_best, library=lib_max, theta=opt_theta, algorithm="simplex", k=float("inf"), shuffle=True)
 
 
+def test_concurrent_contexts_share_the_gpu():
+    """Two contexts driven from two host threads at once -- a simplex and an
+    S-map CCM call, their mixed kernels capped at 1 and 5 resident CTAs per
+    SM (fedm_set_ctas_per_sm) -- give the bits of the same calls made one
+    after the other on an uncapped context."""
+    import threading
+    w = workloads.ccm_config(T=8000, reps=6, n_libs=5, hi=6000)
+    kw = {alg: dict(E=4, library=w["libraries"], numReps=6, seed=w["seed"], algorithm=alg,
+                    theta=2.0 if alg == "smap" else 1.0, savePredictions=True) for alg in ("simplex", "smap")}
+    ref = fedm.Context(0, precision=fedm.PRECISION_MIXED)
+    ctxs = {alg: fedm.Context(0, precision=fedm.PRECISION_MIXED) for alg in kw}
+    ctxs["simplex"].set_ctas_per_sm(1)
+    ctxs["smap"].set_ctas_per_sm(5)
+    try:
+        want = {alg: fedm.edm(w["t"], w["x"], w["y"], ctx=ref, **kw[alg]) for alg in kw}
+        got = {}
+
+        def run(alg):
+            got[alg] = fedm.edm(w["t"], w["x"], w["y"], ctx=ctxs[alg], **kw[alg])
+
+        threads = [threading.Thread(target=run, args=(alg,)) for alg in kw]
+        for th in threads:
+            th.start()
+        for th in threads:
+            th.join()
+    finally:
+        ref.close()
+        for c in ctxs.values():
+            c.close()
+    for alg in kw:
+        assert got[alg]["rc"] == want[alg]["rc"] == 0
+        assert np.array_equal(got[alg]["stats"]["rho"], want[alg]["stats"]["rho"], equal_nan=True)
+        assert np.array_equal(got[alg]["predictions"], want[alg]["predictions"], equal_nan=True)
+
+
 def test_keep_going_stops_between_batches():
     """keep_going() (src/edm.cpp:572-591) is polled before every task batch:
     returning false stops the run with rc 1 (BREAK_HIT).  The context (its
