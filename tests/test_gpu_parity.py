@@ -95,12 +95,23 @@ def _task_pair(ctx, a, lib, pred, E, k, **kw):
     return g, o
 
 
-def test_simplex_config_neighbours_bit_exact(ctx):
-    """250/250 split of the coupled logistic map, E = 1..10, k = E+1."""
+@pytest.mark.parametrize("masks", ["explicit", "usable"])
+def test_simplex_config_neighbours_bit_exact(ctx, masks):
+    """250/250 split of the coupled logistic map, E = 1..10, k = E+1.  The
+    explicit masks include the first rows, whose lags are missing, so every
+    task runs the exact kernels; with usable-row masks the mixed context runs
+    the one-point scan for k <= 6, the 16-slot form for k = 7..9 and the wide
+    form for E = 9, 10."""
     w = workloads.simplex_config()
     a = edm_oracle.normalise(w["t"], w["x"], E=1)
     for E in w["Es"]:
-        _task_pair(ctx, a, w["library_rows"], w["prediction_rows"], E, E + 1)
+        lib, pred = w["library_rows"], w["prediction_rows"]
+        if masks == "usable":
+            usable = fedm.host_usable(edm_oracle.normalise(w["t"], w["x"], E=E), E)
+            lib, pred = lib & usable, pred & usable
+        _task_pair(ctx, a, lib, pred, E, E + 1)
+        if masks == "usable" and ctx.precision == fedm.PRECISION_MIXED:
+            assert ctx.timing()["mixed_form"] >= 0, E
 
 
 @pytest.mark.parametrize("masks", ["raw", "usable"])
