@@ -929,8 +929,28 @@ void run_group(Context& ctx, const Options& o, const std::vector<Task>& tasks, c
       any_finite = true;
     } else if (nfb > 0) {
       h_plist.resize(nfb);
+      std::vector<double> h_thr(nfb);
       ctx.download(h_plist.data(), m.fb_list, (size_t)nfb * 8);
+      ctx.download(h_thr.data(), m.fb_thr, (size_t)nfb * 8);
       ck(cudaStreamSynchronize(s), "sync");
+      // in point order, so that consecutive points share a task and
+      // knn_refine_kernel's CTAs can stage each library tile once for all
+      // their points
+      {
+        std::vector<int> ord(nfb);
+        std::iota(ord.begin(), ord.end(), 0);
+        std::sort(ord.begin(), ord.end(), [&](int u, int v) { return h_plist[u] < h_plist[v]; });
+        std::vector<long long> sp(nfb);
+        std::vector<double> st(nfb);
+        for (int q = 0; q < nfb; q++) {
+          sp[q] = h_plist[ord[q]];
+          st[q] = h_thr[ord[q]];
+        }
+        h_plist.swap(sp);
+        ctx.upload(m.fb_list, h_plist.data(), (size_t)nfb * 8);
+        ctx.upload(m.fb_thr, st.data(), (size_t)nfb * 8);
+        ck(cudaStreamSynchronize(s), "sync");
+      }
       for (long long b = 0; b < nfb; b += chunk) {
         c.p_begin = 0;
         c.p_end = std::min<long long>(nfb - b, chunk);

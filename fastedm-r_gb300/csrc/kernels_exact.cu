@@ -263,119 +263,194 @@ __global__ void knn_exact_kernel(GroupParams g, ChunkBuffers c, int warps_per_bl
 // more than REFINE_CAP kept rows, or whose kept rows cannot supply its k, is
 // marked PT_REDO and left to knn_exact_kernel.
 constexpr int REFINE_CAP = 1024;
-constexpr int REFINE_WARPS = 2;
+constexpr int REFINE_WARPS = 8;
+constexpr int REFINE_TILE = 256;  // library rows staged per tile
 
+// FP32 squared distance of a row to the negated point np, in the scan's
+// operation order
+template<int EA>
+__device__ __forceinline__ float refine_sq(const float* x, const float (&np)[EA])
+{
+  float d = __fadd_rn(x[0], np[0]);
+  float sq = __fmul_rn(d, d);
+#pragma unroll
+  for (int j = 1; j < EA; j++) {
+    d = __fadd_rn(x[j], np[j]);
+    sq = __fmaf_rn(d, d, sq);
+  }
+  return sq;
+}
+
+// Appends a warp's hits (library indices, in index order) to its list;
+// false when the list would overflow (the same answer in every lane).
+__device__ __forceinline__ bool refine_append(bool hit, int i, int lane, int* sI, int& count)
+{
+  const unsigned hm = __ballot_sync(FULL, hit);
+  if (count + __popc(hm) > REFINE_CAP)
+    return false;
+  if (hit)
+    sI[count + __popc(hm & ((1u << lane) - 1u))] = i;
+  count += __popc(hm);
+  return true;
+}
+
+// Dynamic shared memory: per warp REFINE_CAP indices and distances, then a
+// tile of REFINE_TILE rows at an odd row stride (no bank conflicts when the
+// lanes read consecutive rows).
+template<int EA>
+__host__ __device__ constexpr int refine_tile_stride() { return EA | 1; }
+template<int EA>
+__host__ __device__ constexpr size_t refine_smem()
+{
+  return (size_t)REFINE_WARPS * REFINE_CAP * 12 + (size_t)REFINE_TILE * refine_tile_stride<EA>() * 4;
+}
+
+// A CTA takes REFINE_WARPS consecutive points of the (point-ordered) list.
+// When they all belong to one task -- the usual case -- the CTA stages each
+// tile of the library once and every warp scans it from shared memory;
+// otherwise each warp gathers its task's rows itself.
 template<int EA>
 __global__ void __launch_bounds__(32 * REFINE_WARPS) knn_refine_kernel(GroupParams g, ChunkBuffers c, RefineRun r)
 {
-  __shared__ int s_idx[REFINE_WARPS][REFINE_CAP];
-  __shared__ double s_dist[REFINE_WARPS][REFINE_CAP];
+  constexpr int TS = refine_tile_stride<EA>();
+  extern __shared__ __align__(16) unsigned char smem[];
+  __shared__ int s_task[REFINE_WARPS];
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
-  int* sI = s_idx[wib];
-  double* sD = s_dist[wib];
-  const long long nwarps = (long long)gridDim.x * REFINE_WARPS;
+  int* sI = (int*)smem + (size_t)wib * REFINE_CAP;
+  double* sD = (double*)(smem + (size_t)REFINE_WARPS * REFINE_CAP * 4) + (size_t)wib * REFINE_CAP;
+  float* tile = (float*)(smem + (size_t)REFINE_WARPS * REFINE_CAP * 12);
   const long long chunk = c.p_end - c.p_begin;
-  for (long long q = (long long)blockIdx.x * REFINE_WARPS + wib; q < chunk; q += nwarps) {
-    const long long p = point_of(c, q);
-    const DevTask T = g.tasks[find_task(g, p)];
-    const int prow = g.pred_rows[T.pred_off + (int)(p - T.point_base)];
-    const double thr = r.thr[q];
+  for (long long q0 = (long long)blockIdx.x * REFINE_WARPS; q0 < chunk; q0 += (long long)gridDim.x * REFINE_WARPS) {
+    const long long q = q0 + wib;
+    const bool has = q < chunk;
+    long long p = 0;
+    int ti = -1, prow = 0;
+    double thr = 0;
     float np[EA];
 #pragma unroll
     for (int j = 0; j < EA; j++)
-      np[j] = -r.Fp32[(size_t)prow * r.rs + j];
+      np[j] = 0.f;
+    if (has) {
+      p = point_of(c, q);
+      ti = find_task(g, p);
+      const DevTask& Tq = g.tasks[ti];
+      prow = g.pred_rows[Tq.pred_off + (int)(p - Tq.point_base)];
+      thr = r.thr[q];
+#pragma unroll
+      for (int j = 0; j < EA; j++)
+        np[j] = -r.Fp32[(size_t)prow * r.rs + j];
+    }
+    if (lane == 0)
+      s_task[wib] = ti;
+    __syncthreads();
+    const int t0 = s_task[0];  // warp 0 always has a point
+    bool same = true;
+#pragma unroll
+    for (int w = 1; w < REFINE_WARPS; w++)
+      same = same && (s_task[w] < 0 || s_task[w] == t0);
+    const DevTask T = g.tasks[has ? ti : t0];
     int count = 0;
     bool over = false;
-    for (int b0 = 0; b0 < T.n_lib; b0 += 32) {
-      const int i = b0 + lane;
-      bool hit = false;
-      if (i < T.n_lib) {
-        const float* x = r.F32 + (size_t)g.lib_rows[T.lib_off + i] * r.rs;
-        float d = __fadd_rn(x[0], np[0]);
-        float sq = __fmul_rn(d, d);
-#pragma unroll
-        for (int j = 1; j < EA; j++) {
-          d = __fadd_rn(x[j], np[j]);
-          sq = __fmaf_rn(d, d, sq);
+    if (same) {
+      for (int b0 = 0; b0 < T.n_lib; b0 += REFINE_TILE) {
+        const int nrow = min(REFINE_TILE, T.n_lib - b0);
+        __syncthreads();  // every warp is done with the previous tile
+        for (int e = threadIdx.x; e < nrow * EA; e += blockDim.x) {
+          const int i = e / EA, j = e - i * EA;
+          tile[i * TS + j] = r.F32[(size_t)g.lib_rows[T.lib_off + b0 + i] * r.rs + j];
         }
-        hit = (double)sq <= thr;
+        __syncthreads();
+        if (has && !over)
+          for (int i0 = 0; i0 < nrow; i0 += 32) {
+            const int i = i0 + lane;
+            const bool hit = i < nrow && (double)refine_sq<EA>(tile + i * TS, np) <= thr;
+            if (!refine_append(hit, b0 + i, lane, sI, count)) {
+              over = true;
+              break;
+            }
+          }
       }
-      const unsigned hm = __ballot_sync(FULL, hit);
-      if (count + __popc(hm) > REFINE_CAP) {
-        over = true;  // the same decision in every lane
-        break;
+    } else if (has) {
+      for (int b0 = 0; b0 < T.n_lib; b0 += 32) {
+        const int i = b0 + lane;
+        const bool hit =
+          i < T.n_lib && (double)refine_sq<EA>(r.F32 + (size_t)g.lib_rows[T.lib_off + i] * r.rs, np) <= thr;
+        if (!refine_append(hit, i, lane, sI, count)) {
+          over = true;
+          break;
+        }
       }
-      if (hit)
-        sI[count + __popc(hm & ((1u << lane) - 1u))] = i;
-      count += __popc(hm);
     }
-    __syncwarp();
-    int status = PT_REDO, keff = 0;
-    if (!over) {
-      const double* y = g.Fp + (size_t)prow * g.Ea;
-      const int ppanel = g.panel ? g.panel[prow] : 0;
-      const double ptime = g.point_time[prow];
-      int nvalid = 0;
-      for (int e = lane; e < count; e += 32) {
-        double d = 0;
-        const bool valid = exact_distance(g, g.lib_rows[T.lib_off + sI[e]], prow, y, ppanel, ptime, d);
-        sD[e] = valid ? d : -1.0;
-        nvalid += valid ? 1 : 0;
-      }
-      nvalid = __reduce_add_sync(FULL, nvalid);
+    if (has) {
       __syncwarp();
-      const int numValid = T.n_lib - (count - nvalid);
-      // src/edm.cpp:595-617, as in knn_exact_kernel
-      status = PT_OK;
-      keff = T.k_req < 0 ? numValid : T.k_req;
-      if (T.k_req > numValid) {
-        if (g.force_compute)
-          keff = numValid;
-        else
-          status = PT_INSUFFICIENT;
-      }
-      if (status == PT_OK && (keff == 0 || numValid == 0))
-        status = g.force_compute ? PT_EARLY_SUCCESS : PT_INSUFFICIENT;
-      if (status == PT_OK && nvalid < keff)
-        status = PT_REDO;
-      if (status == PT_OK) {
-        // rank among the valid kept rows: (distance, index), or library
-        // order when every valid neighbour is used (src/edm.cpp:615-616)
-        const bool lib_order = keff == numValid;
-        int* oi = c.nn_idx + q * c.kcap;
-        double* od = c.nn_dist + q * c.kcap;
+      int status = PT_REDO, keff = 0;
+      if (!over) {
+        const double* y = g.Fp + (size_t)prow * g.Ea;
+        const int ppanel = g.panel ? g.panel[prow] : 0;
+        const double ptime = g.point_time[prow];
+        int nvalid = 0;
         for (int e = lane; e < count; e += 32) {
-          const double de = sD[e];
-          if (de < 0)
-            continue;
-          const int ie = sI[e];
-          int rank = 0;
-          for (int f = 0; f < count; f++) {
-            const double df = sD[f];
-            if (df < 0)
+          double d = 0;
+          const bool valid = exact_distance(g, g.lib_rows[T.lib_off + sI[e]], prow, y, ppanel, ptime, d);
+          sD[e] = valid ? d : -1.0;
+          nvalid += valid ? 1 : 0;
+        }
+        nvalid = __reduce_add_sync(FULL, nvalid);
+        __syncwarp();
+        const int numValid = T.n_lib - (count - nvalid);
+        // src/edm.cpp:595-617, as in knn_exact_kernel
+        status = PT_OK;
+        keff = T.k_req < 0 ? numValid : T.k_req;
+        if (T.k_req > numValid) {
+          if (g.force_compute)
+            keff = numValid;
+          else
+            status = PT_INSUFFICIENT;
+        }
+        if (status == PT_OK && (keff == 0 || numValid == 0))
+          status = g.force_compute ? PT_EARLY_SUCCESS : PT_INSUFFICIENT;
+        if (status == PT_OK && nvalid < keff)
+          status = PT_REDO;
+        if (status == PT_OK) {
+          // rank among the valid kept rows: (distance, index), or library
+          // order when every valid neighbour is used (src/edm.cpp:615-616)
+          const bool lib_order = keff == numValid;
+          int* oi = c.nn_idx + q * c.kcap;
+          double* od = c.nn_dist + q * c.kcap;
+          for (int e = lane; e < count; e += 32) {
+            const double de = sD[e];
+            if (de < 0)
               continue;
-            rank += lib_order ? (sI[f] < ie) : (df < de || (df == de && sI[f] < ie));
-          }
-          if (rank < keff) {
-            oi[rank] = ie;
-            od[rank] = de;
+            const int ie = sI[e];
+            int rank = 0;
+            for (int f = 0; f < count; f++) {
+              const double df = sD[f];
+              if (df < 0)
+                continue;
+              rank += lib_order ? (sI[f] < ie) : (df < de || (df == de && sI[f] < ie));
+            }
+            if (rank < keff) {
+              oi[rank] = ie;
+              od[rank] = de;
+            }
           }
         }
       }
-    }
-    if (lane == 0) {
-      c.status[q] = status;
-      if (status == PT_REDO)
-        atomicAdd(r.redo_count, 1);
-      else {
-        c.nn_count[q] = keff;
-        if (status == PT_OK)
-          note_k(g, T.task, p, keff);
-        else if (g.kused)
-          g.kused[p] = INT_MIN;
+      if (lane == 0) {
+        c.status[q] = status;
+        if (status == PT_REDO)
+          atomicAdd(r.redo_count, 1);
+        else {
+          c.nn_count[q] = keff;
+          if (status == PT_OK)
+            note_k(g, T.task, p, keff);
+          else if (g.kused)
+            g.kused[p] = INT_MIN;
+        }
       }
+      __syncwarp();
     }
-    __syncwarp();
+    __syncthreads();  // s_task and the tile are reused by the next group
   }
 }
 
@@ -960,33 +1035,41 @@ void launch_knn_exact(const GroupParams& g, const ChunkBuffers& c, int num_sms, 
   knn_exact_kernel<<<(int)blocks, 32 * w, smem, s>>>(g, c, w, per_warp);
 }
 
+template<int EA>
+void launch_refine_ea(const GroupParams& g, const ChunkBuffers& c, const RefineRun& r, int blocks, cudaStream_t s)
+{
+  constexpr size_t smem = refine_smem<EA>();
+  cudaFuncSetAttribute(knn_refine_kernel<EA>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  knn_refine_kernel<EA><<<blocks, 32 * REFINE_WARPS, smem, s>>>(g, c, r);
+}
+
 void launch_knn_refine(const GroupParams& g, const ChunkBuffers& c, const RefineRun& r, int num_sms, cudaStream_t s)
 {
   const long long chunk = c.p_end - c.p_begin;
   if (chunk <= 0)
     return;
   long long blocks = (chunk + REFINE_WARPS - 1) / REFINE_WARPS;
-  const long long cap = (long long)num_sms * 16;
+  const long long cap = (long long)num_sms * 2;  // 113 KB of shared memory per CTA at E_a = 16
   if (blocks > cap)
     blocks = cap;
-  const int b = (int)blocks, t = 32 * REFINE_WARPS;
+  const int b = (int)blocks;
   switch (g.Ea) {
-    case 1: knn_refine_kernel<1><<<b, t, 0, s>>>(g, c, r); break;
-    case 2: knn_refine_kernel<2><<<b, t, 0, s>>>(g, c, r); break;
-    case 3: knn_refine_kernel<3><<<b, t, 0, s>>>(g, c, r); break;
-    case 4: knn_refine_kernel<4><<<b, t, 0, s>>>(g, c, r); break;
-    case 5: knn_refine_kernel<5><<<b, t, 0, s>>>(g, c, r); break;
-    case 6: knn_refine_kernel<6><<<b, t, 0, s>>>(g, c, r); break;
-    case 7: knn_refine_kernel<7><<<b, t, 0, s>>>(g, c, r); break;
-    case 8: knn_refine_kernel<8><<<b, t, 0, s>>>(g, c, r); break;
-    case 9: knn_refine_kernel<9><<<b, t, 0, s>>>(g, c, r); break;
-    case 10: knn_refine_kernel<10><<<b, t, 0, s>>>(g, c, r); break;
-    case 11: knn_refine_kernel<11><<<b, t, 0, s>>>(g, c, r); break;
-    case 12: knn_refine_kernel<12><<<b, t, 0, s>>>(g, c, r); break;
-    case 13: knn_refine_kernel<13><<<b, t, 0, s>>>(g, c, r); break;
-    case 14: knn_refine_kernel<14><<<b, t, 0, s>>>(g, c, r); break;
-    case 15: knn_refine_kernel<15><<<b, t, 0, s>>>(g, c, r); break;
-    case 16: knn_refine_kernel<16><<<b, t, 0, s>>>(g, c, r); break;
+    case 1: launch_refine_ea<1>(g, c, r, b, s); break;
+    case 2: launch_refine_ea<2>(g, c, r, b, s); break;
+    case 3: launch_refine_ea<3>(g, c, r, b, s); break;
+    case 4: launch_refine_ea<4>(g, c, r, b, s); break;
+    case 5: launch_refine_ea<5>(g, c, r, b, s); break;
+    case 6: launch_refine_ea<6>(g, c, r, b, s); break;
+    case 7: launch_refine_ea<7>(g, c, r, b, s); break;
+    case 8: launch_refine_ea<8>(g, c, r, b, s); break;
+    case 9: launch_refine_ea<9>(g, c, r, b, s); break;
+    case 10: launch_refine_ea<10>(g, c, r, b, s); break;
+    case 11: launch_refine_ea<11>(g, c, r, b, s); break;
+    case 12: launch_refine_ea<12>(g, c, r, b, s); break;
+    case 13: launch_refine_ea<13>(g, c, r, b, s); break;
+    case 14: launch_refine_ea<14>(g, c, r, b, s); break;
+    case 15: launch_refine_ea<15>(g, c, r, b, s); break;
+    case 16: launch_refine_ea<16>(g, c, r, b, s); break;
     default: break;
   }
 }
