@@ -135,7 +135,7 @@ __global__ void knn_exact_kernel(GroupParams g, ChunkBuffers c, int warps_per_bl
     for (int j = lane; j < g.Ea; j += 32)
       sy[j] = g.Fp[(size_t)prow * g.Ea + j];
     const int ppanel = g.panel ? g.panel[prow] : 0;
-    const double ptime = g.point_time[prow];
+    const double ptime = g.past_only ? g.point_time[prow] : 0.0;
     __syncwarp();
     const int k = T.k;
     int count = 0, numValid = 0;
@@ -387,7 +387,7 @@ __global__ void __launch_bounds__(32 * REFINE_WARPS) knn_refine_kernel(GroupPara
       if (!over) {
         const double* y = g.Fp + (size_t)prow * g.Ea;
         const int ppanel = g.panel ? g.panel[prow] : 0;
-        const double ptime = g.point_time[prow];
+        const double ptime = g.past_only ? g.point_time[prow] : 0.0;
         int nvalid = 0;
         for (int e = lane; e < count; e += 32) {
           double d = 0;
@@ -610,7 +610,7 @@ __global__ void all_dist_kernel(GroupParams g, ChunkBuffers c, long long max_nli
     for (int j = lane; j < g.Ea; j += 32)
       sy[j] = g.Fp[(size_t)prow * g.Ea + j];
     const int ppanel = g.panel ? g.panel[prow] : 0;
-    const double ptime = g.point_time[prow];
+    const double ptime = g.past_only ? g.point_time[prow] : 0.0;
     __syncwarp();
     double* dq = c.scratch + q * max_nlib;
     int lcnt = 0;

@@ -1,8 +1,9 @@
 // Device pieces shared by the mixed-precision CCM kernels (kernels_mixed.cu,
-// kernels_flat.cu): work-item scan with FP32 candidate lists, the FP64
-// re-rank that settles a point's neighbour list, and the shared-memory
-// hand-off primitives (mbarriers with bounded waits).  Everything sits in an
-// anonymous namespace, so each translation unit has its own copy.
+// kernels_wide.cu, kernels_one16.cu): work-item scan with FP32 candidate
+// lists, the FP64 re-rank that settles a point's neighbour list, and the
+// shared-memory hand-off primitives (mbarriers with bounded waits).
+// Everything sits in an anonymous namespace, so each translation unit has
+// its own copy.
 #pragma once
 
 #include <cfloat>

@@ -58,24 +58,41 @@ void* scratch_address(int device, int& rc)
   return g_addr[device];
 }
 
-__global__ void iota_kernel(int* a, int n, int* b, int m)
+// Everything a call needs besides the caller's buffers, passed by value as
+// a kernel parameter: the host's copies may be gone once the call returns.
+struct StaticInit
 {
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n || i < m; i += gridDim.x * blockDim.x) {
-    if (i < n)
-      a[i] = i;
-    if (i < m)
-      b[i] = i;
-  }
-}
+  DevTask task;
+  int flags[4];  // task rc, kmin, kmax, error flag
+  int n_thetas;
+  double thetas[FEDM_STATIC_MAX_THETAS];
+};
 
-__global__ void fill_missing_kernel(double* p, long long n, int* kused, int n_pred)
+// Writes the task descriptor, the flags, the thetas and the identity row
+// lists into the scratch array, and starts the forecasts as MISSING and
+// kused as INT_MIN like edm_task's buffers (src/edm.cpp:345-361).
+__global__ void static_init_kernel(StaticInit in, DevTask* d_task, int* d_flags, double* d_thetas, int* lib_rows,
+                                   int n_lib, int* pred_rows, int n_pred, double* pred, long long n_forecasts,
+                                   int* kused)
 {
-  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
-    p[i] = 1.0e+100;
-  if (kused)
-    for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n_pred;
-         i += (long long)gridDim.x * blockDim.x)
+  const long long i0 = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  if (i0 == 0) {
+    *d_task = in.task;
+    for (int j = 0; j < 4; j++)
+      d_flags[j] = in.flags[j];
+  }
+  for (long long i = i0; i < in.n_thetas; i += stride)
+    d_thetas[i] = in.thetas[i];
+  for (long long i = i0; i < n_lib; i += stride)
+    lib_rows[i] = (int)i;
+  for (long long i = i0; i < n_pred; i += stride) {
+    pred_rows[i] = (int)i;
+    if (kused)
       kused[i] = INT_MIN;
+  }
+  for (long long i = i0; i < n_forecasts; i += stride)
+    pred[i] = 1.0e+100;
 }
 
 size_t align256(size_t v)
@@ -138,7 +155,8 @@ extern "C" int fedm_predict_static(const double* lib_manifold, const double* lib
   if (off > kScratchBytes)
     return FEDM_NOT_IMPLEMENTED;  // cannot happen within the stated limits
 
-  DevTask task{};
+  StaticInit init{};
+  DevTask& task = init.task;
   task.point_base = 0;
   task.lib_off = 0;
   task.n_lib = n_lib;
@@ -150,28 +168,30 @@ extern "C" int fedm_predict_static(const double* lib_manifold, const double* lib
   task.save_coeffs = 0;
   task.all_mode = 0;
   task.mixed = 0;
-  const int init_flags[4] = { 0, INT_MAX, INT_MIN, 0 };
-  if (cudaMemcpyAsync(d_task, &task, sizeof(task), cudaMemcpyHostToDevice, s) != cudaSuccess ||
-      cudaMemcpyAsync(d_flags, init_flags, sizeof(init_flags), cudaMemcpyHostToDevice, s) != cudaSuccess ||
-      cudaMemcpyAsync(d_thetas, thetas, (size_t)n_thetas * 8, cudaMemcpyHostToDevice, s) != cudaSuccess)
-    return FEDM_UNKNOWN_ERROR;
-  const int m = n_lib > n_pred ? n_lib : n_pred;
-  iota_kernel<<<(m + 255) / 256 < 1024 ? (m + 255) / 256 : 1024, 256, 0, s>>>(d_lib_rows, n_lib, d_pred_rows,
-                                                                              n_pred);
-  // forecasts start as MISSING like edm_task's buffers (src/edm.cpp:345-350)
+  init.flags[0] = 0;
+  init.flags[1] = INT_MAX;
+  init.flags[2] = INT_MIN;
+  init.flags[3] = 0;
+  init.n_thetas = n_thetas;
+  for (int t = 0; t < n_thetas; t++)
+    init.thetas[t] = thetas[t];
   const long long np = (long long)n_pred * n_thetas;
-  fill_missing_kernel<<<(int)((np + 255) / 256 < 1024 ? (np + 255) / 256 : 1024), 256, 0, s>>>(predictions, np,
-                                                                                          kused, n_pred);
+  long long span = np > n_lib ? np : n_lib;
+  const int blocks = (int)((span + 255) / 256 < 1024 ? (span + 255) / 256 : 1024);
+  static_init_kernel<<<blocks, 256, 0, s>>>(init, d_task, d_flags, d_thetas, d_lib_rows, n_lib, d_pred_rows, n_pred,
+                                            predictions, np, kused);
 
   GroupParams g{};
   g.F = lib_manifold;
   g.Fp = pred_manifold;
   g.lib_target = lib_targets;
-  g.pred_target = lib_targets;
-  // the time tables are read only by the past-only rule, which is off here;
-  // they still point at arrays long enough for every row index used
-  g.lib_target_time = lib_targets;    // n_lib entries, indexed by library row
-  g.point_time = pred_manifold;       // >= n_pred entries, indexed by prediction row
+  // no prediction targets (statistics are not computed here) and no time
+  // tables: the kernels read those only for rho/MAE and under the past-only
+  // rule, both off here (g.past_only = 0)
+  g.pred_target = nullptr;
+  g.lib_target_time = nullptr;
+  g.point_time = nullptr;
+  g.past_only = 0;
   g.lib_rows = d_lib_rows;
   g.pred_rows = d_pred_rows;
   g.tasks = d_task;

@@ -293,13 +293,17 @@ int fedm_smap_grad(fedm_ctx* ctx, const double* lib_manifold, const double* lib_
  *
  * Inputs (device pointers): lib_manifold [n_lib x e_actual] and lib_targets
  * [n_lib] (library rows whose target is observed, as edm_task's M),
- * pred_manifold [n_pred x e_actual]; thetas is a HOST array of n_thetas.
+ * pred_manifold [n_pred x e_actual]; thetas is a HOST array of n_thetas,
+ * read before the call returns (its values travel as a kernel parameter).
  * Outputs (device pointers): predictions [n_thetas x n_pred] (theta-major,
  * MISSING = 1e100 where no forecast is made), kused [n_pred] (may be NULL).
- * algorithm 0 simplex, 1 S-map; 1 <= k; exact FP64 path, L2 distance, no
- * missing values, panels or past-only rule; work is queued on `stream` (a
- * cudaStream_t, NULL = legacy default stream) and the call returns before it
- * finishes.
+ * algorithm 0 simplex, 1 S-map; 1 <= k (k >= n_lib uses every valid library
+ * row, in library order); exact FP64 path, L2 distance, no missing values,
+ * panels or past-only rule; work is queued on `stream` (a cudaStream_t, NULL
+ * = legacy default stream) and the call returns before it finishes.  The
+ * return value reports argument and launch errors only: a point without a
+ * forecast (no valid neighbour) shows as MISSING in predictions and INT_MIN
+ * in kused, as in edm_task's outputs.
  *
  * Working memory is one file-scope __device__ array of
  * FEDM_STATIC_SCRATCH_BYTES (32 MiB) that every GPU loading the library holds
@@ -308,10 +312,11 @@ int fedm_smap_grad(fedm_ctx* ctx, const double* lib_manifold, const double* lib_
  * n_thetas <= FEDM_STATIC_MAX_THETAS; larger requests return
  * FEDM_NOT_IMPLEMENTED with a message on stderr.  The first call on a device
  * looks the array's device address up (cudaGetSymbolAddress) with that device
- * current; make that first call before any stream capture.  All calls on a
- * device share the array and it keeps the last call's contents (each call
- * re-initialises what it reads): calls that overlap on the GPU race and must
- * be serialised by the caller. */
+ * current; make that first call before any stream capture.  The address is
+ * kept for the life of the process, so the library must not be used across
+ * a cudaDeviceReset.  All calls on a device share the array and it keeps the
+ * last call's contents (each call re-initialises what it reads): calls that
+ * overlap on the GPU race and must be serialised by the caller. */
 #define FEDM_STATIC_SCRATCH_BYTES (32 << 20)
 #define FEDM_STATIC_MAX_LIB (1 << 20)
 #define FEDM_STATIC_MAX_PRED 65536
