@@ -72,6 +72,105 @@ int g_exp_mode = 0;
 // prediction set (1 = all rows, the reference's behaviour).
 int g_pred_stride = 1;
 
+// Order of the floating-point sums that the reference leaves to Eigen and to
+// its compiler.  Quantification only: it measures how far the reference's
+// own builds spread.  0, the default, is the plain sequential unfused order,
+// which the GPU library reproduces bit for bit.  Bits:
+//   1, 2  Eigen's vectorised order with packets of 2 (SSE2, NEON) or 4 (AVX)
+//         doubles, in the S-map's three Eigen reductions (src/edm.cpp:745,
+//         781-782): mean(d) (Redux.h, linear vectorised traversal), X^T X
+//         (a coefficient-wise lazy product, each entry such a reduction,
+//         below Eigen's threshold rows+cols+depth < 20; else a GEMM whose
+//         depth is blocked, GEMM_KC rows per block, each block summed in
+//         order) and X^T y (a row-major GEMV: one packet accumulator per
+//         row, then the horizontal sum and the scalar tail);
+//   4     the multiply-adds of those products fused (Eigen's pmadd on FMA
+//         targets);
+//   8     the reference's own scalar loops contracted to FMA, as GCC's
+//         default -ffp-contract=fast does on aarch64: the distance sums
+//         (src/distances.cpp:211-215), the simplex sum (src/edm.cpp:729) and
+//         the S-map forecast (src/edm.cpp:793-797).
+int g_sum_mode = 0;
+const int GEMM_KC = 256;
+
+inline double mac(double a, double b, double c, bool fused)
+{
+  return fused ? std::fma(a, b, c) : a * b + c;
+}
+
+// Horizontal sum of one packet: l0 + l1, or (l0 + l2) + (l1 + l3).
+inline double predux(const double* l, int P)
+{
+  return P == 2 ? l[0] + l[1] : (l[0] + l[2]) + (l[1] + l[3]);
+}
+
+// Eigen's linear vectorised reduction of v[0..n) (or of the products
+// a[i*sa] * b[i*sb] when a is given) with packets of P and no aligned
+// prefix: two packet accumulators over blocks of 2P, combined, one more
+// packet if it fits, the horizontal sum, then the remaining scalars.
+double packet_reduce(const double* v, const double* a, int sa, const double* b, int sb, int n, int P, bool fused)
+{
+  auto term = [&](int i) { return a ? a[(size_t)i * sa] * b[(size_t)i * sb] : v[i]; };
+  auto acc = [&](double c, int i) { return a ? mac(a[(size_t)i * sa], b[(size_t)i * sb], c, fused) : c + v[i]; };
+  const int aligned = n / P * P, aligned2 = n / (2 * P) * (2 * P);
+  if (aligned == 0) {
+    double r = term(0);
+    for (int i = 1; i < n; i++)
+      r = acc(r, i);
+    return r;
+  }
+  double p0[4], p1[4];
+  for (int l = 0; l < P; l++)
+    p0[l] = term(l);
+  if (aligned > P) {
+    for (int l = 0; l < P; l++)
+      p1[l] = term(P + l);
+    for (int i = 2 * P; i < aligned2; i += 2 * P)
+      for (int l = 0; l < P; l++) {
+        p0[l] = acc(p0[l], i + l);
+        p1[l] = acc(p1[l], i + P + l);
+      }
+    for (int l = 0; l < P; l++)
+      p0[l] = p0[l] + p1[l];
+    if (aligned > aligned2)
+      for (int l = 0; l < P; l++)
+        p0[l] = acc(p0[l], aligned2 + l);
+  }
+  double r = predux(p0, P);
+  for (int i = aligned; i < n; i++)
+    r = acc(r, i);
+  return r;
+}
+
+// Row-major GEMV order: one packet accumulator from zero over the full
+// packets, the horizontal sum, then the scalar tail.
+double gemv_dot(const double* a, int sa, const double* b, int sb, int n, int P, bool fused)
+{
+  double l[4] = { 0, 0, 0, 0 };
+  const int aligned = n / P * P;
+  for (int i = 0; i < aligned; i += P)
+    for (int q = 0; q < P; q++)
+      l[q] = mac(a[(size_t)(i + q) * sa], b[(size_t)(i + q) * sb], l[q], fused);
+  double r = predux(l, P);
+  for (int i = aligned; i < n; i++)
+    r = mac(a[(size_t)i * sa], b[(size_t)i * sb], r, fused);
+  return r;
+}
+
+// GEMM order: the depth in blocks of GEMM_KC, each summed in order into a
+// register from zero, the blocks added to the result in turn.
+double blocked_dot(const double* a, int sa, const double* b, int sb, int n, bool fused)
+{
+  double r = 0;
+  for (int i0 = 0; i0 < n; i0 += GEMM_KC) {
+    double c = 0;
+    for (int i = i0; i < std::min(n, i0 + GEMM_KC); i++)
+      c = mac(a[(size_t)i * sa], b[(size_t)i * sb], c, fused);
+    r = r + c;
+  }
+  return r;
+}
+
 double pow2i(int k)
 {
   uint64_t b = (uint64_t)(k + 1023) << 52;
@@ -617,7 +716,7 @@ DistanceIndexPairs lp_distances(int Mp_i, const Options& opts, const Manifold& M
       if (l1)
         d += std::abs(dij) / M.E_actual;
       else
-        d += dij * dij;
+        d = mac(dij, dij, d, g_sum_mode & 8);
     }
     if (d != 0 && d != MISSING_D) {
       out.dists.push_back(l1 ? d : std::sqrt(d));
@@ -835,7 +934,7 @@ void simplex_prediction(int Mp_i, int t, const Options& opts, const Manifold& M,
   }
   double r = 0.0;
   for (int j = 0; j < k; j++)
-    r = r + M.targets[inds[j]] * (w[j] / sumw);
+    r = mac(M.targets[inds[j]], w[j] / sumw, r, g_sum_mode & 8);
   o.predictions[(size_t)t * o.numPredictions + Mp_i] = r;
   o.rc[(size_t)t * o.numPredictions + Mp_i] = SUCCESS;
 }
@@ -846,9 +945,15 @@ void smap_prediction(int Mp_i, int t, const Options& opts, const Manifold& M, co
 {
   int k = (int)inds.size();
   int Ea = M.E_actual, n = Ea + 1;
+  const int P = (g_sum_mode & 1) ? 2 : ((g_sum_mode & 2) ? 4 : 0);
+  const bool fused = (g_sum_mode & 4) != 0;
   double mean = 0;
-  for (double d : dists)
-    mean += d;
+  if (P) {
+    mean = packet_reduce(dists.data(), nullptr, 0, nullptr, 0, k, P, false);
+  } else {
+    for (double d : dists)
+      mean += d;
+  }
   mean /= (double)k;
   std::vector<double> w(k);
   for (int i = 0; i < k; i++)
@@ -864,13 +969,21 @@ void smap_prediction(int Mp_i, int t, const Options& opts, const Manifold& M, co
   for (int a = 0; a < n; a++) {
     for (int b = 0; b < n; b++) {
       double s = 0;
-      for (int i = 0; i < k; i++)
-        s += X[(size_t)i * n + a] * X[(size_t)i * n + b];
+      if (P && k + n + k < 20)
+        s = packet_reduce(nullptr, &X[a], n, &X[b], n, k, P, fused);
+      else if (P)
+        s = blocked_dot(&X[a], n, &X[b], n, k, fused);
+      else
+        for (int i = 0; i < k; i++)
+          s += X[(size_t)i * n + a] * X[(size_t)i * n + b];
       XtX[(size_t)a * n + b] = s;
     }
     double s = 0;
-    for (int i = 0; i < k; i++)
-      s += X[(size_t)i * n + a] * y[i];
+    if (P)
+      s = gemv_dot(&X[a], n, y.data(), 1, k, P, fused);
+    else
+      for (int i = 0; i < k; i++)
+        s += X[(size_t)i * n + a] * y[i];
     Xty[a] = s;
   }
   std::vector<double> ics = jacobi_svd_solve(XtX, n, Xty);
@@ -878,7 +991,7 @@ void smap_prediction(int Mp_i, int t, const Options& opts, const Manifold& M, co
   for (int j = 0; j < Ea; j++) {
     double yj = Mp(Mp_i, j);
     if (yj != MISSING_D)
-      r += yj * ics[j + 1];
+      r = mac(yj, ics[j + 1], r, g_sum_mode & 8);
   }
   if (opts.saveSMAPCoeffs && t == (int)opts.thetas.size() - 1) {
     for (int j = 0; j < n; j++)
@@ -1377,6 +1490,11 @@ extern "C" {
 void oracle_set_exp_mode(int mode)
 {
   g_exp_mode = mode;
+}
+
+void oracle_set_sum_mode(int mode)
+{
+  g_sum_mode = mode & 15;
 }
 
 void oracle_set_pred_stride(int stride)

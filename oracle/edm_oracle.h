@@ -158,6 +158,13 @@ int oracle_usable(const oracle_args* args, int maxE, int copredict, unsigned cha
 /* 0 (default): weights use std::exp like the reference.  1: weights use the
  * IEEE-only exp formula the GPU library evaluates, for bit-level parity. */
 void oracle_set_exp_mode(int mode);
+/* Summation orders the reference leaves to Eigen and its compiler, to
+ * measure the spread of the reference's own builds: 0 (default) plain
+ * sequential unfused sums; bit 1 / 2 Eigen's vectorised order with packets
+ * of 2 / 4 doubles in the S-map's mean(d), X^T X and X^T y; bit 4 those
+ * products' multiply-adds fused; bit 8 the scalar loops (distances, simplex
+ * sum, S-map forecast) contracted to FMA. */
+void oracle_set_sum_mode(int mode);
 /* Benchmark sampling: predict only every stride-th row of each prediction
  * set (1, the default, is the reference's behaviour). */
 void oracle_set_pred_stride(int stride);

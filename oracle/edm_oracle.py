@@ -81,6 +81,7 @@ def load():
         _lib.oracle_mt_real2.argtypes = [C.c_ulonglong, C.c_longlong, C.c_void_p]
         _lib.oracle_set_exp_mode.argtypes = [C.c_int]
         _lib.oracle_set_pred_stride.argtypes = [C.c_int]
+        _lib.oracle_set_sum_mode.argtypes = [C.c_int]
         _lib.oracle_smap_grad.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_int,
                                           C.c_double, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
         _lib.oracle_plan.argtypes = [C.POINTER(OracleArgs), C.c_int] + [C.c_void_p] * 7
@@ -327,6 +328,13 @@ def plan(a):
     lib.oracle_plan(C.byref(s), m, C.byref(nt), E.ctypes.data, k.ctypes.data, L.ctypes.data, co.ctypes.data,
                     lm.ctypes.data, pm.ctypes.data)
     return dict(E=E[:m], k=k[:m], library=L[:m], copredict=co[:m], lib=lm[:m].astype(bool), pred=pm[:m].astype(bool))
+
+
+def set_sum_mode(mode):
+    """Summation order of the reference's Eigen reductions and scalar loops
+    (0: sequential unfused; bits 1/2: Eigen packets of 2/4; 4: fused
+    products; 8: FMA-contracted scalar loops)."""
+    load().oracle_set_sum_mode(int(mode))
 
 
 def set_pred_stride(stride):

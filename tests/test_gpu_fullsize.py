@@ -1,0 +1,153 @@
+"""Oracle parity at the benchmark configurations' full sizes.
+
+The GPU runs every prediction row of each task; the oracle, which cannot
+finish the full sizes in test time, runs a strided subset of the same
+prediction rows on the same library masks (a prediction point's forecast and
+neighbour list do not depend on the other prediction points).  At those rows
+the neighbour indices, their FP64 distances, k used and every forecast must
+be the oracle's bits.
+
+* Batched CCM (T = 50 000, E = 4, all 20 library sizes from 100 to 40 000,
+  one random replicate), simplex (k = 5) and S-map (theta = 2, k = 6), on the
+  mixed path; the batched run_command path must give the statistics of the
+  single-task path for every library size and the last task's forecasts.
+* S-map theta sweep with k = all (10 000 library x 10 000 prediction rows,
+  81 thetas), forecasts and the last theta's coefficients.
+* 512 uneven panels with missing values and dt, E = 3..8, simplex and the
+  4-theta S-map, with mixed (panelWeight = 0) and independent
+  (panelWeight = Inf) panels.
+"""
+import numpy as np
+import pytest
+
+import edm_oracle
+from fedm_loader import fedm, workloads
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _device_exp():
+    edm_oracle.set_exp_mode(1)  # the library's IEEE-only exp formula
+    yield
+    edm_oracle.set_exp_mode(0)
+
+
+@pytest.fixture(scope="module")
+def mixed_ctx():
+    c = fedm.Context(0, precision=fedm.PRECISION_MIXED)
+    yield c
+    c.close()
+
+
+def _strided(mask, stride, offset=0):
+    """The prediction mask cut to every stride-th of its rows, and the
+    positions of those rows among the mask's rows."""
+    rows = np.nonzero(mask)[0]
+    sel = np.arange(offset % stride, len(rows), stride)
+    sub = np.zeros_like(mask)
+    sub[rows[sel]] = True
+    return sub, sel
+
+
+def _lists(r, points):
+    off = r["nn_offsets"]
+    idx, dist = [], []
+    for p in points:
+        a, b = off[p], off[p + 1]
+        idx.append(r["nn_idx"][a:b])
+        dist.append(r["nn_dist"][a:b])
+    return idx, dist
+
+
+def _compare_task(g, o, sel, what):
+    """GPU task output g (every prediction row) against oracle output o (the
+    rows at positions sel), bit for bit."""
+    assert g["n_lib"] == o["n_lib"], what
+    assert np.array_equal(g["predictions"][:, sel].view(np.int64), o["predictions"].view(np.int64)), what
+    assert np.array_equal(g["kused"][sel], o["kused"]), what
+    assert np.array_equal(g["rc"][:, sel], o["rc"]), what
+    gi, gd = _lists(g, sel)
+    oi, od = _lists(o, range(len(sel)))
+    for q in range(len(sel)):
+        assert np.array_equal(gi[q], oi[q]), (what, q)
+        assert np.array_equal(gd[q].view(np.int64), od[q].view(np.int64)), (what, q)
+
+
+def _oracle(a_kw, t, x, y, lib, pred, E, k):
+    return edm_oracle.oracle_task(edm_oracle.normalise(t, x, y, numThreads=16, **a_kw), lib, pred, E, k)
+
+
+@pytest.mark.parametrize("algorithm", ["simplex", "smap"])
+def test_ccm_full_size_bit_exact(mixed_ctx, algorithm):
+    """Config 3's shape at full size: every library size up to 40 000."""
+    w = workloads.ccm_config(reps=1)
+    theta = 2.0 if algorithm == "smap" else 1.0
+    kw = dict(E=4, library=w["libraries"], numReps=1, shuffle=True, seed=w["seed"], algorithm=algorithm,
+              theta=theta)
+    a = fedm.normalise(w["t"], w["x"], w["y"], **kw)
+    plan = fedm.host_plan(a)
+    assert len(plan["E"]) == 20 and plan["library"][-1] == 40000
+    rho_task = []
+    counts = {}
+    for f in range(20):
+        g = mixed_ctx.run_task(a, plan["lib"][f], plan["pred"][f], 4, int(plan["k"][f]))
+        tm = mixed_ctx.timing()
+        assert tm["mixed_form"] >= 0  # the mixed kernels served the task
+        counts[int(plan["library"][f])] = (tm["fallback_points"], tm["exact_points"])
+        rho_task.append(g["stats_rho"][0])
+        sub, sel = _strided(plan["pred"][f], 37, offset=f)
+        o = _oracle(kw, w["t"], w["x"], w["y"], plan["lib"][f], sub, 4, int(plan["k"][f]))
+        assert g["n_pred"] > 49000 and len(sel) > 1300
+        _compare_task(g, o, sel, (algorithm, int(plan["library"][f])))
+        last = g
+    # the batched path (every library size in one run_command) against the
+    # single-task path: the same statistics and the last task's forecasts
+    r = fedm.edm(w["t"], w["x"], w["y"], ctx=mixed_ctx, savePredictions=True, **kw)
+    assert r["rc"] == 0
+    assert np.array_equal(np.asarray(r["stats"]["library"]), plan["library"])
+    assert np.array_equal(np.asarray(r["stats"]["rho"]), np.asarray(rho_task))
+    pred_rows = np.nonzero(plan["pred"][-1])[0]
+    saved = np.asarray(r["predictions"], float)[pred_rows, -1]
+    want = np.where(last["predictions"][-1] == 1e100, np.nan, last["predictions"][-1])
+    assert np.array_equal(saved, want, equal_nan=True)
+    print(f"{algorithm}: uncertified / full-search points per library size {counts}")
+
+
+def test_smap_sweep_full_size_bit_exact(mixed_ctx):
+    """Config 2 at full size: 10 000 library and 10 000 prediction rows,
+    k = all, all 81 thetas; forecasts and coefficients of a strided subset of
+    prediction rows against the oracle."""
+    w = workloads.smap_config()
+    kw = dict(E=5, theta=w["thetas"], algorithm="smap")
+    a = fedm.normalise(w["t"], w["x"], **kw)
+    usable = fedm.host_usable(a, 5)
+    lib, pred = w["library_rows"] & usable, w["prediction_rows"] & usable
+    g = mixed_ctx.run_task(a, lib, pred, 5, -1)
+    sub, sel = _strided(pred, 97)
+    o = _oracle(kw, w["t"], w["x"], None, lib, sub, 5, -1)
+    assert g["n_lib"] >= 9990 and g["n_pred"] >= 9990 and g["predictions"].shape[0] == 81 and len(sel) > 100
+    assert np.array_equal(g["predictions"][:, sel].view(np.int64), o["predictions"].view(np.int64))
+    assert np.array_equal(g["coeffs"][sel].view(np.int64), o["coeffs"].view(np.int64))
+    assert np.array_equal(g["kused"][sel], o["kused"])
+
+
+@pytest.mark.parametrize("panel_weight", [0.0, float("inf")], ids=["mixed_panels", "independent_panels"])
+@pytest.mark.parametrize("algorithm", ["simplex", "smap"])
+def test_panels_full_size_bit_exact(mixed_ctx, algorithm, panel_weight):
+    """Config 4 at full size: 512 panels of 50..2000 rows, 5% missing, dt,
+    E = 3..8 (E_actual 6..16); every E's task of run_command's plan."""
+    w = workloads.panel_config()
+    theta = [0.0, 1.0, 2.0, 4.0] if algorithm == "smap" else [1.0]
+    kw = dict(panel=w["panel"], E=[3, 4, 5, 6, 7, 8], dt=True, algorithm=algorithm, theta=theta,
+              panelWeight=panel_weight)
+    a = fedm.normalise(w["t"], w["x"], **kw)
+    plan = fedm.host_plan(a)
+    assert len(plan["E"]) == 6
+    for f in range(6):
+        E, k = int(plan["E"][f]), int(plan["k"][f])
+        g = mixed_ctx.run_task(a, plan["lib"][f], plan["pred"][f], E, k)
+        sub, sel = _strided(plan["pred"][f], 331, offset=f)
+        o = _oracle(kw, w["t"], w["x"], None, plan["lib"][f], sub, E, k)
+        assert g["n_pred"] > 100000 and len(sel) > 300
+        _compare_task(g, o, sel, (algorithm, panel_weight, E))
