@@ -108,7 +108,8 @@ def form_kernel(form, alg):
             2: "knn_smap_ws_kernel<E=4,C=8,4 solver warps>",
             3: "knn_smap_ws_kernel<E=4,C=8,8 solver warps>",
             4: f"knn_one_kernel wide form ({alg})",
-            5: f"knn_one_kernel<E=4,C=16,{alg},4 CTAs/SM>"}.get(int(form), "none")
+            5: f"knn_one_kernel<E=4,C=16,{alg},4 CTAs/SM>",
+            6: "knn_one_kernel<E=4,C=8,lists> + smap_list_kernel<4> (split S-map)"}.get(int(form), "none")
 
 
 def hbm_peak():
@@ -418,8 +419,17 @@ def cpu_baseline(fedm, w, a, reps=1, n_libs=None, stride=8):
 # the configuration through the library's C ABI from host buffers; `value`
 # is forecasts per second of device time, `e2e` per second of wall time.
 # They are measurements of the parity-test configurations, not the headline.
+# Each line carries the roofline of the configuration's dominant kernel
+# (algorithmic work per launch over its CUDA-event time, against this GPU's
+# measured rate for the pipe that bounds it) and the oracle on a bounded
+# sample of the same workload.
 def config_steps(fedm, workloads, ctx, name):
-    """Returns (description, step function -> list of (timing dict, wall s))."""
+    """Returns (description, step function -> list of (timing dict, wall s),
+    CPU-sample function -> (forecasts, seconds, description))."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import edm_oracle
+
+    cores = os.cpu_count() or 1
     if name == "simplex_explore":
         w = workloads.simplex_config()
         args = {E: fedm.normalise(w["t"], w["x"], E=E, theta=1.0) for E in w["Es"]}
@@ -431,22 +441,50 @@ def config_steps(fedm, workloads, ctx, name):
                 ctx.run_task(args[E], w["library_rows"], w["prediction_rows"], E, E + 1)
                 out.append((ctx.timing(), time.perf_counter() - t0))
             return out
-        return {"workload": "simplex_T500_lib250_pred250_E1-10_k=E+1", "T": 500}, step
+
+        def cpu():
+            t0 = time.perf_counter()
+            n = 0
+            for E in w["Es"]:
+                o = edm_oracle.oracle_task(edm_oracle.normalise(w["t"], w["x"], E=E, theta=1.0, numThreads=cores),
+                                           w["library_rows"], w["prediction_rows"], E, E + 1)
+                n += o["n_pred"]
+            return n, time.perf_counter() - t0, "the whole workload (E = 1..10)"
+        return {"workload": "simplex_T500_lib250_pred250_E1-10_k=E+1", "T": 500}, step, cpu
     if name == "smap_sweep":
         # edm()'s explore split of 20 000 rows: the first 9 998 usable rows
         # are the library, the other 9 998 the prediction set
         w = workloads.smap_config()
-        a_ = fedm.normalise(w["t"], w["x"], E=w["E"], theta=w["thetas"], algorithm="smap", k=float("inf"))
+        kw = dict(E=w["E"], theta=w["thetas"], algorithm="smap", k=float("inf"))
+        a_ = fedm.normalise(w["t"], w["x"], **kw)
 
         def step():
             t0 = time.perf_counter()
             ctx.run_command(a_)
             return [(ctx.timing(), time.perf_counter() - t0)]
-        return {"workload": "smap_kall_lib9998_pred9998_E5_theta0-8x81", "T": 20000}, step
-    if name == "panels":
+
+        def cpu(stride=97):
+            edm_oracle.set_pred_stride(stride)
+            try:
+                t0 = time.perf_counter()
+                edm_oracle.oracle_edm(w["t"], w["x"], numThreads=cores, **kw)
+                dt = time.perf_counter() - t0
+            finally:
+                edm_oracle.set_pred_stride(1)
+            n = len(range(0, 9998, stride)) * len(w["thetas"])
+            return n, dt, f"every {stride}th prediction row, all 81 thetas"
+        return {"workload": "smap_kall_lib9998_pred9998_E5_theta0-8x81", "T": 20000}, step, cpu
+    if name in ("panels", "panels_independent"):
+        # independent panels (panelWeight = Inf) are timed with two-fold
+        # cross-validation, so that every panel has library rows: under
+        # edm()'s default split the library is the first half of the rows,
+        # i.e. whole panels, and almost no prediction panel has a neighbour
         w = workloads.panel_config()
-        kws = [dict(panel=w["panel"], E=[3, 4, 5, 6, 7, 8], dt=True, algorithm="simplex"),
-               dict(panel=w["panel"], E=[3, 4, 5, 6, 7, 8], dt=True, algorithm="smap", theta=[0.0, 1.0, 2.0, 4.0])]
+        pw = float("inf") if name == "panels_independent" else 0.0
+        extra = dict(crossfold=2) if pw else {}
+        kws = [dict(panel=w["panel"], E=[3, 4, 5, 6, 7, 8], dt=True, algorithm="simplex", panelWeight=pw, **extra),
+               dict(panel=w["panel"], E=[3, 4, 5, 6, 7, 8], dt=True, algorithm="smap", theta=[0.0, 1.0, 2.0, 4.0],
+                    panelWeight=pw, **extra)]
 
         def step():
             out = []
@@ -455,8 +493,104 @@ def config_steps(fedm, workloads, ctx, name):
                 fedm.edm(w["t"], w["x"], ctx=ctx, **kw)
                 out.append((ctx.timing(), time.perf_counter() - t0))
             return out
-        return {"workload": f"panels{512}_rows{len(w['t'])}_E3-8_dt_simplex+smap4theta_mixed_library",
-                "rows": len(w["t"])}, step
+
+        def cpu(stride=1000 if pw == 0 else 50):
+            edm_oracle.set_pred_stride(stride)
+            n = 0
+            try:
+                t0 = time.perf_counter()
+                for kw in kws:
+                    r = edm_oracle.oracle_edm(w["t"], w["x"], numThreads=cores, **kw)
+                    n += len(r["stats"]["rho"])
+                dt = time.perf_counter() - t0
+            finally:
+                edm_oracle.set_pred_stride(1)
+            n_pred = int(fedm.host_plan(fedm.normalise(w["t"], w["x"], **kws[0]))["pred"][0].sum())
+            return n * len(range(0, n_pred, stride)), dt, f"every {stride}th prediction row, every E and theta"
+        mode = "independent_panels_crossfold2" if pw else "mixed_library"
+        return {"workload": f"panels512_rows{len(w['t'])}_E3-8_dt_simplex+smap4theta_{mode}",
+                "rows": len(w["t"]), "panelWeight": "Inf" if pw else 0}, step, cpu
+    if name == "easy_edm":
+        # easy_edm()'s default (quantile) workflow, R/easy_edm.R:40-433, on a
+        # coupled logistic pair of T = 5000: E search 3..10; a 101-theta
+        # S-map with k = Inf; S-maps with k = 20 at theta = 0 and at the best
+        # theta, 20 replicates each; a lag scan of 12 cross maps (simplex,
+        # k = Inf); the max-library call with saveManifolds; 1000 replicates
+        # at a tenth of the max library and one at the max library
+        # (simplex, k = Inf, shuffle).  One step is the whole sequence.
+        t, x, y = workloads.coupled_logistic(5000, seed=21)
+
+        def tslag(v, lag):
+            out = np.full(len(v), np.nan)
+            if lag >= 0:
+                out[lag:] = v[:len(v) - lag]
+            else:
+                out[:lag] = v[-lag:]
+            return out
+
+        def seq_calls():
+            r = yield dict(args=(t, x), kw=dict(E=list(range(3, 11))))
+            E = int(r["stats"]["E"][int(np.nanargmax(r["stats"]["rho"]))])
+            r = yield dict(args=(t, x), kw=dict(E=E, theta=list(np.linspace(0, 5, 101)), algorithm="smap",
+                                                 k=float("inf")))
+            th = float(r["stats"]["theta"][int(np.nanargmax(r["stats"]["rho"]))])
+            yield dict(args=(t, x), kw=dict(E=E, theta=0.0, numReps=20, k=20, algorithm="smap"))
+            yield dict(args=(t, x), kw=dict(E=E, theta=th, numReps=20, k=20, algorithm="smap"))
+            for lag in range(-5, 7):
+                yield dict(args=(t, x, tslag(y, lag)), kw=dict(E=E, theta=th, algorithm="simplex", k=float("inf")))
+            r = yield dict(args=(t, y), kw=dict(E=E, algorithm="simplex", full=True, saveManifolds=True))
+            lib_max = r["Ms"][0].shape[0]
+            small = max(E + 2, lib_max // 10)
+            yield dict(args=(t, y, x), kw=dict(E=E, library=small, numReps=1000, theta=th, algorithm="simplex",
+                                                k=float("inf"), shuffle=True))
+            yield dict(args=(t, y, x), kw=dict(E=E, library=lib_max, theta=th, algorithm="simplex",
+                                                k=float("inf"), shuffle=True))
+
+        def step():
+            out = []
+            gen = seq_calls()
+            call = next(gen)
+            while True:
+                t0 = time.perf_counter()
+                r = fedm.edm(*call["args"], ctx=ctx, **call["kw"])
+                if r["rc"] != 0:
+                    raise RuntimeError(f"easy_edm call rc={r['rc']}")
+                out.append((ctx.timing(), time.perf_counter() - t0))
+                try:
+                    call = gen.send(r)
+                except StopIteration:
+                    return out
+
+        def cpu():
+            # the sequence's calls on the oracle, the 1000-replicate call cut
+            # to 20 replicates, every 10th prediction row
+            edm_oracle.set_pred_stride(10)
+            n = 0
+            try:
+                t0 = time.perf_counter()
+                gen = seq_calls()
+                call = next(gen)
+                while True:
+                    kw = dict(call["kw"])
+                    if kw.get("numReps") == 1000:
+                        kw["numReps"] = 20
+                    r = edm_oracle.oracle_edm(*call["args"], numThreads=cores, **kw)
+                    if "Ms" not in r and kw.get("saveManifolds"):
+                        r["Ms"] = [np.zeros((len(t) - kw["E"], kw["E"]))]
+                    # prediction rows: half the usable rows when exploring,
+                    # all of them for cross maps and full
+                    half = len(call["args"]) == 2 and not kw.get("full")
+                    n_pred = (len(t) - kw["E"] if not half else (len(t) - kw["E"]) // 2)
+                    n += len(r["stats"]["rho"]) * ((n_pred + 9) // 10)
+                    try:
+                        call = gen.send(r)
+                    except StopIteration:
+                        break
+                dt = time.perf_counter() - t0
+            finally:
+                edm_oracle.set_pred_stride(1)
+            return n, dt, "the sequence with 20 instead of 1000 replicates, every 10th prediction row"
+        return {"workload": "easy_edm_quantile_T5000_Esearch3-10_theta101_reps20_lags12_ccm1000", "T": 5000}, step, cpu
     if name == "adjoint":
         w = workloads.lorenz_config()
         a_ = fedm.normalise(w["t"], w["x"], E=6, tau=5)
@@ -473,15 +607,116 @@ def config_steps(fedm, workloads, ctx, name):
             tm = ctx.timing()
             tm = dict(tm, predictions=len(pred_rows))
             return [(tm, time.perf_counter() - t0)]
-        return {"workload": "lorenz_smap_grad_kall_lib50000_pred20000_E6_tau5", "T": 100000}, step
+
+        def cpu(n=200):
+            t0 = time.perf_counter()
+            edm_oracle.smap_grad(lib, lib_t, pred[:n], pred_t[:n], 1.0, np.ones(6))
+            return n, time.perf_counter() - t0, f"the first {n} prediction points, forward and backward, 1 thread"
+        return {"workload": "lorenz_smap_grad_kall_lib50000_pred20000_E6_tau5", "T": 100000}, step, cpu
     raise ValueError(name)
+
+
+def config_roofline(name, precision, steps_tm, peaks):
+    """Roofline of a configuration's dominant kernel from the timings of one
+    step (a list of per-call timing dicts)."""
+    def tot(key):
+        return sum(tm[key] for tm in steps_tm)
+
+    if name == "simplex_explore":
+        # rows 0..E-2 of the explicit library lack lags, which keeps the
+        # tasks on the exact FP64 scan (3 E_a FP64 operations per pair,
+        # unfused) unless a mixed form reports it served them
+        ms = tot("knn_kernel_ms")
+        flops = tot("scan_flops")
+        mixed = any(tm["mixed_form"] >= 0 for tm in steps_tm)
+        peak = peaks["fp32"] if mixed else peaks["fp64_unfused"]
+        return {"kernel": "knn_one_kernel (FP32 scan + FP64 re-rank)" if mixed else
+                          "knn_exact_kernel (FP64 distances + exact top-k)",
+                "bound": "fp32_simt" if mixed else "fp64_simt",
+                "achieved": flops / (ms * 1e-3) / 1e12, "peak": peak, "unit": "TFLOP/s",
+                "frac": flops / (ms * 1e-3) / 1e12 / peak, "traffic": None,
+                "kernel_ms_per_step": ms, "launches_per_step": tot("knn_launches"),
+                "work": "3 E_actual operations per (prediction, library) pair",
+                "peak_source": "measured FFMA rate (fedm_measure_peak kind 0)" if mixed else
+                               "measured unfused FP64 multiply/add rate (fedm_measure_peak kind 3)"}
+    if name == "smap_sweep":
+        tm = steps_tm[0]
+        ms = tm["forecast_kernel_ms"]
+        E, n_th = 5, 81
+        n = E + 1
+        flops = 2.0 * tm["distance_pairs"] * n_th * (n * (n + 1) / 2 + n)
+        fast = precision == "fast"
+        peak = peaks["fp32"] if fast else peaks["fp64_unfused"]
+        return {"kernel": ("all_df_prep_kernel + all_smap_df_kernel<5> (FP32 weights, double-float normal "
+                           "equations)") if fast else "all_smap_kernel<5> (FP64 weights and normal equations)",
+                "bound": "fp32_simt" if fast else "fp64_simt", "achieved": flops / (ms * 1e-3) / 1e12,
+                "peak": peak, "unit": "TFLOP/s", "frac": flops / (ms * 1e-3) / 1e12 / peak, "traffic": None,
+                "kernel_ms_per_step": ms, "launches_per_step": tm["forecast_launches"],
+                "work": "2 N_p Theta N_L ((E_a+1)(E_a+2)/2 + E_a+1) flops of the weighted normal equations",
+                "peak_source": ("measured FFMA rate (fedm_measure_peak kind 0); each double-float multiply-add "
+                                "takes ~11 FP32 instructions") if fast else
+                               "measured unfused FP64 multiply/add rate (fedm_measure_peak kind 3)"}
+    if name in ("panels", "panels_independent"):
+        # two pipes share the kernel: the FP32 scan and the FP64 re-rank and
+        # S-map solves (up to 17 x 17 Jacobi SVDs at E = 8 with dt); the
+        # bound is the one with the larger fraction, the other is given beside
+        ms = tot("knn_kernel_ms")
+        flops = tot("scan_flops")
+        ops = tot("fp64_ops")
+        fp32 = {"achieved": flops / (ms * 1e-3) / 1e12, "peak": peaks["fp32"],
+                "frac": flops / (ms * 1e-3) / 1e12 / peaks["fp32"],
+                "work": "3 E_actual FP32 flops per (prediction, library) pair scanned" +
+                        (" (own-panel pairs only)" if name == "panels_independent" else ""),
+                "peak_source": "measured FFMA rate (fedm_measure_peak kind 0)"}
+        fp64 = {"achieved": ops / (ms * 1e-3) / 1e12, "peak": peaks["fp64_unfused"],
+                "frac": ops / (ms * 1e-3) / 1e12 / peaks["fp64_unfused"],
+                "work": "FP64 operations of the re-rank and forecasts, counted by the kernels",
+                "peak_source": "measured unfused FP64 multiply/add rate (fedm_measure_peak kind 3)"}
+        main, other, bound = (fp64, fp32, "fp64_simt") if fp64["frac"] >= fp32["frac"] else (fp32, fp64, "fp32_simt")
+        return {"kernel": "knn_one_kernel (one point per thread; wide form for E_a 10..16) + re-rank + forecast",
+                "bound": bound, "achieved": main["achieved"], "peak": main["peak"], "unit": "TFLOP/s",
+                "frac": main["frac"], "traffic": None, "kernel_ms_per_step": ms,
+                "launches_per_step": tot("knn_launches"), "work": main["work"], "peak_source": main["peak_source"],
+                "fp32" if bound == "fp64_simt" else "fp64": other}
+    if name == "easy_edm":
+        # the sequence mixes the exact FP64 neighbour search (k = 20), the
+        # mixed scan and the k = all forecasts; the figure is the FP64
+        # distance work (3 E_a per pair) over the neighbour and forecast
+        # kernels' time
+        ms = tot("knn_kernel_ms") + tot("forecast_kernel_ms")
+        flops = tot("scan_flops")
+        return {"kernel": "neighbour search + k = all forecast kernels over the sequence's 20 calls",
+                "bound": "fp64_simt", "achieved": flops / (ms * 1e-3) / 1e12, "peak": peaks["fp64_unfused"],
+                "unit": "TFLOP/s", "frac": flops / (ms * 1e-3) / 1e12 / peaks["fp64_unfused"], "traffic": None,
+                "kernel_ms_per_step": ms, "launches_per_step": tot("knn_launches") + tot("forecast_launches"),
+                "work": "3 E_actual operations per (prediction, library) pair scanned",
+                "peak_source": "measured unfused FP64 multiply/add rate (fedm_measure_peak kind 3)",
+                "per_call_ms": [{"device": tm["device_ms"], "host": tm["host_ms"], "prep": tm["prep_ms"],
+                                 "manifold": tm["manifold_ms"], "setup": tm["setup_ms"],
+                                 "finish": tm["finish_ms"]} for tm in steps_tm]}
+    if name == "adjoint":
+        tm = steps_tm[0]
+        ms = tm["knn_kernel_ms"]
+        E = 6
+        n = E + 1
+        per_pair = 2 * (n * (n + 1) / 2 + n) + 2 * (3 * E + 1) + 4 * n
+        flops = per_pair * 50000 * tm["predictions"]
+        return {"kernel": "smap_grad_kernel<6> (three passes per point: distances, normal equations, adjoint sums)",
+                "bound": "fp64_simt", "achieved": flops / (ms * 1e-3) / 1e12, "peak": peaks["fp64_fma"],
+                "unit": "TFLOP/s", "frac": flops / (ms * 1e-3) / 1e12 / peaks["fp64_fma"], "traffic": None,
+                "kernel_ms_per_step": ms, "launches_per_step": 1,
+                "work": f"{per_pair:.0f} flops per (prediction, library row): the normal equations "
+                        "2((E+1)(E+2)/2 + E+1), the adjoint sums 2(3E+1) and the residual and g.u products 4(E+1)",
+                "peak_source": "measured DFMA rate (fedm_measure_peak kind 1): the adjoint passes use FMA"}
+    return None
 
 
 def run_config(a):
     fedm, workloads = load_pkg()
     world, rank, local = dist_setup()
     ctx = fedm.Context(local, precision={"mixed": fedm.PRECISION_MIXED, "fast": fedm.PRECISION_FAST}[a.precision])
-    cfg, step = config_steps(fedm, workloads, ctx, a.workload)
+    peaks = {"fp32": ctx.measure_peak(0), "fp64_fma": ctx.measure_peak(1), "fp64_unfused": ctx.measure_peak(3)}
+    cfg, step, cpu = config_steps(fedm, workloads, ctx, a.workload)
     for _ in range(max(3, a.warmup)):
         step()
         flush_l2(local)
@@ -489,9 +724,12 @@ def run_config(a):
     dev = wall = 0.0
     preds = launches = fallback = exact = 0
     host = {k: 0.0 for k in ("host_ms", "prep_ms", "manifold_ms", "list_wait_ms", "setup_ms", "finish_ms")}
+    step_tms = []
     with Clocks(local) as clk:
         for _ in range(a.steps):
-            for tm, ws in step():
+            tms = step()
+            step_tms.append([tm for tm, _ in tms])
+            for tm, ws in tms:
                 dev += tm["device_ms"] / 1e3
                 wall += ws
                 preds += tm["predictions"]
@@ -505,6 +743,16 @@ def run_config(a):
     wall = allreduce_max(world, wall)
     if rank != 0:
         return
+    roof = config_roofline(a.workload, a.precision, step_tms[-1], peaks)
+    if roof is not None:
+        roof["share_of_device_time"] = roof["kernel_ms_per_step"] / (dev / a.steps * 1e3)
+    cpu_line = None
+    if world == 1 and not a.no_cpu:
+        n, dt, what = cpu()
+        cpu_line = {"value": n / dt, "unit": "predictions/s", "cores": os.cpu_count() or 1, "kind": "port",
+                    "sample": f"{what} ({n} forecasts, {dt:.1f} s)"}
+        if a.workload == "adjoint":
+            cpu_line["cores"] = 1
     cfg["l2"] = "flushed between steps (512 MiB write)"
     cfg["parallelism"] = f"replicas x{world}"
     out = {
@@ -516,7 +764,7 @@ def run_config(a):
                 "host_ms_per_step": {k: v / a.steps for k, v in host.items()}},
         "gpu_launches": launches, "predictions_per_step": preds // a.steps,
         "fallback_points_per_step": fallback // a.steps, "exact_points_per_step": exact // a.steps,
-        "roofline": None, "cpu_baseline": None,
+        "roofline": roof, "cpu_baseline": cpu_line,
         "clocks": clk.summary(),
     }
     print(json.dumps(out), flush=True)
@@ -572,7 +820,8 @@ def main():
                     help="context precision for the non-headline workloads: mixed (bit-exact) or fast (FP32 "
                          "weights and double-float normal equations for the k = all S-map)")
     ap.add_argument("--workload", default="ccm",
-                    choices=["ccm", "simplex_explore", "smap_sweep", "panels", "adjoint"],
+                    choices=["ccm", "simplex_explore", "smap_sweep", "panels", "panels_independent", "adjoint",
+                             "easy_edm"],
                     help="ccm (default): the headline CCM benchmark; the others time the other benchmark "
                          "configurations at full size")
     a = ap.parse_args()

@@ -48,11 +48,12 @@ Context::Context(int dev) : device(dev)
 {
   ck(cudaSetDevice(dev), "cudaSetDevice");
   ck(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking), "cudaStreamCreate");
+  ck(cudaStreamCreateWithFlags(&stream2, cudaStreamNonBlocking), "cudaStreamCreate");
   ck(cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, dev), "cudaDeviceGetAttribute");
   if (const char* v = std::getenv("FEDM_MIXED_KERNEL")) {
     static const std::pair<const char*, int> forms[] = {
       { "one6", MIXED_ONE6 }, { "fused2", MIXED_FUSED2 }, { "ws4", MIXED_WS4 }, { "ws8", MIXED_WS8 },
-      { "one16", MIXED_ONE16 }
+      { "one16", MIXED_ONE16 }, { "split", MIXED_SPLIT }
     };
     for (const auto& f : forms)
       if (std::strcmp(v, f.first) == 0) {
@@ -70,6 +71,12 @@ Context::Context(int dev) : device(dev)
       autotune = false;
   if (const char* v = std::getenv("FEDM_CTAS_PER_SM"))
     ctas_per_sm = std::max(0, std::atoi(v));
+  if (const char* v = std::getenv("FEDM_SPLIT_SCAN_CTAS"))
+    split_scan_ctas = std::max(1, std::atoi(v));
+  if (const char* v = std::getenv("FEDM_SPLIT_SOLVE_CTAS"))
+    split_solve_ctas = std::max(1, std::atoi(v));
+  if (const char* v = std::getenv("FEDM_SPLIT_CHUNK_POINTS"))
+    split_chunk_points = std::max(256LL, std::atoll(v));
   reset_timing();
 }
 
@@ -84,6 +91,8 @@ Context::~Context()
   cudaSetDevice(device);
   if (stream)
     cudaStreamSynchronize(stream);
+  if (stream2)
+    cudaStreamSynchronize(stream2);
   for (auto& kv : bufs_)
     if (kv.second.p)
       cudaFree(kv.second.p);
@@ -92,6 +101,8 @@ Context::~Context()
       cudaFreeHost(kv.second.p);
   if (stream)
     cudaStreamDestroy(stream);
+  if (stream2)
+    cudaStreamDestroy(stream2);
 }
 
 void* Context::host_buf(const std::string& name, size_t bytes)
@@ -253,6 +264,7 @@ struct DevRows
   float* id_w;
   int n_pid;
   int n_rows;
+  const int* panel_host;  // the generator's panel ids (host), null without panels
 };
 
 DevRows upload_rows(Context& ctx, const Generator& g, const RowTables& rt, const Options& o)
@@ -271,6 +283,7 @@ DevRows upload_rows(Context& ctx, const Generator& g, const RowTables& rt, const
   if (g.panel_mode) {
     d.panel = (int*)ctx.buf("panel", n * 4);
     ctx.upload(d.panel, g.panel.data(), n * 4);
+    d.panel_host = g.panel.data();
     if (o.has_id_weights) {
       std::vector<int> ids(g.panel);
       std::sort(ids.begin(), ids.end());
@@ -343,15 +356,18 @@ constexpr long long FB_CAP = 1 << 24;
 
 // Whether the mixed kernel's preconditions hold for a group (see
 // kernels_mixed.cu): L2, no missing values in any used row, no panel
-// penalty or restriction, no past-only rule, Ea <= 8.  Also returns the
-// per-column centre and the largest centred row norm.
-bool mixed_eligible(const Context& ctx, const Options& o, const GroupJob& job, std::vector<double>& center,
-                    double& R)
+// penalty (independent panels only through per-panel sub-tasks), no
+// past-only rule, Ea <= 16.  Also returns the per-column centre and the
+// largest centred row norm.
+bool mixed_eligible(const Context& ctx, const Options& o, const GroupJob& job, bool panel_split,
+                    std::vector<double>& center, double& R)
 {
   if (ctx.precision == FEDM_PRECISION_FP64 || o.distance != 1 || o.has_missing || o.low_memory || o.past_only ||
       !o.force_compute || job.Ea > WIDE_EA || job.Ea < 1 || !job.hF || !job.hFp)
     return false;
-  if (o.panel_mode && (o.idw != 0 || o.has_id_weights))
+  // a panel penalty or id weights change the distances; independent panels
+  // are served when every task is split into per-panel sub-tasks
+  if (o.panel_mode && (o.idw > 0 || o.has_id_weights || (o.idw < 0 && !panel_split)))
     return false;
   const int Ea = job.Ea;
   std::vector<double> lo(Ea, INFINITY), hi(Ea, -INFINITY);
@@ -432,12 +448,21 @@ void run_group(Context& ctx, const Options& o, const std::vector<Task>& tasks, c
   const int nth = (int)o.thetas.size();
   cudaStream_t s = ctx.stream;
 
+  // Independent panels (panelWeight = Inf): a point's neighbours come from
+  // its own panel only (src/distances.cpp:167-169), so every task runs as
+  // sub-tasks, one per run of same-panel prediction rows, each scanning the
+  // task's library rows of that panel.  A sub-list keeps library order, so
+  // positions, ties and the k rules are those of the whole list; rho/MAE,
+  // k and the outputs stay per task.
+  const bool split = o.panel_mode && o.idw < 0 && rows.panel_host != nullptr;
   std::vector<double> center;
   double R = 0;
-  const bool mixed_group = mixed_eligible(ctx, o, job, center, R);
+  const bool mixed_group = mixed_eligible(ctx, o, job, split, center, R);
 
-  // task table and row pools: offsets first, then the distinct lists copied
-  // in parallel into pinned host buffers, uploaded without staging
+  // task tables and row pools: offsets first, then the distinct lists copied
+  // in parallel into pinned host buffers, uploaded without staging.  dt has
+  // one entry per task (statistics, outputs); dk one per kernel task (the
+  // tasks themselves, or their per-panel sub-tasks), in point order.
   std::vector<DevTask> dt(nT);
   std::unordered_map<const std::vector<int>*, int> lib_off, pred_off;
   std::vector<const std::vector<int>*> lib_src, pred_src;
@@ -445,16 +470,25 @@ void run_group(Context& ctx, const Options& o, const std::vector<Task>& tasks, c
   long long P = 0, max_nlib_all = 1;
   int kcap = 1, kmix = 0;
   bool any_finite = false, any_all = false, any_coeffs = false, any_mixed = false;
+  struct PanelLists
+  {
+    std::unordered_map<int, int> of_panel;
+    std::vector<std::vector<int>> rows, pos;  // per panel: library rows, their positions in the list
+  };
+  std::unordered_map<const std::vector<int>*, PanelLists> panel_lists;
+  const std::vector<int> no_rows;
+  struct KTask
+  {
+    int parent;
+    const std::vector<int>* L;    // library rows scanned
+    const std::vector<int>* pos;  // their positions in the task's list (null: the list itself)
+    int pstart, plen;             // slice of the task's prediction rows
+  };
+  std::vector<KTask> kt;
   for (int j = 0; j < nT; j++) {
     const Task& t = tasks[job.task_ids[j]];
     const std::vector<int>* L = job.lib_lists[j];
     const std::vector<int>* Pl = job.pred_lists[j];
-    auto it = lib_off.find(L);
-    if (it == lib_off.end()) {
-      it = lib_off.emplace(L, (int)lib_total).first;
-      lib_src.push_back(L);
-      lib_total += (long long)L->size();
-    }
     auto it2 = pred_off.find(Pl);
     if (it2 == pred_off.end()) {
       it2 = pred_off.emplace(Pl, (int)pred_total).first;
@@ -463,7 +497,7 @@ void run_group(Context& ctx, const Options& o, const std::vector<Task>& tasks, c
     }
     DevTask& d = dt[j];
     d.point_base = P;
-    d.lib_off = it->second;
+    d.lib_off = 0;
     d.n_lib = (int)L->size();
     d.pred_off = it2->second;
     d.n_pred = (int)Pl->size();
@@ -492,11 +526,74 @@ void run_group(Context& ctx, const Options& o, const std::vector<Task>& tasks, c
     }
     any_coeffs |= (bool)d.save_coeffs && o.algorithm == 1;
     P += d.n_pred;
+    if (!split) {
+      kt.push_back(KTask{ j, L, nullptr, 0, d.n_pred });
+      continue;
+    }
+    auto pit = panel_lists.find(L);
+    if (pit == panel_lists.end()) {
+      pit = panel_lists.emplace(L, PanelLists{}).first;
+      PanelLists& pl = pit->second;
+      for (int q = 0; q < (int)L->size(); q++) {
+        const int pn = rows.panel_host[(*L)[q]];
+        auto f = pl.of_panel.find(pn);
+        if (f == pl.of_panel.end()) {
+          f = pl.of_panel.emplace(pn, (int)pl.rows.size()).first;
+          pl.rows.emplace_back();
+          pl.pos.emplace_back();
+        }
+        pl.rows[f->second].push_back((*L)[q]);
+        pl.pos[f->second].push_back(q);
+      }
+    }
+    const PanelLists& pl = pit->second;
+    for (int i = 0; i < d.n_pred;) {
+      const int pn = rows.panel_host[(*Pl)[i]];
+      int e = i + 1;
+      while (e < d.n_pred && rows.panel_host[(*Pl)[e]] == pn)
+        e++;
+      auto f = pl.of_panel.find(pn);
+      if (f == pl.of_panel.end())
+        kt.push_back(KTask{ j, &no_rows, &no_rows, i, e - i });
+      else
+        kt.push_back(KTask{ j, &pl.rows[f->second], &pl.pos[f->second], i, e - i });
+      i = e;
+    }
   }
+  const int nK = (int)kt.size();
+  std::vector<DevTask> dk(nK);
+  std::vector<long long> kbase(nK);
+  for (int q = 0; q < nK; q++) {
+    const KTask& kq = kt[q];
+    auto it = lib_off.find(kq.L);
+    if (it == lib_off.end()) {
+      it = lib_off.emplace(kq.L, (int)lib_total).first;
+      lib_src.push_back(kq.L);
+      lib_total += (long long)kq.L->size();
+    }
+    DevTask d = dt[kq.parent];
+    d.point_base += kq.pstart;
+    d.pred_off += kq.pstart;
+    d.n_pred = kq.plen;
+    d.lib_off = it->second;
+    d.n_lib = (int)kq.L->size();
+    dk[q] = d;
+    kbase[q] = d.point_base;
+  }
+  for (const DevTask& d : dk)
+    ctx.timing.scan_flops += 3LL * Ea * d.n_pred * (long long)d.n_lib;
+  // library position of slot v of point p in its task's list (detail mode)
+  auto task_pos = [&](long long p, int v) {
+    if (!split)
+      return v;
+    const int q = (int)(std::upper_bound(kbase.begin(), kbase.end(), p) - kbase.begin()) - 1;
+    return (*kt[q].pos)[v];
+  };
   if (Ea + 32 * (n + 1) + n * (n + 1) / 2 + n > 24000 && any_all && o.algorithm == 1)
     throw Error{ RC_NOT_IMPLEMENTED, "embedding too wide for the all-neighbour S-map" };
 
-  DevTask* d_tasks = (DevTask*)ctx.buf("tasks", dt.size() * sizeof(DevTask));
+  DevTask* d_tasks = (DevTask*)ctx.buf("tasks", std::max<size_t>(dk.size(), 1) * sizeof(DevTask));
+  DevTask* d_ptasks = (DevTask*)ctx.buf("ptasks", dt.size() * sizeof(DevTask));
   if (lib_total > INT_MAX || pred_total > INT_MAX)
     throw Error{ RC_NOT_IMPLEMENTED, "row pool of a task batch above 2^31 rows" };
   // an upload from these buffers by an earlier call that ended in an error
@@ -526,7 +623,8 @@ void run_group(Context& ctx, const Options& o, const std::vector<Task>& tasks, c
   int* d_lib = (int*)ctx.buf("lib_pool", (size_t)std::max<long long>(lib_total, 1) * 4);
   int* d_pred = (int*)ctx.buf("pred_pool", (size_t)std::max<long long>(pred_total, 1) * 4);
   double* d_thetas = (double*)ctx.buf("thetas", nth * 8);
-  ctx.upload(d_tasks, dt.data(), dt.size() * sizeof(DevTask));
+  ctx.upload(d_tasks, dk.data(), dk.size() * sizeof(DevTask));
+  ctx.upload(d_ptasks, dt.data(), dt.size() * sizeof(DevTask));
   ctx.upload(d_lib, h_lib, (size_t)lib_total * 4);
   ctx.upload(d_pred, h_pred, (size_t)pred_total * 4);
   ctx.upload(d_thetas, o.thetas.data(), nth * 8);
@@ -545,7 +643,7 @@ void run_group(Context& ctx, const Options& o, const std::vector<Task>& tasks, c
   g.lib_rows = d_lib;
   g.pred_rows = d_pred;
   g.tasks = d_tasks;
-  g.n_tasks = nT;
+  g.n_tasks = nK;
   g.Ea = Ea;
   g.n_thetas = nth;
   g.thetas = d_thetas;
@@ -660,12 +758,16 @@ void run_group(Context& ctx, const Options& o, const std::vector<Task>& tasks, c
         continue;
       pt_idx[p].assign(h_idx.begin() + q * kcap, h_idx.begin() + q * kcap + h_cnt[q]);
       pt_dist[p].assign(h_dist.begin() + q * kcap, h_dist.begin() + q * kcap + h_cnt[q]);
+      for (int& v : pt_idx[p])
+        v = task_pos(p, v);
     }
   };
 
-  cudaEvent_t e0, e1;
+  cudaEvent_t e0, e1, f0, f1;
   ck(cudaEventCreate(&e0), "event");
   ck(cudaEventCreate(&e1), "event");
+  ck(cudaEventCreate(&f0), "event");
+  ck(cudaEventCreate(&f1), "event");
   float knn_ms = 0;
   auto timed = [&](auto&& launch) {
     ck(cudaEventRecord(e0, s), "event");
@@ -708,8 +810,13 @@ void run_group(Context& ctx, const Options& o, const std::vector<Task>& tasks, c
         rdist = (float*)ctx.buf("df_rdist", (size_t)(c.p_end - c.p_begin) * max_nlib_all * 4);
         means = (double*)ctx.buf("df_means", (size_t)(c.p_end - c.p_begin) * 8);
       }
-      launch_all_mode(g, c, ctx.num_sms, max_nlib_all, s, gram_terms, rdist, means);
+      launch_all_mode(g, c, ctx.num_sms, max_nlib_all, s, gram_terms, rdist, means, f0, f1);
       ctx.check("all_mode");
+      ck(cudaEventSynchronize(f1), "sync");
+      float ms = 0;
+      cudaEventElapsedTime(&ms, f0, f1);
+      ctx.timing.forecast_kernel_ms += ms;
+      ctx.timing.forecast_launches += 1;
       ctx.timing.kernel_launches += o.algorithm == 1 ? (gram_terms ? 3 : 2) : 1;
     }
   };
@@ -730,6 +837,8 @@ void run_group(Context& ctx, const Options& o, const std::vector<Task>& tasks, c
       const bool ws = o.algorithm == 1 && (form == MIXED_WS4 || form == MIXED_WS8);
       return form != MIXED_FUSED2 && form != MIXED_ONE16 && !ws;
     };
+    // the split S-map serves E_a <= 4 with at most six neighbours
+    const bool split_ok = o.algorithm == 1 && !wide && C == 8 && kmix <= SPLIT_SLOTS && Ea <= SPLIT_MAX_EA;
     auto points_per_item = [&](int form) { return (wide || is_one(form)) ? WIDE_POINTS : MIX_POINTS; };
     const long long nrows = (long long)rows.n_rows;
     double* d_center = (double*)ctx.buf("center", Ea * 8);
@@ -742,10 +851,10 @@ void run_group(Context& ctx, const Options& o, const std::vector<Task>& tasks, c
       center_to_f32(job.dFp, nrows, Ea, d_center, Fp32, S, s);
     }
     std::vector<int> order;
-    for (int j = 0; j < nT; j++)
-      if (dt[j].mixed)
+    for (int j = 0; j < nK; j++)
+      if (dk[j].mixed)
         order.push_back(j);
-    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return dt[a].n_lib > dt[b].n_lib; });
+    std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return dk[a].n_lib > dk[b].n_lib; });
     // work items of the tasks in LPT order, up to the task that takes the
     // count of points past max_points
     auto items_of = [&](int per_item, long long max_points) {
@@ -754,17 +863,17 @@ void run_group(Context& ctx, const Options& o, const std::vector<Task>& tasks, c
       for (int j : order) {
         if (covered >= max_points)
           break;
-        for (int b = 0; b < dt[j].n_pred; b += per_item)
+        for (int b = 0; b < dk[j].n_pred; b += per_item)
           it.push_back(make_int2(j, b));
-        covered += dt[j].n_pred;
+        covered += dk[j].n_pred;
       }
       return it;
     };
     long long mixed_points = 0;
     size_t max_items = 1;
     for (int j : order) {
-      mixed_points += dt[j].n_pred;
-      max_items += (dt[j].n_pred + WIDE_POINTS - 1) / WIDE_POINTS;
+      mixed_points += dk[j].n_pred;
+      max_items += (dk[j].n_pred + WIDE_POINTS - 1) / WIDE_POINTS;
     }
     MixedRun m{};
     m.F32 = F32;
@@ -792,10 +901,63 @@ void run_group(Context& ctx, const Options& o, const std::vector<Task>& tasks, c
     ctx.timing.kernel_launches += (job.dFp != job.dF ? 2 : 1) + 1;  // centring, counter fill
     m.kslots = C;
     m.ctas_per_sm = ctx.ctas_per_sm;
+    // The split S-map: the items in chunks; the scan of a chunk writes its
+    // neighbour lists into one of three list buffers on the main stream,
+    // and the solves of that chunk run on the second stream while the next
+    // chunk is scanned.  A buffer is rescanned only after its solves are
+    // done; the main stream waits for the last solve.
+    constexpr int SPLIT_BUFS = 3;
+    cudaEvent_t scan_ev[SPLIT_BUFS] = {}, solve_ev[SPLIT_BUFS] = {}, split_done = nullptr;
+    auto split_pipeline = [&]() {
+      const int ib0 = m.item_begin, ie0 = m.item_end;
+      const long long items = ie0 - ib0;
+      if (items <= 0)
+        return;
+      long long nchunks = std::max<long long>(4, (items * WIDE_POINTS + ctx.split_chunk_points - 1) /
+                                                     ctx.split_chunk_points);
+      nchunks = std::min(nchunks, items);
+      const long long per_chunk = (items + nchunks - 1) / nchunks;
+      const long long lslots = per_chunk * WIDE_POINTS;
+      int* keff = (int*)ctx.buf("split_keff", (size_t)SPLIT_BUFS * lslots * 4);
+      int* lrows = (int*)ctx.buf("split_rows", (size_t)SPLIT_BUFS * SPLIT_SLOTS * lslots * 4);
+      double* ldist = (double*)ctx.buf("split_dist", (size_t)SPLIT_BUFS * SPLIT_SLOTS * lslots * 8);
+      if (!split_done) {
+        for (int b = 0; b < SPLIT_BUFS; b++) {
+          ck(cudaEventCreateWithFlags(&scan_ev[b], cudaEventDisableTiming), "event");
+          ck(cudaEventCreateWithFlags(&solve_ev[b], cudaEventDisableTiming), "event");
+        }
+        ck(cudaEventCreateWithFlags(&split_done, cudaEventDisableTiming), "event");
+      }
+      for (long long c = 0; c * per_chunk < items; c++) {
+        const int b = (int)(c % SPLIT_BUFS);
+        if (c >= SPLIT_BUFS)
+          ck(cudaStreamWaitEvent(s, solve_ev[b], 0), "wait");
+        MixedRun mc = m;
+        mc.item_begin = (int)(ib0 + c * per_chunk);
+        mc.item_end = (int)std::min<long long>(ie0, ib0 + (c + 1) * per_chunk);
+        mc.l_keff = keff + b * lslots;
+        mc.l_rows = lrows + (size_t)b * SPLIT_SLOTS * lslots;
+        mc.l_dist = ldist + (size_t)b * SPLIT_SLOTS * lslots;
+        mc.l_slots = lslots;
+        mc.ctas_per_sm = ctx.ctas_per_sm > 0 ? std::min(ctx.ctas_per_sm, ctx.split_scan_ctas) : ctx.split_scan_ctas;
+        ck(cudaMemsetAsync(m.counter, 0, 4, s), "memset");  // the queue head
+        launch_smap_scan_lists(g, mc, ctx.num_sms, s);
+        ck(cudaEventRecord(scan_ev[b], s), "event");
+        ck(cudaStreamWaitEvent(ctx.stream2, scan_ev[b], 0), "wait");
+        const SolveRun r{ m.items, mc.item_begin, mc.item_end, mc.l_keff, mc.l_rows, mc.l_dist, lslots, m.fp64_ops };
+        launch_smap_lists(g, r, ctx.num_sms, ctx.split_solve_ctas, ctx.stream2);
+        ck(cudaEventRecord(solve_ev[b], ctx.stream2), "event");
+        ctx.timing.kernel_launches += 2;
+      }
+      ck(cudaEventRecord(split_done, ctx.stream2), "event");
+      ck(cudaStreamWaitEvent(s, split_done, 0), "wait");
+    };
     auto launch_form = [&](int form) {
       m.form = form;
       if (wide)
         launch_knn_wide(g, m, ctx.num_sms, s);
+      else if (form == MIXED_SPLIT && split_ok)
+        split_pipeline();
       else if (is_one(form) && C == 16)
         launch_mixed_one16(g, m, ctx.num_sms, s);
       else if (is_one(form))
@@ -831,6 +993,7 @@ void run_group(Context& ctx, const Options& o, const std::vector<Task>& tasks, c
           cands = { MIXED_ONE16, MIXED_FUSED2 };
         else if (o.algorithm == 1)
           cands.push_back(MIXED_WS8);
+
         std::vector<float> best(cands.size(), INFINITY);
         for (int f : cands) {
           fill_i32(m.counter, 8, 0, s);
@@ -876,8 +1039,12 @@ void run_group(Context& ctx, const Options& o, const std::vector<Task>& tasks, c
         ctx.tuned_forms[key] = form;
       }
     }
+    if (form == MIXED_SPLIT && !split_ok)
+      form = MIXED_ONE6;  // a context fixed to the split form, on a shape it does not serve
     if (wide)
       ctx.timing.mixed_form = MIXED_WIDE;
+    else if (form == MIXED_SPLIT)
+      ctx.timing.mixed_form = MIXED_SPLIT;
     else if (is_one(form))
       ctx.timing.mixed_form = C == 16 ? MIXED_ONE16 : MIXED_ONE6;
     else
@@ -894,6 +1061,13 @@ void run_group(Context& ctx, const Options& o, const std::vector<Task>& tasks, c
       throw Error{ RC_UNKNOWN_ERROR, "mixed S-map kernel: scan/solve hand-off timed out" };
     ctx.timing.fallback_points += nfb;
     ctx.timing.fp64_ops += (long long)nops;
+    if (split_done) {
+      for (int b = 0; b < SPLIT_BUFS; b++) {
+        cudaEventDestroy(scan_ev[b]);
+        cudaEventDestroy(solve_ev[b]);
+      }
+      cudaEventDestroy(split_done);
+    }
     if (job.detail) {
       std::vector<int> ku(P), mi((size_t)P * C);
       std::vector<double> md((size_t)P * C);
@@ -901,19 +1075,22 @@ void run_group(Context& ctx, const Options& o, const std::vector<Task>& tasks, c
       ctx.download(mi.data(), m.nn_idx, (size_t)P * C * 4);
       ctx.download(md.data(), m.nn_dist, (size_t)P * C * 8);
       ck(cudaStreamSynchronize(s), "sync");
-      for (int j = 0; j < nT; j++)
-        if (dt[j].mixed)
-          for (long long p = dt[j].point_base; p < dt[j].point_base + dt[j].n_pred; p++)
+      for (int j = 0; j < nK; j++)
+        if (dk[j].mixed)
+          for (long long p = dk[j].point_base; p < dk[j].point_base + dk[j].n_pred; p++)
             if (ku[p] != MISSING_I) {
               pt_idx[p].assign(mi.begin() + p * C, mi.begin() + p * C + ku[p]);
               pt_dist[p].assign(md.begin() + p * C, md.begin() + p * C + ku[p]);
+              if (kt[j].pos)
+                for (int& v : pt_idx[p])
+                  v = (*kt[j].pos)[v];
             }
     }
     if (nfb > m.fb_cap) {
       // too many uncertified points: run every mixed task exactly
-      for (auto& d : dt)
+      for (auto& d : dk)
         d.mixed = 0;
-      ctx.upload(d_tasks, dt.data(), dt.size() * sizeof(DevTask));
+      ctx.upload(d_tasks, dk.data(), dk.size() * sizeof(DevTask));
       fill_f64(g.pred, P * nth, MISSING_D, s);
       if (g.coeffs)
         fill_f64(g.coeffs, P * n, MISSING_D, s);
@@ -991,11 +1168,16 @@ void run_group(Context& ctx, const Options& o, const std::vector<Task>& tasks, c
   ctx.timing.knn_kernel_ms += knn_ms;
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
+  cudaEventDestroy(f0);
+  cudaEventDestroy(f1);
 
   // statistics
   double* d_rho = (double*)ctx.buf("rho", (size_t)nT * nth * 8);
   double* d_mae = (double*)ctx.buf("mae", (size_t)nT * nth * 8);
-  launch_stats(g, nullptr, nT, d_rho, d_mae, s);
+  GroupParams gt = g;  // per task, not per kernel task
+  gt.tasks = d_ptasks;
+  gt.n_tasks = nT;
+  launch_stats(gt, nullptr, nT, d_rho, d_mae, s);
   ctx.check("stats");
   ctx.timing.kernel_launches += 1;
   ck(cudaEventRecord(ge, s), "event");

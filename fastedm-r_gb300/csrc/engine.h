@@ -27,8 +27,8 @@ public:
   int precision = FEDM_PRECISION_MIXED;
   int (*keep_going)(void) = nullptr;
   // Kernel form of the mixed path (MixedForm in kernels.h); the environment
-  // variable FEDM_MIXED_KERNEL (one6, fused2, ws4, ws8) overrides it when
-  // the context is created.
+  // variable FEDM_MIXED_KERNEL (one6, fused2, ws4, ws8, split, one16)
+  // overrides it when the context is created.
   int mixed_form = MIXED_ONE6;     // for k <= 6
   int mixed_form16 = MIXED_ONE16;  // for 7 <= k <= 14
   // With autotune on (the default; FEDM_AUTOTUNE=0 or a named form turns it
@@ -39,6 +39,13 @@ public:
   // as many as fit), so that calls from other contexts can share the SMs;
   // FEDM_CTAS_PER_SM sets it when the context is created.
   int ctas_per_sm = 0;
+  // The split S-map (MIXED_SPLIT): a second stream for the solves, the
+  // scan's and the solver's resident CTAs per SM (FEDM_SPLIT_SCAN_CTAS,
+  // FEDM_SPLIT_SOLVE_CTAS) and the points per chunk of the pipeline.
+  cudaStream_t stream2 = nullptr;
+  int split_scan_ctas = 3;
+  int split_solve_ctas = 2;
+  long long split_chunk_points = 4 << 20;
   std::map<std::array<int, 3>, int> tuned_forms;
   std::string last_error;
   fedm_timing timing{};

@@ -102,8 +102,11 @@ struct ChunkBuffers
 void launch_knn_exact(const GroupParams& g, const ChunkBuffers& c, int num_sms, cudaStream_t s);
 void launch_simplex_nn(const GroupParams& g, const ChunkBuffers& c, cudaStream_t s);
 void launch_smap_nn(const GroupParams& g, const ChunkBuffers& c, int num_sms, cudaStream_t s);
+// ev0 / ev1 (optional) are recorded around the forecast kernel, after the
+// distance pass.
 void launch_all_mode(const GroupParams& g, const ChunkBuffers& c, int num_sms, long long max_nlib, cudaStream_t s,
-                     const float2* gram_terms = nullptr, float* rdist = nullptr, double* means = nullptr);
+                     const float2* gram_terms = nullptr, float* rdist = nullptr, double* means = nullptr,
+                     cudaEvent_t ev0 = nullptr, cudaEvent_t ev1 = nullptr);
 // FAST precision, k = all S-map (E_a <= 8): per library-pool row the
 // n(n+1)/2 + n Gram and right-hand-side products as float pairs; *bad is set
 // when a product is not below 1e30 in magnitude.  launch_all_mode then also
@@ -125,7 +128,8 @@ enum MixedForm
   MIXED_WS4 = 2,     // S-map: knn_smap_ws_kernel, 8 scan warps, 4 FP64 solver warps
   MIXED_WS8 = 3,     // S-map: knn_smap_ws_kernel, 8 scan warps, 8 FP64 solver warps
   MIXED_WIDE = 4,    // knn_one_kernel's wide form (E_a 9..16), chosen by E_a; reported in timings only
-  MIXED_ONE16 = 5    // 7 <= k <= 14: knn_one_kernel with 16 candidate slots, four CTAs per SM
+  MIXED_ONE16 = 5,   // 7 <= k <= 14: knn_one_kernel with 16 candidate slots, four CTAs per SM
+  MIXED_SPLIT = 6    // S-map, k <= 6: scan writes neighbour lists, smap_list_kernel solves in registers
 };
 
 // Mixed-precision neighbour scan for the common case (L2, no missing values,
@@ -156,9 +160,36 @@ struct MixedRun
   int ctas_per_sm;     // cap on resident CTAs per SM for the persistent grid (0: as many as fit)
   int item_begin;      // first item of this launch (the queue head starts here)
   int item_end;        // one past the last item of this launch
+  // S-map lists (the scan of the split S-map, MIXED_SPLIT): per point slot
+  // (item - item_begin) * 256 + thread, the neighbours a forecast uses
+  int* l_keff;         // [slots] neighbours used; 0: no forecast to make
+  int* l_rows;         // [L x slots] their library manifold rows
+  double* l_dist;      // [L x slots] their FP64 distances
+  long long l_slots;   // slots of the list buffers (the stride of l_rows / l_dist)
 };
 
 void launch_knn_mixed(const GroupParams& g, const MixedRun& m, int C, int num_sms, cudaStream_t s);
+
+// The split S-map (E_a <= 4, k <= 6; kernels_split.cu).  The scan
+// (knn_one_kernel's list form: FP32 scan, certification, FP64 re-rank)
+// writes every point's neighbour list; smap_list_kernel then makes the
+// forecasts with the whole JacobiSVD in registers, a few warps per SM,
+// alongside the next chunk's scan on another stream.  Bits are those of the
+// fused form.
+constexpr int SPLIT_SLOTS = 6;  // neighbours a list holds (k <= 6)
+constexpr int SPLIT_MAX_EA = 4;
+struct SolveRun
+{
+  const int2* items;   // the scan's work items
+  int item_begin, item_end;
+  const int* l_keff;
+  const int* l_rows;
+  const double* l_dist;
+  long long l_slots;
+  unsigned long long* fp64_ops;  // optional: FP64 operations of the solves
+};
+void launch_smap_scan_lists(const GroupParams& g, const MixedRun& m, int num_sms, cudaStream_t s);
+void launch_smap_lists(const GroupParams& g, const SolveRun& r, int num_sms, int ctas_per_sm, cudaStream_t s);
 
 // Points the mixed kernels could not certify (ChunkBuffers::plist): the rows
 // whose FP32 value is within the certified bound, scored in FP64 and ranked

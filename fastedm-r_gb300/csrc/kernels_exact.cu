@@ -1141,21 +1141,13 @@ void launch_gram_terms(const GroupParams& g, long long pool_size, float2* P, int
   }
 }
 
-void launch_all_mode(const GroupParams& g, const ChunkBuffers& c, int num_sms, long long max_nlib, cudaStream_t s,
+namespace {
+
+void launch_forecast(const GroupParams& g, const ChunkBuffers& c, long long max_nlib, cudaStream_t s,
                      const float2* gram_terms, float* rdist, double* means)
 {
-  int per_warp;
-  const int w = all_warps_per_block(g.Ea, per_warp);
   const long long chunk = c.p_end - c.p_begin;
-  long long blocks = (chunk + w - 1) / w;
-  if (blocks > (long long)num_sms * 64)
-    blocks = (long long)num_sms * 64;
-  if (blocks < 1)
-    blocks = 1;
-  all_dist_kernel<<<(int)blocks, 32 * w, (size_t)w * per_warp, s>>>(g, c, max_nlib, per_warp);
   const long long total = chunk * g.n_thetas;
-  if (total <= 0)
-    return;
   const int fb = (int)((total + 127) / 128);
   if (g.algorithm == 1 && g.Ea <= 8 && gram_terms && rdist && means) {
     all_df_prep_kernel<<<(int)((chunk * 32 + 127) / 128), 128, 0, s>>>(g, c, max_nlib, rdist, means);
@@ -1185,6 +1177,29 @@ void launch_all_mode(const GroupParams& g, const ChunkBuffers& c, int num_sms, l
     }
   }
   all_forecast_kernel<<<fb, 128, 0, s>>>(g, c, max_nlib, all_mode_slab(g.Ea));
+}
+
+} // namespace
+
+void launch_all_mode(const GroupParams& g, const ChunkBuffers& c, int num_sms, long long max_nlib, cudaStream_t s,
+                     const float2* gram_terms, float* rdist, double* means, cudaEvent_t ev0, cudaEvent_t ev1)
+{
+  int per_warp;
+  const int w = all_warps_per_block(g.Ea, per_warp);
+  const long long chunk = c.p_end - c.p_begin;
+  long long blocks = (chunk + w - 1) / w;
+  if (blocks > (long long)num_sms * 64)
+    blocks = (long long)num_sms * 64;
+  if (blocks < 1)
+    blocks = 1;
+  all_dist_kernel<<<(int)blocks, 32 * w, (size_t)w * per_warp, s>>>(g, c, max_nlib, per_warp);
+  if (chunk * g.n_thetas <= 0)
+    return;
+  if (ev0)
+    cudaEventRecord(ev0, s);
+  launch_forecast(g, c, max_nlib, s, gram_terms, rdist, means);
+  if (ev1)
+    cudaEventRecord(ev1, s);
 }
 
 void launch_stats(const GroupParams& g, const DevTask*, int n_tasks, double* rho, double* mae, cudaStream_t s)

@@ -112,7 +112,26 @@ __global__ void __launch_bounds__(NT, OCC) knn_one_kernel(GroupParams g, MixedRu
     int prow0;
     bool a0;
     scan_item_one<EA, C, RS, TR, NT>(g, m, T, it.y, tid, tile, c0, prow0, a0);
-    if (a0) {
+    if constexpr (ALG == 2) {
+      // S-map lists for smap_list_kernel: settle the neighbours, write them
+      const long long slot = (long long)(item - m.item_begin) * NT + tid;
+      int keff = 0, iops = 0;
+      int rows[C + ZCAP];
+      double cd[C + ZCAP];
+      if (a0) {
+        const Cand<C> c = c0;
+        if (!prepare_point<EA, C>(g, m, T, T.point_base + it.y + tid, prow0, c, keff, rows, cd, iops))
+          keff = 0;
+      }
+      m.l_keff[slot] = keff;
+#pragma unroll
+      for (int j = 0; j < SPLIT_SLOTS; j++)
+        if (j < keff) {
+          m.l_rows[j * m.l_slots + slot] = rows[j];
+          m.l_dist[j * m.l_slots + slot] = cd[j];
+        }
+      ops += iops;
+    } else if (a0) {
       const Cand<C> c = c0;
       ops += finalize_point<EA, C, ALG>(g, m, T, T.point_base + it.y + tid, prow0, c);
     }

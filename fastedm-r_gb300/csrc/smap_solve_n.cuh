@@ -1,7 +1,8 @@
 // The JacobiSVD restatement of smap_solve.cuh for a compile-time size N,
 // fully unrolled so the work matrix lives in registers.  The two rotation
-// accumulators U and V are reached through an accessor (StridedMat: a
-// per-thread slice of shared memory interleaved across threads).  Every floating-point operation and
+// accumulators U and V are reached through accessors (StridedMat: a
+// per-thread slice of shared memory interleaved across threads; or a matrix
+// held in registers).  Every floating-point operation and
 // its order are those of svd_solve(): the results are the same bits.
 #pragma once
 
@@ -24,9 +25,9 @@ struct StridedMat
 
 // ops accumulates the FP64 add/sub/mul/div/sqrt operations performed, with
 // the same rules as svd_solve.
-template<int N, class M>
+template<int N, class M, class MV>
 __device__ __forceinline__ void svd_solve_nm(double (&W)[N][N], const double (&b)[N], double (&x)[N], const M& U,
-                                             const M& V, int& ops)
+                                             const MV& V, int& ops)
 {
   const double tiny = DBL_MIN, eps = DBL_EPSILON;
   double scale = 0;

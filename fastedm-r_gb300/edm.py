@@ -74,7 +74,8 @@ class Timing(C.Structure):
         ("kernel_launches", C.c_int), ("fp64_ops", C.c_longlong), ("list_wait_ms", C.c_double),
         ("setup_ms", C.c_double), ("finish_ms", C.c_double), ("exact_points", C.c_int),
         ("mixed_form", C.c_int), ("autotune_probes", C.c_int), ("prep_ms", C.c_double),
-        ("manifold_ms", C.c_double),
+        ("manifold_ms", C.c_double), ("scan_flops", C.c_longlong), ("forecast_kernel_ms", C.c_double),
+        ("forecast_launches", C.c_int),
     ]
 
 

@@ -231,6 +231,12 @@ typedef struct fedm_timing {
   double prep_ms;            /* host time before the first batch: argument
                                 handling, usable rows, task plan, row tables */
   double manifold_ms;        /* host time building and uploading manifolds  */
+  long long scan_flops;      /* 3 * E_actual per (prediction, library) pair
+                                the neighbour kernels scan (per-panel pairs
+                                under independent panels)                    */
+  double forecast_kernel_ms; /* k = all: time of the forecast kernels after
+                                the distance pass (CUDA events)              */
+  int forecast_launches;     /* their launches                               */
 } fedm_timing;
 
 int fedm_last_timing(const fedm_ctx* ctx, fedm_timing* out);

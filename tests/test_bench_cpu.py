@@ -26,7 +26,12 @@ class FakeContext:
         return {0: 78.0, 1: 1.05, 2: 65.0, 3: 0.53}[kind]
 
     def run_command(self, args):
-        return {"rc": 0, "stats": {"rho": np.zeros(4)}}
+        n = len(args["Es"]) * len(args["thetas"])
+        out = {"rc": 0, "stats": {"rho": np.linspace(0.1, 0.9, n), "E": np.repeat(args["Es"], len(args["thetas"])),
+                                  "theta": np.tile(args["thetas"], len(args["Es"]))}}
+        if args["save_manifolds"]:
+            out["Ms"] = [np.zeros((args["n"] // 2, args["Es"][0]))]
+        return out
 
     def run_task(self, *a, **k):
         return {}
@@ -38,7 +43,8 @@ class FakeContext:
         return dict(device_ms=100.0, knn_kernel_ms=90.0, knn_launches=1, host_ms=101.0, distance_pairs=10**9,
                     predictions=10**6, h2d_bytes=1000, d2h_bytes=100, fallback_points=3, kernel_launches=10,
                     fp64_ops=10**10, list_wait_ms=1.0, setup_ms=2.0, finish_ms=0.5, exact_points=1, mixed_form=1,
-                    autotune_probes=0, prep_ms=0.3, manifold_ms=0.2)
+                    autotune_probes=0, prep_ms=0.3, manifold_ms=0.2, scan_flops=12 * 10**9,
+                    forecast_kernel_ms=80.0, forecast_launches=1)
 
     def close(self):
         pass
@@ -106,12 +112,22 @@ def test_headline_line(bench, monkeypatch):
     assert d["concurrent_calls"]["value"] > 0 and d["concurrent_calls"]["rho_identical_to_sequential"]
 
 
-@pytest.mark.parametrize("workload", ["simplex_explore", "smap_sweep", "panels", "adjoint"])
+@pytest.mark.parametrize("workload", ["simplex_explore", "smap_sweep", "panels", "panels_independent", "adjoint",
+                                      "easy_edm"])
 def test_other_workloads_line(bench, monkeypatch, workload):
-    d = run(bench, monkeypatch, "--workload", workload, "--steps", "1", "--warmup", "3")
-    for k in BASE_KEYS + ["ms_per_step", "gpu_launches", "clocks"]:
+    # the oracle's CPU sample runs for real on the quick workloads
+    quick = workload in ("simplex_explore", "adjoint")
+    d = run(bench, monkeypatch, "--workload", workload, "--steps", "1", "--warmup", "3", *([] if quick else ["--no-cpu"]))
+    for k in BASE_KEYS + ["ms_per_step", "gpu_launches", "clocks", "roofline", "cpu_baseline"]:
         assert k in d, k
     assert d["value"] > 0 and d["config"]["workload"]
+    for k in ("bound", "achieved", "peak", "unit", "frac", "traffic", "kernel_ms_per_step"):
+        assert k in d["roofline"], k
+    assert d["roofline"]["frac"] == pytest.approx(d["roofline"]["achieved"] / d["roofline"]["peak"])
+    if quick:
+        for k in ("value", "unit", "cores", "kind", "sample"):
+            assert k in d["cpu_baseline"], k
+        assert d["cpu_baseline"]["value"] > 0
 
 
 def test_reference_arm_line(bench, monkeypatch):

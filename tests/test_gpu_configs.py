@@ -73,6 +73,8 @@ def test_uneven_panels_missing_dt(ctx, panel_weight, algorithm):
     kw = dict(panel=w["panel"], E=[3, 4, 5, 6, 7, 8], dt=True, algorithm=algorithm, theta=theta,
               panelWeight=panel_weight)
     g = fedm.edm(w["t"], w["x"], ctx=ctx, **kw)
+    if ctx.precision == fedm.PRECISION_MIXED:
+        assert ctx.timing()["mixed_form"] >= 0  # mixed or per-panel sub-tasks on the mixed kernels
     o = edm_oracle.oracle_edm(w["t"], w["x"], numThreads=16, **kw)
     _stats_close(g, o)
     assert g["kMin"] == o["kMin"] and g["kMax"] == o["kMax"] and g["dtWeight"] == o["dtWeight"]
@@ -193,13 +195,14 @@ def test_mixed_fp64_operation_count(ctx):
 
 
 @pytest.mark.parametrize("algorithm", ["simplex", "smap"])
-@pytest.mark.parametrize("form", ["one6", "fused2", "ws4", "ws8"])
+@pytest.mark.parametrize("form", ["one6", "fused2", "ws4", "ws8", "split"])
 def test_mixed_kernel_forms_agree(form, algorithm, monkeypatch):
-    """The mixed path runs in one of four kernel forms: every warp scans then
+    """The mixed path runs in one of five kernel forms: every warp scans then
     finishes its points, with one point per thread at six CTAs per SM or two
     points per thread at two; or (S-map) 8 scan warps hand candidate lists to
-    4 or 8 FP64 solver warps through shared memory.  All give the FP64 path's
-    bits."""
+    4 or 8 FP64 solver warps through shared memory; or (S-map, E_a <= 4) the
+    scan writes neighbour lists that a register-resident solver kernel turns
+    into forecasts on a second stream.  All give the FP64 path's bits."""
     monkeypatch.setenv("FEDM_MIXED_KERNEL", form)
     w = workloads.ccm_config(T=6000, reps=3, n_libs=5, hi=5000)
     kw = dict(E=4, library=w["libraries"], numReps=3, seed=w["seed"], algorithm=algorithm,
@@ -208,6 +211,7 @@ def test_mixed_kernel_forms_agree(form, algorithm, monkeypatch):
     c64 = fedm.Context(0, precision=fedm.PRECISION_FP64)
     try:
         g = fedm.edm(w["t"], w["x"], w["y"], ctx=cm, **kw)
+        tm = cm.timing()
         f = fedm.edm(w["t"], w["x"], w["y"], ctx=c64, **kw)
     finally:
         cm.close()
@@ -217,6 +221,8 @@ def test_mixed_kernel_forms_agree(form, algorithm, monkeypatch):
     assert np.array_equal(g["predictions"], f["predictions"], equal_nan=True)
     if algorithm == "smap":
         assert np.array_equal(g["coeffs"], f["coeffs"], equal_nan=True)
+    if form == "split":
+        assert tm["mixed_form"] == (6 if algorithm == "smap" else 1)
 
 
 @pytest.mark.parametrize("algorithm", ["simplex", "smap"])

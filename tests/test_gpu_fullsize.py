@@ -78,9 +78,15 @@ def _oracle(a_kw, t, x, y, lib, pred, E, k):
     return edm_oracle.oracle_task(edm_oracle.normalise(t, x, y, numThreads=16, **a_kw), lib, pred, E, k)
 
 
-@pytest.mark.parametrize("algorithm", ["simplex", "smap"])
-def test_ccm_full_size_bit_exact(mixed_ctx, algorithm):
-    """Config 3's shape at full size: every library size up to 40 000."""
+@pytest.mark.parametrize("algorithm,form", [("simplex", None), ("smap", None), ("smap", "split")],
+                         ids=["simplex", "smap", "smap_split"])
+def test_ccm_full_size_bit_exact(mixed_ctx, algorithm, form, monkeypatch):
+    """Config 3's shape at full size: every library size up to 40 000 (the
+    S-map also with the split form: neighbour lists, then the
+    register-resident solver kernel)."""
+    if form:
+        monkeypatch.setenv("FEDM_MIXED_KERNEL", form)
+        mixed_ctx = fedm.Context(0, precision=fedm.PRECISION_MIXED)
     w = workloads.ccm_config(reps=1)
     theta = 2.0 if algorithm == "smap" else 1.0
     kw = dict(E=4, library=w["libraries"], numReps=1, shuffle=True, seed=w["seed"], algorithm=algorithm,
@@ -93,7 +99,7 @@ def test_ccm_full_size_bit_exact(mixed_ctx, algorithm):
     for f in range(20):
         g = mixed_ctx.run_task(a, plan["lib"][f], plan["pred"][f], 4, int(plan["k"][f]))
         tm = mixed_ctx.timing()
-        assert tm["mixed_form"] >= 0  # the mixed kernels served the task
+        assert tm["mixed_form"] == 6 if form == "split" else tm["mixed_form"] >= 0  # the mixed kernels served it
         counts[int(plan["library"][f])] = (tm["fallback_points"], tm["exact_points"])
         rho_task.append(g["stats_rho"][0])
         sub, sel = _strided(plan["pred"][f], 37, offset=f)
@@ -111,7 +117,9 @@ def test_ccm_full_size_bit_exact(mixed_ctx, algorithm):
     saved = np.asarray(r["predictions"], float)[pred_rows, -1]
     want = np.where(last["predictions"][-1] == 1e100, np.nan, last["predictions"][-1])
     assert np.array_equal(saved, want, equal_nan=True)
-    print(f"{algorithm}: uncertified / full-search points per library size {counts}")
+    print(f"{algorithm} {form or ''}: uncertified / full-search points per library size {counts}")
+    if form:
+        mixed_ctx.close()
 
 
 def test_smap_sweep_full_size_bit_exact(mixed_ctx):
@@ -147,6 +155,9 @@ def test_panels_full_size_bit_exact(mixed_ctx, algorithm, panel_weight):
     for f in range(6):
         E, k = int(plan["E"][f]), int(plan["k"][f])
         g = mixed_ctx.run_task(a, plan["lib"][f], plan["pred"][f], E, k)
+        # both panel modes run on the mixed kernels (independent panels as
+        # per-panel sub-tasks)
+        assert mixed_ctx.timing()["mixed_form"] >= 0
         sub, sel = _strided(plan["pred"][f], 331, offset=f)
         o = _oracle(kw, w["t"], w["x"], None, plan["lib"][f], sub, E, k)
         assert g["n_pred"] > 100000 and len(sel) > 300
