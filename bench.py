@@ -476,12 +476,12 @@ def config_steps(fedm, workloads, ctx, name):
         return {"workload": "smap_kall_lib9998_pred9998_E5_theta0-8x81", "T": 20000}, step, cpu
     if name in ("panels", "panels_independent"):
         # independent panels (panelWeight = Inf) are timed with two-fold
-        # cross-validation, so that every panel has library rows: under
-        # edm()'s default split the library is the first half of the rows,
-        # i.e. whole panels, and almost no prediction panel has a neighbour
+        # cross-validation over shuffled folds, so that every panel has
+        # library rows: edm()'s default split (and unshuffled folds) give the
+        # library whole panels, and almost no prediction panel a neighbour
         w = workloads.panel_config()
         pw = float("inf") if name == "panels_independent" else 0.0
-        extra = dict(crossfold=2) if pw else {}
+        extra = dict(crossfold=2, shuffle=True, seed=1) if pw else {}
         kws = [dict(panel=w["panel"], E=[3, 4, 5, 6, 7, 8], dt=True, algorithm="simplex", panelWeight=pw, **extra),
                dict(panel=w["panel"], E=[3, 4, 5, 6, 7, 8], dt=True, algorithm="smap", theta=[0.0, 1.0, 2.0, 4.0],
                     panelWeight=pw, **extra)]
@@ -507,7 +507,7 @@ def config_steps(fedm, workloads, ctx, name):
                 edm_oracle.set_pred_stride(1)
             n_pred = int(fedm.host_plan(fedm.normalise(w["t"], w["x"], **kws[0]))["pred"][0].sum())
             return n * len(range(0, n_pred, stride)), dt, f"every {stride}th prediction row, every E and theta"
-        mode = "independent_panels_crossfold2" if pw else "mixed_library"
+        mode = "independent_panels_crossfold2_shuffled" if pw else "mixed_library"
         return {"workload": f"panels512_rows{len(w['t'])}_E3-8_dt_simplex+smap4theta_{mode}",
                 "rows": len(w["t"]), "panelWeight": "Inf" if pw else 0}, step, cpu
     if name == "easy_edm":
@@ -576,11 +576,12 @@ def config_steps(fedm, workloads, ctx, name):
                         kw["numReps"] = 20
                     r = edm_oracle.oracle_edm(*call["args"], numThreads=cores, **kw)
                     if "Ms" not in r and kw.get("saveManifolds"):
-                        r["Ms"] = [np.zeros((len(t) - kw["E"], kw["E"]))]
+                        r["Ms"] = [np.zeros((len(t) - kw["E"], kw["E"]))]  # the oracle keeps no manifolds
                     # prediction rows: half the usable rows when exploring,
                     # all of them for cross maps and full
                     half = len(call["args"]) == 2 and not kw.get("full")
-                    n_pred = (len(t) - kw["E"] if not half else (len(t) - kw["E"]) // 2)
+                    E = max(np.atleast_1d(kw["E"]))
+                    n_pred = (len(t) - E if not half else (len(t) - E) // 2)
                     n += len(r["stats"]["rho"]) * ((n_pred + 9) // 10)
                     try:
                         call = gen.send(r)
@@ -647,6 +648,20 @@ def config_roofline(name, precision, steps_tm, peaks):
         flops = 2.0 * tm["distance_pairs"] * n_th * (n * (n + 1) / 2 + n)
         fast = precision == "fast"
         peak = peaks["fp32"] if fast else peaks["fp64_unfused"]
+        if fast and tm.get("tensor_core_tiles", 0) > 0:
+            # the tensor-core pass computes 15 bf16 slice products of the
+            # 32-column padded GEMM: 15 x 2 N_p Theta N_L 32 tensor flops
+            tflops = 15 * 2.0 * tm["distance_pairs"] * n_th * 32
+            return {"kernel": "all_df_prep_kernel + gram_tc_kernel (tcgen05, bf16 slices, FP32 in TMEM) + "
+                              "all_smap_gram_kernel<5> (FP64 JacobiSVD)",
+                    "bound": "tensor", "achieved": tflops / (ms * 1e-3) / 1e12, "peak": peaks["bf16"],
+                    "unit": "TFLOP/s", "frac": tflops / (ms * 1e-3) / 1e12 / peaks["bf16"], "traffic": None,
+                    "kernel_ms_per_step": ms, "launches_per_step": tm["forecast_launches"],
+                    "tensor_core_tiles": tm["tensor_core_tiles"],
+                    "work": "15 slice products x 2 N_p Theta N_L x 32 (padded) columns of bf16 tensor flops over "
+                            "the prep, tensor-core and solve kernels' time",
+                    "peak_source": peaks["bf16_source"],
+                    "algorithmic_fp64_equivalent": {"achieved": flops / (ms * 1e-3) / 1e12, "flops": flops}}
         return {"kernel": ("all_df_prep_kernel + all_smap_df_kernel<5> (FP32 weights, double-float normal "
                            "equations)") if fast else "all_smap_kernel<5> (FP64 weights and normal equations)",
                 "bound": "fp32_simt" if fast else "fp64_simt", "achieved": flops / (ms * 1e-3) / 1e12,
@@ -716,6 +731,12 @@ def run_config(a):
     world, rank, local = dist_setup()
     ctx = fedm.Context(local, precision={"mixed": fedm.PRECISION_MIXED, "fast": fedm.PRECISION_FAST}[a.precision])
     peaks = {"fp32": ctx.measure_peak(0), "fp64_fma": ctx.measure_peak(1), "fp64_unfused": ctx.measure_peak(3)}
+    try:
+        peaks["bf16"] = float(json.loads((ROOT / "MEASURED_PEAKS.json").read_text())["bf16_tflops"])
+        peaks["bf16_source"] = "MEASURED_PEAKS.json bf16_tflops (cuBLAS bf16 GEMM, burst), of measured"
+    except (OSError, ValueError, KeyError):
+        peaks["bf16"] = 1900.0
+        peaks["bf16_source"] = "fallback 1.9 PFLOP/s bf16"
     cfg, step, cpu = config_steps(fedm, workloads, ctx, a.workload)
     for _ in range(max(3, a.warmup)):
         step()

@@ -27,6 +27,7 @@ CU_FLAGS = {
     "kernels_wide.cu": [],
     "kernels_one16.cu": [],
     "kernels_split.cu": [],
+    "kernels_gram_tc.cu": [],
     "static_entry.cu": [],
     "kernels_adjoint.cu": [],
 }

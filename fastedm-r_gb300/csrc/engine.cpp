@@ -77,6 +77,8 @@ Context::Context(int dev) : device(dev)
     split_solve_ctas = std::max(1, std::atoi(v));
   if (const char* v = std::getenv("FEDM_SPLIT_CHUNK_POINTS"))
     split_chunk_points = std::max(256LL, std::atoll(v));
+  if (const char* v = std::getenv("FEDM_GRAM_TC"))
+    gram_tc = std::strcmp(v, "0") != 0;
   reset_timing();
 }
 
@@ -708,6 +710,47 @@ void run_group(Context& ctx, const Options& o, const std::vector<Task>& tasks, c
     }
   }
 
+  // FAST precision on the tensor cores: the product slices of every
+  // all-mode task's library, once per batch
+  GramTC tc{};
+  std::vector<GramTask> gt_tasks;
+  std::vector<int> gt_of;  // kernel task -> its GramTask (-1: none)
+  if (gram_terms && ctx.gram_tc && gram_tc_supported(Ea)) {
+    bool fits = true;
+    gt_of.assign(nK, -1);
+    long long blocks = 0;
+    int max_lib = 0;
+    for (int j = 0; j < nK; j++)
+      if (dk[j].all_mode) {
+        if (dk[j].n_lib > 30000)
+          fits = false;  // the int64 sums stay exact below ~32 000 rows
+        GramTask t{};
+        t.lib_off = dk[j].lib_off;
+        t.n_lib = dk[j].n_lib;
+        t.n_blocks = (dk[j].n_lib + gram_tc_block_rows() - 1) / gram_tc_block_rows();
+        t.b_off = (int)blocks;
+        blocks += t.n_blocks;
+        max_lib = std::max(max_lib, dk[j].n_lib);
+        gt_of[j] = (int)gt_tasks.size();
+        gt_tasks.push_back(t);
+      }
+    if (fits && !gt_tasks.empty() && blocks > 0) {
+      const int nA = (int)gt_tasks.size();
+      tc.tasks = (const GramTask*)ctx.buf("gt_tasks", gt_tasks.size() * sizeof(GramTask));
+      tc.colmax = (unsigned long long*)ctx.buf("gt_colmax", (size_t)nA * gram_tc_columns() * 8);
+      tc.bslices = (unsigned char*)ctx.buf("gt_slices", (size_t)blocks * gram_tc_block_bytes());
+      tc.error = (int*)ctx.buf("gt_error", 4);
+      ctx.upload((void*)tc.tasks, gt_tasks.data(), gt_tasks.size() * sizeof(GramTask));
+      ck(cudaMemsetAsync(tc.colmax, 0, (size_t)nA * gram_tc_columns() * 8, s), "memset");
+      fill_i32(tc.error, 1, 0, s);
+      launch_gram_tc_slices(g, tc, nA, max_lib, s);
+      ctx.check("gram slices");
+      ctx.timing.kernel_launches += 3;
+    } else {
+      gt_tasks.clear();
+    }
+  }
+
   // chunking: neighbour lists, statuses and the all-mode Gram buffer
   const long long budget = 2LL << 30;
   long long per_point = (long long)kcap * 12 + 8;
@@ -806,18 +849,54 @@ void run_group(Context& ctx, const Options& o, const std::vector<Task>& tasks, c
     if (with_all) {
       float* rdist = nullptr;
       double* means = nullptr;
+      float* dmin = nullptr;
+      int tiles = 0;
       if (gram_terms) {
         rdist = (float*)ctx.buf("df_rdist", (size_t)(c.p_end - c.p_begin) * max_nlib_all * 4);
         means = (double*)ctx.buf("df_means", (size_t)(c.p_end - c.p_begin) * 8);
       }
-      launch_all_mode(g, c, ctx.num_sms, max_nlib_all, s, gram_terms, rdist, means, f0, f1);
+      if (!gt_tasks.empty()) {
+        // the chunk's rows ((point, theta), theta fastest) of every all-mode
+        // task, in tiles of 128
+        const long long cl = c.p_end - c.p_begin;
+        std::vector<GramTile> tl;
+        for (int j = 0; j < nK; j++) {
+          if (gt_of[j] < 0)
+            continue;
+          const long long a = std::max(dk[j].point_base, c.p_begin);
+          const long long b = std::min(dk[j].point_base + dk[j].n_pred, c.p_end);
+          GramTask& t = gt_tasks[gt_of[j]];
+          t.q0 = (int)(a - c.p_begin);
+          if (b <= a)
+            continue;
+          const long long rows = (b - a) * nth;
+          for (long long r = 0; r < rows; r += gram_tc_tile_rows())
+            tl.push_back(GramTile{ gt_of[j], (int)r, (int)std::min<long long>(gram_tc_tile_rows(), rows - r) });
+        }
+        tiles = (int)tl.size();
+        ctx.timing.tensor_core_tiles += tiles;
+        ctx.upload((void*)tc.tasks, gt_tasks.data(), gt_tasks.size() * sizeof(GramTask));
+        tc.tiles = (const GramTile*)ctx.buf("gt_tiles", std::max<size_t>(tl.size(), 1) * sizeof(GramTile));
+        ctx.upload((void*)tc.tiles, tl.data(), tl.size() * sizeof(GramTile));
+        dmin = (float*)ctx.buf("df_dmin", (size_t)cl * 4);
+        tc.rdist = rdist;
+        tc.dmin = dmin;
+        tc.means = means;
+        tc.thetas = g.thetas;
+        tc.n_thetas = nth;
+        tc.max_nlib = max_nlib_all;
+        tc.np = n * (n + 1) / 2 + n;
+        tc.G = (double*)ctx.buf("gt_G", (size_t)cl * nth * gram_tc_columns() * 8);
+      }
+      launch_all_mode(g, c, ctx.num_sms, max_nlib_all, s, gram_terms, rdist, means, f0, f1, tiles ? &tc : nullptr,
+                      tiles, dmin);
       ctx.check("all_mode");
       ck(cudaEventSynchronize(f1), "sync");
       float ms = 0;
       cudaEventElapsedTime(&ms, f0, f1);
       ctx.timing.forecast_kernel_ms += ms;
       ctx.timing.forecast_launches += 1;
-      ctx.timing.kernel_launches += o.algorithm == 1 ? (gram_terms ? 3 : 2) : 1;
+      ctx.timing.kernel_launches += o.algorithm == 1 ? (gram_terms ? (tiles ? 4 : 3) : 2) : 1;
     }
   };
 
@@ -1202,6 +1281,13 @@ void run_group(Context& ctx, const Options& o, const std::vector<Task>& tasks, c
   ck(cudaStreamSynchronize(s), "sync");
   if (err)
     throw Error{ RC_UNKNOWN_ERROR, "panel weight missing for a compared pair of panels" };
+  if (!gt_tasks.empty()) {
+    int terr = 0;
+    ctx.download(&terr, tc.error, 4);
+    ck(cudaStreamSynchronize(s), "sync");
+    if (terr)
+      throw Error{ RC_UNKNOWN_ERROR, "tensor-core normal equations: a bounded wait ran out" };
+  }
   for (int j = 0; j < nT; j++) {
     TaskOut& to = outs[job.task_ids[j]];
     const Task& t = tasks[job.task_ids[j]];

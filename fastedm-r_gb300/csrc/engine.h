@@ -46,6 +46,9 @@ public:
   int split_scan_ctas = 3;
   int split_solve_ctas = 2;
   long long split_chunk_points = 4 << 20;
+  // FAST precision: the k = all S-map's normal equations on the tensor cores
+  // (E_a <= 5); FEDM_GRAM_TC=0 keeps the double-float SIMT kernel.
+  bool gram_tc = true;
   std::map<std::array<int, 3>, int> tuned_forms;
   std::string last_error;
   fedm_timing timing{};

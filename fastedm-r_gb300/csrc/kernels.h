@@ -18,6 +18,8 @@
 
 namespace fedm {
 
+struct GramTC;
+
 struct DevTask
 {
   long long point_base;  // first global point id of this task
@@ -102,11 +104,14 @@ struct ChunkBuffers
 void launch_knn_exact(const GroupParams& g, const ChunkBuffers& c, int num_sms, cudaStream_t s);
 void launch_simplex_nn(const GroupParams& g, const ChunkBuffers& c, cudaStream_t s);
 void launch_smap_nn(const GroupParams& g, const ChunkBuffers& c, int num_sms, cudaStream_t s);
-// ev0 / ev1 (optional) are recorded around the forecast kernel, after the
-// distance pass.
+// ev0 / ev1 (optional) are recorded around the forecast kernels, after the
+// distance pass.  With tc (FAST precision, E_a <= 5) the forecasts take the
+// tensor-core path: rdist, means and dmin are filled, tc->G computed and
+// solved.
 void launch_all_mode(const GroupParams& g, const ChunkBuffers& c, int num_sms, long long max_nlib, cudaStream_t s,
                      const float2* gram_terms = nullptr, float* rdist = nullptr, double* means = nullptr,
-                     cudaEvent_t ev0 = nullptr, cudaEvent_t ev1 = nullptr);
+                     cudaEvent_t ev0 = nullptr, cudaEvent_t ev1 = nullptr, const GramTC* tc = nullptr,
+                     int tc_tiles = 0, float* dmin = nullptr);
 // FAST precision, k = all S-map (E_a <= 8): per library-pool row the
 // n(n+1)/2 + n Gram and right-hand-side products as float pairs; *bad is set
 // when a product is not below 1e30 in magnitude.  launch_all_mode then also
@@ -189,6 +194,45 @@ struct SolveRun
   unsigned long long* fp64_ops;  // optional: FP64 operations of the solves
 };
 void launch_smap_scan_lists(const GroupParams& g, const MixedRun& m, int num_sms, cudaStream_t s);
+
+// FAST precision, k = all S-map, E_a <= 5 (kernels_gram_tc.cu): the
+// weighted normal equations of every (point, theta) as one GEMM on the
+// tensor cores (tcgen05), on exact bf16 slices of the weights and of the
+// library-side products, then the FP64 solve (all_smap_gram_kernel).
+struct GramTask
+{
+  int lib_off, n_lib;  // the task's library list (slice of lib_rows)
+  int n_blocks;        // 64-row blocks of it
+  int b_off;           // its first block in GramTC::bslices
+  int q0;              // its first point of the chunk (chunk index; rows = points x thetas)
+};
+struct GramTile
+{
+  int task, row0, n_rows;  // 128 rows (or fewer) of one task's (point, theta) rows
+};
+struct GramTC
+{
+  const GramTask* tasks;
+  const GramTile* tiles;
+  unsigned long long* colmax;  // [tasks x 32] largest |product| per column, as bits
+  unsigned char* bslices;      // product slices, 20 KB per block
+  const float* rdist;          // [chunk x max_nlib] FP32 distances, -1: not a neighbour
+  const float* dmin;           // [chunk] smallest distance
+  const double* means;         // [chunk] mean distance
+  const double* thetas;
+  int n_thetas;
+  long long max_nlib;
+  int np;                      // terms: (E_a+1)(E_a+2)/2 + E_a+1
+  double* G;                   // [chunk x n_thetas x 32] the sums
+  int* error;                  // set when a bounded wait ran out
+};
+bool gram_tc_supported(int Ea);
+int gram_tc_columns();
+long long gram_tc_block_bytes();
+int gram_tc_block_rows();
+int gram_tc_tile_rows();
+void launch_gram_tc_slices(const GroupParams& g, const GramTC& t, int n_tasks, int max_lib, cudaStream_t s);
+void launch_gram_tc(const GramTC& t, int n_tiles, cudaStream_t s);
 void launch_smap_lists(const GroupParams& g, const SolveRun& r, int num_sms, int ctas_per_sm, cudaStream_t s);
 
 // Points the mixed kernels could not certify (ChunkBuffers::plist): the rows

@@ -843,7 +843,8 @@ __global__ void gram_terms_kernel(GroupParams g, long long pool_size, float2* P,
 // Once per point for every theta: the mean distance (a warp reduction, not
 // the reference's sequential sum: this path is not bit-exact anyway) and the
 // distances in FP32 (-1: not a neighbour).
-__global__ void all_df_prep_kernel(GroupParams g, ChunkBuffers c, long long max_nlib, float* rdist, double* means)
+__global__ void all_df_prep_kernel(GroupParams g, ChunkBuffers c, long long max_nlib, float* rdist, double* means,
+                                   float* dmin)
 {
   const int lane = threadIdx.x & 31;
   const long long q = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
@@ -852,21 +853,72 @@ __global__ void all_df_prep_kernel(GroupParams g, ChunkBuffers c, long long max_
     return;
   const long long p = point_of(c, q);
   const DevTask T = g.tasks[find_task(g, p)];
+  if (dmin && lane == 0)
+    dmin[q] = INFINITY;  // no neighbour (set below otherwise)
   if (!T.all_mode || c.status[q] != PT_OK)
     return;
   const double* dq = c.scratch + q * max_nlib;
   float* rq = rdist + q * max_nlib;
   double sum = 0;
+  float mn = INFINITY;
   for (int i = lane; i < T.n_lib; i += 32) {
     const double d = dq[i];
-    rq[i] = d >= 0 ? (float)d : -1.f;
-    if (d >= 0)
+    const float f = d >= 0 ? (float)d : -1.f;
+    rq[i] = f;
+    if (d >= 0) {
       sum += d;
+      mn = fminf(mn, f);
+    }
   }
-  for (int o = 16; o > 0; o >>= 1)
+  for (int o = 16; o > 0; o >>= 1) {
     sum += __shfl_xor_sync(FULL, sum, o);
-  if (lane == 0)
+    mn = fminf(mn, __shfl_xor_sync(FULL, mn, o));
+  }
+  if (lane == 0) {
     means[q] = sum / (double)c.nn_count[q];
+    if (dmin)
+      dmin[q] = mn;
+  }
+}
+
+// The solve of the tensor-core sums (kernels_gram_tc.cu): per (point,
+// theta), the normal equations from G, the FP64 JacobiSVD, the forecast.
+template<int EA>
+__global__ void __launch_bounds__(128) all_smap_gram_kernel(GroupParams g, ChunkBuffers c, const double* G)
+{
+  constexpr int n = EA + 1;
+  const long long chunk = c.p_end - c.p_begin;
+  const long long idx = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= chunk * g.n_thetas)
+    return;
+  const long long q = idx / g.n_thetas;
+  const int t = (int)(idx - q * g.n_thetas);
+  const long long p = point_of(c, q);
+  const DevTask T = g.tasks[find_task(g, p)];
+  if (!T.all_mode)
+    return;
+  const int st = c.status[q];
+  if (st != PT_OK) {
+    early_rc(g, T.task, st, t);
+    return;
+  }
+  const double* gr = G + (size_t)idx * 32;
+  double Wl[n * n], bv[n], U[n * n], V[n * n], sv[n], tmp[n], xs[n];
+  int e = 0;
+#pragma unroll
+  for (int a = 0; a < n; a++)
+#pragma unroll
+    for (int b = a; b < n; b++) {
+      Wl[a * n + b] = gr[e];
+      Wl[b * n + a] = gr[e];
+      e++;
+    }
+#pragma unroll
+  for (int a = 0; a < n; a++)
+    bv[a] = gr[e++];
+  svd_solve(Wl, U, V, sv, tmp, bv, xs, n);
+  const int prow = g.pred_rows[T.pred_off + (int)(p - T.point_base)];
+  smap_finish(g, T, p, prow, t, xs, n);
 }
 
 template<int EA>
@@ -1144,13 +1196,26 @@ void launch_gram_terms(const GroupParams& g, long long pool_size, float2* P, int
 namespace {
 
 void launch_forecast(const GroupParams& g, const ChunkBuffers& c, long long max_nlib, cudaStream_t s,
-                     const float2* gram_terms, float* rdist, double* means)
+                     const float2* gram_terms, float* rdist, double* means, const GramTC* tc, int tc_tiles,
+                     float* dmin)
 {
   const long long chunk = c.p_end - c.p_begin;
   const long long total = chunk * g.n_thetas;
   const int fb = (int)((total + 127) / 128);
+  if (g.algorithm == 1 && tc && tc_tiles > 0 && rdist && means && dmin && gram_tc_supported(g.Ea)) {
+    all_df_prep_kernel<<<(int)((chunk * 32 + 127) / 128), 128, 0, s>>>(g, c, max_nlib, rdist, means, dmin);
+    launch_gram_tc(*tc, tc_tiles, s);
+    switch (g.Ea) {
+      case 1: all_smap_gram_kernel<1><<<fb, 128, 0, s>>>(g, c, tc->G); return;
+      case 2: all_smap_gram_kernel<2><<<fb, 128, 0, s>>>(g, c, tc->G); return;
+      case 3: all_smap_gram_kernel<3><<<fb, 128, 0, s>>>(g, c, tc->G); return;
+      case 4: all_smap_gram_kernel<4><<<fb, 128, 0, s>>>(g, c, tc->G); return;
+      case 5: all_smap_gram_kernel<5><<<fb, 128, 0, s>>>(g, c, tc->G); return;
+      default: break;
+    }
+  }
   if (g.algorithm == 1 && g.Ea <= 8 && gram_terms && rdist && means) {
-    all_df_prep_kernel<<<(int)((chunk * 32 + 127) / 128), 128, 0, s>>>(g, c, max_nlib, rdist, means);
+    all_df_prep_kernel<<<(int)((chunk * 32 + 127) / 128), 128, 0, s>>>(g, c, max_nlib, rdist, means, nullptr);
     switch (g.Ea) {
       case 1: all_smap_df_kernel<1><<<fb, 128, 0, s>>>(g, c, max_nlib, gram_terms, rdist, means); return;
       case 2: all_smap_df_kernel<2><<<fb, 128, 0, s>>>(g, c, max_nlib, gram_terms, rdist, means); return;
@@ -1182,7 +1247,8 @@ void launch_forecast(const GroupParams& g, const ChunkBuffers& c, long long max_
 } // namespace
 
 void launch_all_mode(const GroupParams& g, const ChunkBuffers& c, int num_sms, long long max_nlib, cudaStream_t s,
-                     const float2* gram_terms, float* rdist, double* means, cudaEvent_t ev0, cudaEvent_t ev1)
+                     const float2* gram_terms, float* rdist, double* means, cudaEvent_t ev0, cudaEvent_t ev1,
+                     const GramTC* tc, int tc_tiles, float* dmin)
 {
   int per_warp;
   const int w = all_warps_per_block(g.Ea, per_warp);
@@ -1197,7 +1263,7 @@ void launch_all_mode(const GroupParams& g, const ChunkBuffers& c, int num_sms, l
     return;
   if (ev0)
     cudaEventRecord(ev0, s);
-  launch_forecast(g, c, max_nlib, s, gram_terms, rdist, means);
+  launch_forecast(g, c, max_nlib, s, gram_terms, rdist, means, tc, tc_tiles, dmin);
   if (ev1)
     cudaEventRecord(ev1, s);
 }

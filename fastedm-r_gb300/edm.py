@@ -75,7 +75,7 @@ class Timing(C.Structure):
         ("setup_ms", C.c_double), ("finish_ms", C.c_double), ("exact_points", C.c_int),
         ("mixed_form", C.c_int), ("autotune_probes", C.c_int), ("prep_ms", C.c_double),
         ("manifold_ms", C.c_double), ("scan_flops", C.c_longlong), ("forecast_kernel_ms", C.c_double),
-        ("forecast_launches", C.c_int),
+        ("forecast_launches", C.c_int), ("tensor_core_tiles", C.c_int),
     ]
 
 

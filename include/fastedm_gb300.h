@@ -237,6 +237,8 @@ typedef struct fedm_timing {
   double forecast_kernel_ms; /* k = all: time of the forecast kernels after
                                 the distance pass (CUDA events)              */
   int forecast_launches;     /* their launches                               */
+  int tensor_core_tiles;     /* FAST k = all S-map: 128-row tiles whose
+                                normal equations ran on the tensor cores     */
 } fedm_timing;
 
 int fedm_last_timing(const fedm_ctx* ctx, fedm_timing* out);

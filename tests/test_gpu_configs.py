@@ -142,6 +142,41 @@ def test_fast_precision_smap_all_neighbours(T):
           f"exact {te['device_ms']:.1f}")
 
 
+@pytest.mark.parametrize("T", [1600, 20000], ids=["reduced", "full_size"])
+def test_fast_precision_tensor_core_normal_equations(T, monkeypatch):
+    """FEDM_PRECISION_FAST's k = all S-map at E_a <= 5 forms its normal
+    equations on the tensor cores (tcgen05, exact bf16 slices of the weights
+    and of the library-side products, FP32 accumulation exact per 64-row
+    block, int64 across blocks).  Against the bit-exact path the forecasts
+    agree within the FAST bar, as the double-float SIMT kernel
+    (FEDM_GRAM_TC=0) does, and rho within 1e-6."""
+    w = workloads.smap_config(T=T)
+    thetas = [0.0, 0.5, 1.0, 2.0, 4.0, 8.0]
+    kw = dict(E=5, k=float("inf"), theta=thetas, algorithm="smap", savePredictions=True)
+    out = {}
+    for name, prec, env in (("tc", fedm.PRECISION_FAST, "1"), ("simt", fedm.PRECISION_FAST, "0"),
+                            ("exact", fedm.PRECISION_MIXED, "1")):
+        monkeypatch.setenv("FEDM_GRAM_TC", env)
+        c = fedm.Context(0, precision=prec)
+        try:
+            out[name] = (fedm.edm(w["t"], w["x"], ctx=c, **kw), c.timing())
+        finally:
+            c.close()
+    (tc, ttc), (simt, tsimt), (exact, _) = out["tc"], out["simt"], out["exact"]
+    assert ttc["tensor_core_tiles"] > 0 and tsimt["tensor_core_tiles"] == 0
+    assert tc["rc"] == simt["rc"] == exact["rc"] == 0
+    pe = np.asarray(exact["predictions"], float)
+    m = ~np.isnan(pe)
+    scale = np.max(np.abs(pe[m]))
+    err = {k: np.max(np.abs(np.asarray(v[0]["predictions"], float)[m] - pe[m])) / scale
+           for k, v in (("tc", out["tc"]), ("simt", out["simt"]))}
+    drho = np.max(np.abs(np.asarray(tc["stats"]["rho"]) - np.asarray(exact["stats"]["rho"])))
+    print(f"T={T}: max |forecast - exact| / max |forecast|: tensor cores {err['tc']:.2e}, "
+          f"double-float SIMT {err['simt']:.2e}; |drho| {drho:.2e}; forecast kernels "
+          f"{ttc['forecast_kernel_ms']:.1f} ms vs {tsimt['forecast_kernel_ms']:.1f} ms")
+    assert err["tc"] < 1e-5 and drho <= 1e-6
+
+
 @pytest.mark.parametrize("case", ["missing", "simplex_k_all", "wide_dt", "finite_k"])
 def test_fast_precision_elsewhere_is_mixed(case):
     """FEDM_PRECISION_FAST changes only the S-map with every library row as a
