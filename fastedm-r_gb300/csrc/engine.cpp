@@ -591,6 +591,9 @@ void run_group(Context& ctx, const Options& o, const std::vector<Task>& tasks, c
     const int q = (int)(std::upper_bound(kbase.begin(), kbase.end(), p) - kbase.begin()) - 1;
     return (*kt[q].pos)[v];
   };
+  // the all-mode distance rows' stride, a multiple of four so that rows of
+  // FP32 distances start on 16-byte boundaries
+  max_nlib_all = (max_nlib_all + 3) & ~3LL;
   if (Ea + 32 * (n + 1) + n * (n + 1) / 2 + n > 24000 && any_all && o.algorithm == 1)
     throw Error{ RC_NOT_IMPLEMENTED, "embedding too wide for the all-neighbour S-map" };
 

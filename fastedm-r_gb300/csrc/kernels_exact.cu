@@ -657,7 +657,7 @@ __global__ void all_forecast_kernel(GroupParams g, ChunkBuffers c, long long max
     early_rc(g, T.task, st, t);
     return;
   }
-  const double* dq = c.scratch + q * max_nlib;
+  double* dq = c.scratch + q * max_nlib;
   const double theta = g.thetas[t];
   if (g.algorithm == 0) {
     // src/edm.cpp:707-735
@@ -665,15 +665,25 @@ __global__ void all_forecast_kernel(GroupParams g, ChunkBuffers c, long long max
     for (int i = 0; i < T.n_lib; i++)
       if (dq[i] >= 0 && dq[i] < minDist)
         minDist = dq[i];
+    const double ymin = rcp(minDist);
     double sumw = 0.0;
+    // with one theta this thread alone reads the point's distance row, so
+    // each weight replaces its distance (weights are positive, the -1 marks
+    // of invalid rows stay) and is not evaluated twice
+    const bool keep = g.n_thetas == 1;
     for (int i = 0; i < T.n_lib; i++)
-      if (dq[i] >= 0)
-        sumw = sumw + exp_rn(-theta * (dq[i] / minDist));
+      if (dq[i] >= 0) {
+        const double w = exp_rn(-theta * dvd_r(dq[i], minDist, ymin));
+        sumw = sumw + w;
+        if (keep)
+          dq[i] = w;
+      }
+    const double ysum = rcp(sumw);
     double r = 0.0;
     for (int i = 0; i < T.n_lib; i++)
       if (dq[i] >= 0) {
-        const double w = exp_rn(-theta * (dq[i] / minDist));
-        r = r + g.lib_target[g.lib_rows[T.lib_off + i]] * (w / sumw);
+        const double w = keep ? dq[i] : exp_rn(-theta * dvd_r(dq[i], minDist, ymin));
+        r = r + g.lib_target[g.lib_rows[T.lib_off + i]] * dvd_r(w, sumw, ysum);
       }
     g.pred[(size_t)t * g.total_points + p] = r;
     return;

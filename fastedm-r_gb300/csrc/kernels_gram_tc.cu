@@ -28,12 +28,15 @@
 // approximate: 2^-40 of the row's largest weight and 2^-41 of the column's
 // largest product.
 //
-// One CTA of 128 threads takes 128 rows (thread = row = TMEM lane).  Per
-// block it writes the five weight slices of its 128 x 64 tile to shared
-// memory, takes the block's 20 KB of library-side slices (precomputed in the
-// MMA's shared-memory layout) with one cp.async.bulk, issues 60
-// tcgen05.mma (M = 128, N = 32, K = 16, bf16 in, FP32 in TMEM) from one
-// thread and reads the five accumulators back.  Every wait is bounded; on a
+// One CTA of 256 threads takes 128 rows (TMEM lanes); two threads share a
+// row, each generating the weight digits of half of every 64-row block and
+// reading back part of the accumulators (two CTAs, 16 warps, per SM: shared
+// memory and TMEM allow no more CTAs).  Per block the CTA writes the five
+// weight slices of its 128 x 64 tile to shared memory, takes the block's
+// 20 KB of library-side slices (precomputed in the MMA's shared-memory
+// layout) with one cp.async.bulk, issues 60 tcgen05.mma (M = 128, N = 32,
+// K = 16, bf16 in, FP32 in TMEM) from one thread and reads the five
+// accumulators back.  Every wait is bounded; on a
 // timeout the CTA sets the error flag, and TMEM is always freed.
 #include <cuda_bf16.h>
 
@@ -49,6 +52,7 @@ namespace fedm {
 namespace {
 
 constexpr int TC_M = 128;        // rows per tile (TMEM lanes)
+constexpr int TC_NT = 256;       // threads per CTA: two per row
 constexpr int TC_KB = 64;        // library rows per block
 constexpr int TC_KS = 4;         // 16-row MMA K-steps per block
 constexpr int TC_SA = 5;         // weight slices
@@ -120,6 +124,16 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity)
     }
   }
   return false;
+}
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, uint32_t (&v)[16])
+{
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+      : "=r"(v[0]), "=r"(v[1]), "=r"(v[2]), "=r"(v[3]), "=r"(v[4]), "=r"(v[5]), "=r"(v[6]), "=r"(v[7]), "=r"(v[8]),
+        "=r"(v[9]), "=r"(v[10]), "=r"(v[11]), "=r"(v[12]), "=r"(v[13]), "=r"(v[14]), "=r"(v[15])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
 
 __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&v)[32])
@@ -214,7 +228,7 @@ __global__ void gram_tc_slices_kernel(GroupParams g, GramTC t)
   }
 }
 
-__global__ void __launch_bounds__(TC_M, 1) gram_tc_kernel(GramTC t)
+__global__ void __launch_bounds__(TC_NT, 2) gram_tc_kernel(GramTC t)
 {
   extern __shared__ __align__(1024) unsigned char tc_smem[];
   unsigned char* sA = tc_smem;
@@ -222,10 +236,12 @@ __global__ void __launch_bounds__(TC_M, 1) gram_tc_kernel(GramTC t)
   unsigned long long* bars = (unsigned long long*)(tc_smem + A_BYTES + B_BYTES);  // [0] B copy, [1] MMAs
   uint32_t* tmem_slot = (uint32_t*)(bars + 2);
   const int tid = threadIdx.x;
+  const int lrow = tid & (TC_M - 1);  // the tile row (TMEM lane) of this thread: (warp % 4) * 32 + lane
+  const int half = tid >> 7;          // which half of each block's 64 library rows it generates
   const GramTile tile = t.tiles[blockIdx.x];
   const GramTask& K = t.tasks[tile.task];
-  const int row = tile.row0 + tid;  // the task's row (point-major, theta fastest)
-  const bool active = tid < tile.n_rows;
+  const int row = tile.row0 + lrow;  // the task's row (point-major, theta fastest)
+  const bool active = lrow < tile.n_rows;
   // this row's weights: exp(c2 d) with c2 = -2 theta / mean, scaled by the
   // row's largest weight exp(c2 dmin)
   int q = 0;
@@ -256,7 +272,7 @@ __global__ void __launch_bounds__(TC_M, 1) gram_tc_kernel(GramTC t)
   __syncthreads();
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = *tmem_slot;
-  const uint32_t lane_base = tmem + ((uint32_t)((tid >> 5) * 32) << 16);
+  const uint32_t lane_base = tmem + ((uint32_t)(((tid >> 5) & 3) * 32) << 16);
   long long acc[TC_N];
 #pragma unroll
   for (int c = 0; c < TC_N; c++)
@@ -276,23 +292,33 @@ __global__ void __launch_bounds__(TC_M, 1) gram_tc_kernel(GramTC t)
           "l"(src), "r"(B_BYTES), "r"(smem_u32(&bars[0]))
           : "memory");
     }
-    // the five weight slices of this row for the block's 64 library rows
+    // the five weight slices of this row for its half of the block's 64
+    // library rows
     const int i0 = b * TC_KB;
 #pragma unroll 1
-    for (int k8 = 0; k8 < TC_KB; k8 += 8) {
+    for (int k8 = half * (TC_KB / 2); k8 < (half + 1) * (TC_KB / 2); k8 += 8) {
+      // eight distances; rows start on 16-byte boundaries (the stride is a
+      // multiple of four), so a full group is two vector loads
+      float d8[8];
+      if (active && i0 + k8 + 8 <= K.n_lib) {
+        const float4 lo = *reinterpret_cast<const float4*>(rq + i0 + k8);
+        const float4 hi = *reinterpret_cast<const float4*>(rq + i0 + k8 + 4);
+        d8[0] = lo.x; d8[1] = lo.y; d8[2] = lo.z; d8[3] = lo.w;
+        d8[4] = hi.x; d8[5] = hi.y; d8[6] = hi.z; d8[7] = hi.w;
+      } else {
+#pragma unroll
+        for (int j = 0; j < 8; j++)
+          d8[j] = (active && i0 + k8 + j < K.n_lib) ? rq[i0 + k8 + j] : -1.f;
+      }
       uint32_t packed[TC_SA][4];
 #pragma unroll
       for (int j = 0; j < 8; j += 2) {
         float a2[2];
 #pragma unroll
         for (int h = 0; h < 2; h++) {
-          const int i = i0 + k8 + j + h;
-          float w = 0.f;
-          if (active && i < K.n_lib) {
-            const float d = rq[i];
-            if (d >= 0.f)
-              w = expf(__fmul_rn(c2, d)) * rscale;  // exact scaling by a power of two
-          }
+          const float d = d8[j + h];
+          // exact scaling by a power of two; -1 marks a row that is no neighbour
+          const float w = d >= 0.f ? expf(__fmul_rn(c2, d)) * rscale : 0.f;
           a2[h] = fminf(w, 1.f);
         }
         float digit[TC_SA][2];
@@ -320,7 +346,7 @@ __global__ void __launch_bounds__(TC_M, 1) gram_tc_kernel(GramTC t)
         v.y = packed[s][1];
         v.z = packed[s][2];
         v.w = packed[s][3];
-        *reinterpret_cast<uint4*>(sA + (s * TC_KS + ks) * A_TILE + core_off(tid, k)) = v;
+        *reinterpret_cast<uint4*>(sA + (s * TC_KS + ks) * A_TILE + core_off(lrow, k)) = v;
       }
     }
     // the weight tiles (generic proxy) must be visible to the tensor core
@@ -362,21 +388,41 @@ __global__ void __launch_bounds__(TC_M, 1) gram_tc_kernel(GramTC t)
     ok = __syncthreads_and(done && (tid != 0 || ok)) != 0;
     if (!ok)
       break;
+    // the first half of the threads reads groups 0..2, the second 3..4
 #pragma unroll
     for (int gsum = 0; gsum < TC_G; gsum++) {
-      uint32_t v[32];
-      tmem_ld32(lane_base + gsum * TC_N, v);
+      if ((gsum < 3) != (half == 0))
+        continue;
       const int sh = 8 * (TC_G - 1 - gsum);
 #pragma unroll
-      for (int c = 0; c < TC_N; c++)
-        acc[c] += (long long)(int)__uint_as_float(v[c]) << sh;
+      for (int c0 = 0; c0 < TC_N; c0 += 16) {
+        uint32_t v[16];
+        tmem_ld16(lane_base + gsum * TC_N + c0, v);
+#pragma unroll
+        for (int c = 0; c < 16; c++)
+          acc[c0 + c] += (long long)(int)__uint_as_float(v[c]) << sh;
+      }
     }
     asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
     __syncthreads();  // the tiles and accumulators are reused by the next block
   }
   if (!ok && tid == 0)
     atomicExch(t.error, 1);
-  if (ok && active) {
+  // the second half hands its partial sums to the first through shared
+  // memory (the weight tiles are free: every MMA has completed)
+  long long* part = reinterpret_cast<long long*>(sA);
+  if (ok && half == 1) {
+#pragma unroll
+    for (int c = 0; c < TC_N; c++)
+      part[c * TC_M + lrow] = acc[c];
+  }
+  __syncthreads();
+  if (ok && half == 0) {
+#pragma unroll
+    for (int c = 0; c < TC_N; c++)
+      acc[c] += part[c * TC_M + lrow];
+  }
+  if (ok && active && half == 0) {
     // acc holds sum_g S_g 2^(8 (4 - g)); the slices' scales make the sum
     // acc 2^-48 2^rexp 2^F_c
     double* out = t.G + ((size_t)K.q0 * t.n_thetas + row) * TC_N;
@@ -439,7 +485,7 @@ void launch_gram_tc(const GramTC& t, int n_tiles, cudaStream_t s)
   if (n_tiles <= 0)
     return;
   cudaFuncSetAttribute(gram_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TC_SMEM);
-  gram_tc_kernel<<<n_tiles, TC_M, TC_SMEM, s>>>(t);
+  gram_tc_kernel<<<n_tiles, TC_NT, TC_SMEM, s>>>(t);
 }
 
 } // namespace fedm
