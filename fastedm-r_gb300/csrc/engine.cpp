@@ -79,6 +79,10 @@ Context::Context(int dev) : device(dev)
     split_chunk_points = std::max(256LL, std::atoll(v));
   if (const char* v = std::getenv("FEDM_GRAM_TC"))
     gram_tc = std::strcmp(v, "0") != 0;
+  if (const char* v = std::getenv("FEDM_ITEM_ORDER"))
+    item_order = std::strcmp(v, "lpt") == 0 ? 0 : 1;
+  if (const char* v = std::getenv("FEDM_POINT_ORDER"))
+    point_order = std::strcmp(v, "list") == 0 ? 0 : 1;
   reset_timing();
 }
 
@@ -86,7 +90,59 @@ void Context::reset_timing()
 {
   timing = fedm_timing{};
   timing.mixed_form = -1;
+  lane_orders.clear();  // list and manifold addresses are reused by later calls
 }
+
+namespace {
+
+// Spreads the low 10 bits of v to every third bit (a Morton code of three
+// coordinates).
+uint32_t spread3(uint32_t v)
+{
+  v &= 0x3ff;
+  v = (v | (v << 16)) & 0x030000ff;
+  v = (v | (v << 8)) & 0x0300f00f;
+  v = (v | (v << 4)) & 0x030c30c3;
+  v = (v | (v << 2)) & 0x09249249;
+  return v;
+}
+
+// Slot order of the rows rows[0..n): the Morton order of their first three
+// manifold coordinates (F row-major, Ea columns), quantised to 10 bits over
+// the rows' range.  Ties keep list order.
+std::vector<int> morton_lane_order(const std::vector<double>& F, int Ea, const int* rows, int n)
+{
+  const int D = std::min(Ea, 3);
+  double lo[3] = { 0, 0, 0 }, hi[3] = { 0, 0, 0 };
+  for (int j = 0; j < D; j++) {
+    lo[j] = INFINITY;
+    hi[j] = -INFINITY;
+  }
+  for (int i = 0; i < n; i++)
+    for (int j = 0; j < D; j++) {
+      const double v = F[(size_t)rows[i] * Ea + j];
+      lo[j] = std::min(lo[j], v);
+      hi[j] = std::max(hi[j], v);
+    }
+  std::vector<std::pair<uint32_t, int>> key(n);
+  for (int i = 0; i < n; i++) {
+    uint32_t k = 0;
+    for (int j = 0; j < D; j++) {
+      const double span = hi[j] - lo[j];
+      const double v = F[(size_t)rows[i] * Ea + j];
+      const uint32_t qv = span > 0 && std::isfinite(v) ? (uint32_t)std::min(1023.0, (v - lo[j]) / span * 1023.0) : 0;
+      k |= spread3(qv) << (2 - j);
+    }
+    key[i] = { k, i };
+  }
+  std::sort(key.begin(), key.end());
+  std::vector<int> order(n);
+  for (int i = 0; i < n; i++)
+    order[i] = key[i].second;
+  return order;
+}
+
+} // namespace
 
 Context::~Context()
 {
@@ -584,6 +640,32 @@ void run_group(Context& ctx, const Options& o, const std::vector<Task>& tasks, c
   }
   for (const DevTask& d : dk)
     ctx.timing.scan_flops += 3LL * Ea * d.n_pred * (long long)d.n_lib;
+  // lane orders of the one-point mixed kernels: per kernel task, its
+  // prediction rows in Morton order of their coordinates (computed once per
+  // list and call)
+  std::vector<int> perm_pool;
+  for (int j = 0; j < nK; j++)
+    dk[j].perm_off = -1;
+  if (mixed_group && ctx.point_order == 1 && Ea <= 16) {
+    std::map<std::tuple<const void*, int, int, const void*>, int> offs;
+    for (int j = 0; j < nK; j++) {
+      if (!dk[j].mixed || dk[j].n_pred < 64)
+        continue;
+      const std::vector<int>* Pl = job.pred_lists[kt[j].parent];
+      const auto key = std::make_tuple((const void*)Pl, kt[j].pstart, kt[j].plen, (const void*)job.hFp);
+      auto it = offs.find(key);
+      if (it == offs.end()) {
+        auto c = ctx.lane_orders.find(key);
+        if (c == ctx.lane_orders.end())
+          c = ctx.lane_orders
+                  .emplace(key, morton_lane_order(*job.hFp, Ea, Pl->data() + kt[j].pstart, kt[j].plen))
+                  .first;
+        it = offs.emplace(key, (int)perm_pool.size()).first;
+        perm_pool.insert(perm_pool.end(), c->second.begin(), c->second.end());
+      }
+      dk[j].perm_off = it->second;
+    }
+  }
   // library position of slot v of point p in its task's list (detail mode)
   auto task_pos = [&](long long p, int v) {
     if (!split)
@@ -630,6 +712,9 @@ void run_group(Context& ctx, const Options& o, const std::vector<Task>& tasks, c
   double* d_thetas = (double*)ctx.buf("thetas", nth * 8);
   ctx.upload(d_tasks, dk.data(), dk.size() * sizeof(DevTask));
   ctx.upload(d_ptasks, dt.data(), dt.size() * sizeof(DevTask));
+  int* d_perm = (int*)ctx.buf("perm_pool", std::max<size_t>(perm_pool.size(), 1) * 4);
+  if (!perm_pool.empty())
+    ctx.upload(d_perm, perm_pool.data(), perm_pool.size() * 4);
   ctx.upload(d_lib, h_lib, (size_t)lib_total * 4);
   ctx.upload(d_pred, h_pred, (size_t)pred_total * 4);
   ctx.upload(d_thetas, o.thetas.data(), nth * 8);
@@ -648,6 +733,7 @@ void run_group(Context& ctx, const Options& o, const std::vector<Task>& tasks, c
   g.lib_rows = d_lib;
   g.pred_rows = d_pred;
   g.tasks = d_tasks;
+  g.perm = d_perm;
   g.n_tasks = nK;
   g.Ea = Ea;
   g.n_thetas = nth;
@@ -937,7 +1023,18 @@ void run_group(Context& ctx, const Options& o, const std::vector<Task>& tasks, c
       if (dk[j].mixed)
         order.push_back(j);
     std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return dk[a].n_lib > dk[b].n_lib; });
-    // work items of the tasks in LPT order, up to the task that takes the
+    if (ctx.item_order == 1 && order.size() > 2) {
+      // largest, smallest, second largest, second smallest, ...
+      std::vector<int> mix;
+      mix.reserve(order.size());
+      for (size_t lo = 0, hi = order.size(); lo < hi;) {
+        mix.push_back(order[lo++]);
+        if (lo < hi)
+          mix.push_back(order[--hi]);
+      }
+      order.swap(mix);
+    }
+    // work items of the tasks in this order, up to the task that takes the
     // count of points past max_points
     auto items_of = [&](int per_item, long long max_points) {
       std::vector<int2> it;

@@ -5,6 +5,7 @@
 #include <array>
 #include <map>
 #include <string>
+#include <tuple>
 #include <vector>
 
 #include "host.h"
@@ -39,6 +40,17 @@ public:
   // as many as fit), so that calls from other contexts can share the SMs;
   // FEDM_CTAS_PER_SM sets it when the context is created.
   int ctas_per_sm = 0;
+  // Order of the mixed kernels' work items: 1 (default) largest and
+  // smallest library alternately, so that scan-heavy and solve-heavy items
+  // share the SMs; 0 largest first (FEDM_ITEM_ORDER=interleave|lpt).
+  int item_order = 1;
+  // Lane order of the one-point mixed kernels: 1 (default) points of a work
+  // item in Morton order of their manifold coordinates, 0 list order
+  // (FEDM_POINT_ORDER=morton|list).  Results do not depend on it.
+  int point_order = 1;
+  // the lane orders computed during the current call, by (list, first row,
+  // rows, manifold): a CCM call's batches share its prediction list
+  std::map<std::tuple<const void*, int, int, const void*>, std::vector<int>> lane_orders;
   // The split S-map (MIXED_SPLIT): a second stream for the solves, the
   // scan's and the solver's resident CTAs per SM (FEDM_SPLIT_SCAN_CTAS,
   // FEDM_SPLIT_SOLVE_CTAS) and the points per chunk of the pipeline.

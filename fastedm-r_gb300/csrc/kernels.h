@@ -31,6 +31,9 @@ struct DevTask
   int save_coeffs;
   int all_mode;          // k < 0 or k >= n_lib: every valid neighbour, library order
   int mixed;             // handled by the mixed-precision kernel
+  int perm_off;          // one-point mixed kernels: point i of a work item's
+                         // slot order is GroupParams::perm[perm_off + slot]
+                         // (-1: slot order is list order)
 };
 
 struct GroupParams
@@ -50,6 +53,7 @@ struct GroupParams
   const int* lib_rows;
   const int* pred_rows;
   const DevTask* tasks;
+  const int* perm;         // lane orders of the one-point mixed kernels (DevTask::perm_off)
   int n_tasks;
   int Ea;
   int n_thetas;

@@ -60,7 +60,8 @@ __global__ void __launch_bounds__(SOLVE_NT) smap_list_kernel(GroupParams g, Solv
       continue;
     const int2 it = r.items[r.item_begin + (int)(slot / TPB)];
     const DevTask& T = g.tasks[it.x];
-    const int i = it.y + (int)(slot % TPB);
+    const int si = it.y + (int)(slot % TPB);  // the scan's slot order
+    const int i = T.perm_off >= 0 ? g.perm[T.perm_off + si] : si;
     const long long p = T.point_base + i;
     const int prow = g.pred_rows[T.pred_off + i];
     int rows[SPLIT_SLOTS];

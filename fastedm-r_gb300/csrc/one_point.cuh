@@ -18,11 +18,15 @@ namespace {
 // TR library rows per shared-memory tile, NT threads per CTA.
 template<int EA, int C, int RS, int TR, int NT>
 __device__ __forceinline__ void scan_item_one(const GroupParams& g, const MixedRun& m, const DevTask& T, int first,
-                                              int tid, float2* tile, Cand<C>& c0, int& prow0, bool& a0)
+                                              int tid, float2* tile, Cand<C>& c0, int& prow0, bool& a0, int& pi)
 {
-  const int pi0 = first + tid;
-  a0 = pi0 < T.n_pred;
-  prow0 = a0 ? g.pred_rows[T.pred_off + pi0] : 0;
+  // the slot's point: list order, or the task's lane order (points close
+  // in the manifold on neighbouring lanes, so that a warp's candidate
+  // lists and solver rotations diverge less)
+  const int slot = first + tid;
+  a0 = slot < T.n_pred;
+  pi = (a0 && T.perm_off >= 0) ? g.perm[T.perm_off + slot] : slot;
+  prow0 = a0 ? g.pred_rows[T.pred_off + pi] : 0;
   // negated prediction coordinates, duplicated in both halves; an idle slot
   // sits at 1e30 so its squared distances overflow to +inf and never enter
   float2 na[EA];
@@ -109,9 +113,9 @@ __global__ void __launch_bounds__(NT, OCC) knn_one_kernel(GroupParams g, MixedRu
     const int2 it = m.items[item];
     const DevTask T = g.tasks[it.x];
     Cand<C> c0;
-    int prow0;
+    int prow0, pi0;
     bool a0;
-    scan_item_one<EA, C, RS, TR, NT>(g, m, T, it.y, tid, tile, c0, prow0, a0);
+    scan_item_one<EA, C, RS, TR, NT>(g, m, T, it.y, tid, tile, c0, prow0, a0, pi0);
     if constexpr (ALG == 2) {
       // S-map lists for smap_list_kernel: settle the neighbours, write them
       const long long slot = (long long)(item - m.item_begin) * NT + tid;
@@ -120,7 +124,7 @@ __global__ void __launch_bounds__(NT, OCC) knn_one_kernel(GroupParams g, MixedRu
       double cd[C + ZCAP];
       if (a0) {
         const Cand<C> c = c0;
-        if (!prepare_point<EA, C>(g, m, T, T.point_base + it.y + tid, prow0, c, keff, rows, cd, iops))
+        if (!prepare_point<EA, C>(g, m, T, T.point_base + pi0, prow0, c, keff, rows, cd, iops))
           keff = 0;
       }
       m.l_keff[slot] = keff;
@@ -133,7 +137,7 @@ __global__ void __launch_bounds__(NT, OCC) knn_one_kernel(GroupParams g, MixedRu
       ops += iops;
     } else if (a0) {
       const Cand<C> c = c0;
-      ops += finalize_point<EA, C, ALG>(g, m, T, T.point_base + it.y + tid, prow0, c);
+      ops += finalize_point<EA, C, ALG>(g, m, T, T.point_base + pi0, prow0, c);
     }
   }
 }

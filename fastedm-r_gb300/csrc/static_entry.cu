@@ -168,6 +168,7 @@ extern "C" int fedm_predict_static(const double* lib_manifold, const double* lib
   task.save_coeffs = 0;
   task.all_mode = 0;
   task.mixed = 0;
+  task.perm_off = -1;
   init.flags[0] = 0;
   init.flags[1] = INT_MAX;
   init.flags[2] = INT_MIN;
