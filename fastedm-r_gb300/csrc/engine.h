@@ -45,8 +45,9 @@ public:
   // share the SMs; 0 largest first (FEDM_ITEM_ORDER=interleave|lpt).
   int item_order = 1;
   // Lane order of the one-point mixed kernels: 1 (default) points of a work
-  // item in Morton order of their manifold coordinates, 0 list order
-  // (FEDM_POINT_ORDER=morton|list).  Results do not depend on it.
+  // item in Morton order of their first four manifold coordinates (three
+  // when E_a < 4), 2 of their first three, 0 list order
+  // (FEDM_POINT_ORDER=morton|morton3|list).  Results do not depend on it.
   int point_order = 1;
   // the lane orders computed during the current call, by (list, first row,
   // rows, manifold): a CCM call's batches share its prediction list

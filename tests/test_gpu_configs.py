@@ -261,6 +261,34 @@ def test_mixed_kernel_forms_agree(form, algorithm, monkeypatch):
 
 
 @pytest.mark.parametrize("algorithm", ["simplex", "smap"])
+@pytest.mark.parametrize("point_order,item_order", [("list", "lpt"), ("morton3", "interleave"),
+                                                    ("morton", "lpt"), ("morton", "interleave")])
+def test_lane_and_item_orders_keep_bits(point_order, item_order, algorithm, monkeypatch):
+    """The one-point kernels put a work item's points on lanes in list order
+    or in Morton order of three or four manifold coordinates, and take work
+    items largest first or large and small alternately: scheduling only, so
+    every order gives the FP64 path's bits (E = 4 and E = 2 tasks)."""
+    monkeypatch.setenv("FEDM_POINT_ORDER", point_order)
+    monkeypatch.setenv("FEDM_ITEM_ORDER", item_order)
+    w = workloads.ccm_config(T=5000, reps=2, n_libs=4, hi=4000)
+    cm = fedm.Context(0, precision=fedm.PRECISION_MIXED)
+    c64 = fedm.Context(0, precision=fedm.PRECISION_FP64)
+    try:
+        for E in (4, 2):
+            kw = dict(E=E, library=w["libraries"], numReps=2, seed=w["seed"], algorithm=algorithm,
+                      theta=2.0 if algorithm == "smap" else 1.0, savePredictions=True)
+            g = fedm.edm(w["t"], w["x"], w["y"], ctx=cm, **kw)
+            assert cm.timing()["mixed_form"] >= 0
+            f = fedm.edm(w["t"], w["x"], w["y"], ctx=c64, **kw)
+            assert g["rc"] == f["rc"] == 0
+            assert np.array_equal(g["stats"]["rho"], f["stats"]["rho"], equal_nan=True), E
+            assert np.array_equal(g["predictions"], f["predictions"], equal_nan=True), E
+    finally:
+        cm.close()
+        c64.close()
+
+
+@pytest.mark.parametrize("algorithm", ["simplex", "smap"])
 @pytest.mark.parametrize("form", ["one16", "fused2"])
 def test_k_up_to_16_forms_agree(form, algorithm, monkeypatch):
     """For 7 <= k <= 14 the mixed path has two forms: one point per thread
