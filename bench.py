@@ -474,13 +474,14 @@ def config_steps(fedm, workloads, ctx, name):
             n = len(range(0, 9998, stride)) * len(w["thetas"])
             return n, dt, f"every {stride}th prediction row, all 81 thetas"
         return {"workload": "smap_kall_lib9998_pred9998_E5_theta0-8x81", "T": 20000}, step, cpu
-    if name in ("panels", "panels_independent"):
-        # independent panels (panelWeight = Inf) are timed with two-fold
-        # cross-validation over shuffled folds, so that every panel has
-        # library rows: edm()'s default split (and unshuffled folds) give the
-        # library whole panels, and almost no prediction panel a neighbour
+    if name in ("panels", "panels_independent", "panels_penalty"):
+        # independent panels (panelWeight = Inf) and penalised ones
+        # (panelWeight = 0.1) are timed with two-fold cross-validation over
+        # shuffled folds, so that every panel has library rows: edm()'s
+        # default split (and unshuffled folds) give the library whole
+        # panels, and almost no prediction panel a neighbour of its own
         w = workloads.panel_config()
-        pw = float("inf") if name == "panels_independent" else 0.0
+        pw = {"panels": 0.0, "panels_independent": float("inf"), "panels_penalty": 0.1}[name]
         extra = dict(crossfold=2, shuffle=True, seed=1) if pw else {}
         kws = [dict(panel=w["panel"], E=[3, 4, 5, 6, 7, 8], dt=True, algorithm="simplex", panelWeight=pw, **extra),
                dict(panel=w["panel"], E=[3, 4, 5, 6, 7, 8], dt=True, algorithm="smap", theta=[0.0, 1.0, 2.0, 4.0],
@@ -494,7 +495,7 @@ def config_steps(fedm, workloads, ctx, name):
                 out.append((ctx.timing(), time.perf_counter() - t0))
             return out
 
-        def cpu(stride=1000 if pw == 0 else 50):
+        def cpu(stride=50 if pw == float("inf") else 1000):
             edm_oracle.set_pred_stride(stride)
             n = 0
             try:
@@ -507,9 +508,10 @@ def config_steps(fedm, workloads, ctx, name):
                 edm_oracle.set_pred_stride(1)
             n_pred = int(fedm.host_plan(fedm.normalise(w["t"], w["x"], **kws[0]))["pred"][0].sum())
             return n * len(range(0, n_pred, stride)), dt, f"every {stride}th prediction row, every E and theta"
-        mode = "independent_panels_crossfold2_shuffled" if pw else "mixed_library"
+        mode = {"panels": "mixed_library", "panels_independent": "independent_panels_crossfold2_shuffled",
+                "panels_penalty": "penalty0.1_crossfold2_shuffled"}[name]
         return {"workload": f"panels512_rows{len(w['t'])}_E3-8_dt_simplex+smap4theta_{mode}",
-                "rows": len(w["t"]), "panelWeight": "Inf" if pw else 0}, step, cpu
+                "rows": len(w["t"]), "panelWeight": "Inf" if pw == float("inf") else pw}, step, cpu
     if name == "easy_edm":
         # easy_edm()'s default (quantile) workflow, R/easy_edm.R:40-433, on a
         # coupled logistic pair of T = 5000: E search 3..10; a 101-theta
@@ -671,7 +673,7 @@ def config_roofline(name, precision, steps_tm, peaks):
                 "peak_source": ("measured FFMA rate (fedm_measure_peak kind 0); each double-float multiply-add "
                                 "takes ~11 FP32 instructions") if fast else
                                "measured unfused FP64 multiply/add rate (fedm_measure_peak kind 3)"}
-    if name in ("panels", "panels_independent"):
+    if name in ("panels", "panels_independent", "panels_penalty"):
         # two pipes share the kernel: the FP32 scan and the FP64 re-rank and
         # S-map solves (up to 17 x 17 Jacobi SVDs at E = 8 with dt); the
         # bound is the one with the larger fraction, the other is given beside
@@ -841,8 +843,8 @@ def main():
                     help="context precision for the non-headline workloads: mixed (bit-exact) or fast (FP32 "
                          "weights and double-float normal equations for the k = all S-map)")
     ap.add_argument("--workload", default="ccm",
-                    choices=["ccm", "simplex_explore", "smap_sweep", "panels", "panels_independent", "adjoint",
-                             "easy_edm"],
+                    choices=["ccm", "simplex_explore", "smap_sweep", "panels", "panels_independent",
+                             "panels_penalty", "adjoint", "easy_edm"],
                     help="ccm (default): the headline CCM benchmark; the others time the other benchmark "
                          "configurations at full size")
     a = ap.parse_args()

@@ -26,6 +26,7 @@ CU_FLAGS = {
     "kernels_mixed.cu": [],
     "kernels_wide.cu": [],
     "kernels_one16.cu": [],
+    "kernels_pen.cu": [],
     "kernels_split.cu": [],
     "kernels_gram_tc.cu": [],
     "static_entry.cu": [],

@@ -428,8 +428,10 @@ constexpr size_t LAZY_FIRST_BATCH = 64;  // first task batch of a group with laz
 constexpr long long FB_CAP = 1 << 24;
 
 // Whether the mixed kernel's preconditions hold for a group (see
-// kernels_mixed.cu): L2, no missing values in any used row, no panel
-// penalty (independent panels only through per-panel sub-tasks), no
+// kernels_mixed.cu): L2, no missing values in any used row, no id weights,
+// a panel penalty only between 1e-30 and 1e30 (a normal FP32 number whose
+// sum with a squared distance cannot overflow; served by the one-point
+// forms), independent panels only through per-panel sub-tasks, no
 // past-only rule, Ea <= 16.  Also returns the per-column centre and the
 // largest centred row norm.
 bool mixed_eligible(const Context& ctx, const Options& o, const GroupJob& job, bool panel_split,
@@ -438,9 +440,10 @@ bool mixed_eligible(const Context& ctx, const Options& o, const GroupJob& job, b
   if (ctx.precision == FEDM_PRECISION_FP64 || o.distance != 1 || o.has_missing || o.low_memory || o.past_only ||
       !o.force_compute || job.Ea > WIDE_EA || job.Ea < 1 || !job.hF || !job.hFp)
     return false;
-  // a panel penalty or id weights change the distances; independent panels
+  // id weights change the distances per pair of panels; independent panels
   // are served when every task is split into per-panel sub-tasks
-  if (o.panel_mode && (o.idw > 0 || o.has_id_weights || (o.idw < 0 && !panel_split)))
+  if (o.panel_mode && (o.has_id_weights || (o.idw > 0 && !(o.idw >= 1e-30 && o.idw <= 1e30)) ||
+                       (o.idw < 0 && !panel_split)))
     return false;
   const int Ea = job.Ea;
   std::vector<double> lo(Ea, INFINITY), hi(Ea, -INFINITY);
@@ -1021,8 +1024,11 @@ void run_group(Context& ctx, const Options& o, const std::vector<Task>& tasks, c
       const bool ws = o.algorithm == 1 && (form == MIXED_WS4 || form == MIXED_WS8);
       return form != MIXED_FUSED2 && form != MIXED_ONE16 && !ws;
     };
+    // panels with a finite penalty: the one-point forms only
+    const bool pen = o.panel_mode && o.idw > 0;
     // the split S-map serves E_a <= 4 with at most six neighbours
-    const bool split_ok = o.algorithm == 1 && !wide && C == 8 && kmix <= SPLIT_SLOTS && Ea <= SPLIT_MAX_EA;
+    const bool split_ok =
+      o.algorithm == 1 && !wide && !pen && C == 8 && kmix <= SPLIT_SLOTS && Ea <= SPLIT_MAX_EA;
     auto points_per_item = [&](int form) { return (wide || is_one(form)) ? WIDE_POINTS : MIX_POINTS; };
     const long long nrows = (long long)rows.n_rows;
     double* d_center = (double*)ctx.buf("center", Ea * 8);
@@ -1149,7 +1155,9 @@ void run_group(Context& ctx, const Options& o, const std::vector<Task>& tasks, c
     };
     auto launch_form = [&](int form) {
       m.form = form;
-      if (wide)
+      if (pen)
+        launch_mixed_pen(g, m, C, ctx.num_sms, s);
+      else if (wide)
         launch_knn_wide(g, m, ctx.num_sms, s);
       else if (form == MIXED_SPLIT && split_ok)
         split_pipeline();
@@ -1167,7 +1175,9 @@ void run_group(Context& ctx, const Options& o, const std::vector<Task>& tasks, c
       m.item_end = m.n_items;
     };
     int form = C == 16 ? ctx.mixed_form16 : ctx.mixed_form;
-    if (!wide && ctx.autotune) {
+    if (pen)
+      form = C == 16 ? MIXED_ONE16 : MIXED_ONE6;
+    if (!wide && !pen && ctx.autotune) {
       // Autotuner: every form gives the same bits, so the first batch of
       // each (algorithm, E_a, k) with enough points times each candidate
       // form on the same leading tasks (about two waves of the default

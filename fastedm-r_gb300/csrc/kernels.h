@@ -264,6 +264,11 @@ void launch_mixed_one(const GroupParams& g, const MixedRun& m, int num_sms, cuda
 // The same for 7 <= k <= 14 (MIXED_ONE16, kernels_one16.cu).
 void launch_mixed_one16(const GroupParams& g, const MixedRun& m, int num_sms, cudaStream_t s);
 
+// Panels with a finite penalty (panel_mode, idw > 0): the one-point form for
+// E_a and C (8 or 16 slots; the wide form at E_a > 8) with the penalty in
+// the scan (kernels_pen.cu).
+void launch_mixed_pen(const GroupParams& g, const MixedRun& m, int C, int num_sms, cudaStream_t s);
+
 // Differentiable S-map over every library neighbour (kernels_adjoint.cu).
 struct AdjointParams
 {

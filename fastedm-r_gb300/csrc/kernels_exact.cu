@@ -349,6 +349,15 @@ __global__ void __launch_bounds__(32 * REFINE_WARPS) knn_refine_kernel(GroupPara
     for (int w = 1; w < REFINE_WARPS; w++)
       same = same && (s_task[w] < 0 || s_task[w] == t0);
     const DevTask T = g.tasks[has ? ti : t0];
+    // panels with a finite penalty: the scan's FP32 value of a row of
+    // another panel carries idw (one_point.cuh), and so does the value
+    // compared with the point's bound here
+    const bool pen = g.panel_mode && g.idw > 0;
+    const float penf = pen ? (float)g.idw : 0.f;
+    const int ppan = pen && has ? g.panel[prow] : 0;
+    auto value = [&](float v, int li) {
+      return pen && g.panel[g.lib_rows[T.lib_off + li]] != ppan ? __fadd_rn(v, penf) : v;
+    };
     int count = 0;
     bool over = false;
     if (same) {
@@ -363,7 +372,7 @@ __global__ void __launch_bounds__(32 * REFINE_WARPS) knn_refine_kernel(GroupPara
         if (has && !over)
           for (int i0 = 0; i0 < nrow; i0 += 32) {
             const int i = i0 + lane;
-            const bool hit = i < nrow && (double)refine_sq<EA>(tile + i * TS, np) <= thr;
+            const bool hit = i < nrow && (double)value(refine_sq<EA>(tile + i * TS, np), b0 + i) <= thr;
             if (!refine_append(hit, b0 + i, lane, sI, count)) {
               over = true;
               break;
@@ -373,8 +382,8 @@ __global__ void __launch_bounds__(32 * REFINE_WARPS) knn_refine_kernel(GroupPara
     } else if (has) {
       for (int b0 = 0; b0 < T.n_lib; b0 += 32) {
         const int i = b0 + lane;
-        const bool hit =
-          i < T.n_lib && (double)refine_sq<EA>(r.F32 + (size_t)g.lib_rows[T.lib_off + i] * r.rs, np) <= thr;
+        const bool hit = i < T.n_lib &&
+                         (double)value(refine_sq<EA>(r.F32 + (size_t)g.lib_rows[T.lib_off + i] * r.rs, np), i) <= thr;
         if (!refine_append(hit, i, lane, sI, count)) {
           over = true;
           break;

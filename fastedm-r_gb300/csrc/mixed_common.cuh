@@ -57,11 +57,13 @@ __device__ __forceinline__ void note_rc_m(const GroupParams& g, int task, int co
 
 // FP64 distance of library row `row` to the prediction row values y
 // (src/distances.cpp:194-225 without missing values or panels).
+// s0: the panel penalty the reference adds first (0, or idw for a row of
+// another panel; src/distances.cpp:180-181).
 template<int EA>
-__device__ __forceinline__ double fp64_sq(const GroupParams& g, int row, const double (&y)[EA])
+__device__ __forceinline__ double fp64_sq(const GroupParams& g, int row, const double (&y)[EA], double s0 = 0.0)
 {
   const double* x = g.F + (size_t)row * EA;
-  double s = 0.0;
+  double s = s0;
 #pragma unroll
   for (int j = 0; j < EA; j++) {
     const double df = sub(x[j], y[j]);
@@ -135,12 +137,18 @@ __device__ __forceinline__ bool prepare_point(const GroupParams& g, const MixedR
 #pragma unroll
   for (int j = 0; j < EA; j++)
     y[j] = g.Fp[(size_t)prow * EA + j];
+  // panels with a finite penalty: the reference starts a row of another
+  // panel at 0 + idw * 1 = idw, a row of the point's panel at 0
+  const bool pen = g.panel_mode && g.idw > 0;
+  const int ppan = pen ? g.panel[prow] : 0;
+  auto start = [&](int row) { return pen && g.panel[row] != ppan ? g.idw : 0.0; };
   int ci[C + ZCAP];
   int nc = 0;
 #pragma unroll
   for (int j = 0; j < C; j++) {
     if (j < lc && (double)D[j] <= thr) {
-      const double s = fp64_sq<EA>(g, g.lib_rows[T.lib_off + I[j]], y);
+      const int row = g.lib_rows[T.lib_off + I[j]];
+      const double s = fp64_sq<EA>(g, row, y, start(row));
       cd[nc] = __dsqrt_rn(s);
       ci[nc] = I[j];
       nc++;
@@ -150,7 +158,8 @@ __device__ __forceinline__ bool prepare_point(const GroupParams& g, const MixedR
 #pragma unroll
   for (int j = 0; j < ZCAP; j++) {
     if (j < z) {
-      const double s = fp64_sq<EA>(g, g.lib_rows[T.lib_off + zi[j]], y);
+      const int row = g.lib_rows[T.lib_off + zi[j]];
+      const double s = fp64_sq<EA>(g, row, y, start(row));
       if (s != 0) {
         cd[nc] = __dsqrt_rn(s);
         ci[nc] = zi[j];
@@ -159,7 +168,7 @@ __device__ __forceinline__ bool prepare_point(const GroupParams& g, const MixedR
       }
     }
   }
-  ops += nc * (3 * EA + 1);
+  ops += nc * (3 * EA + 1 + (pen ? 2 : 0));
   const int numValid = T.n_lib - z + zvalid;
   const int kr = T.k_req < 0 ? numValid : T.k_req;
   keff = kr < numValid ? kr : numValid;

@@ -15,10 +15,16 @@ namespace fedm {
 namespace {
 
 // One point per thread: C candidate slots, float manifold row stride RS,
-// TR library rows per shared-memory tile, NT threads per CTA.
-template<int EA, int C, int RS, int TR, int NT>
+// TR library rows per shared-memory tile, NT threads per CTA.  PEN: panels
+// with a finite penalty (panelWeight = idw > 0): a library row of another
+// panel than the point's scores idw more (src/distances.cpp:180-181), with
+// the tile's panel ids staged in tpan.  The FP32 value then carries one more
+// rounded addition, within the certification's accumulation bound, and
+// sqrt(idw + x^2) is 1-Lipschitz in x, so the input-rounding term holds too.
+template<int EA, int C, int RS, int TR, int NT, bool PEN = false>
 __device__ __forceinline__ void scan_item_one(const GroupParams& g, const MixedRun& m, const DevTask& T, int first,
-                                              int tid, float2* tile, Cand<C>& c0, int& prow0, bool& a0, int& pi)
+                                              int tid, float2* tile, int* tpan, Cand<C>& c0, int& prow0, bool& a0,
+                                              int& pi)
 {
   // the slot's point: list order, or the task's lane order (points close
   // in the manifold on neighbouring lanes, so that a warp's candidate
@@ -47,6 +53,8 @@ __device__ __forceinline__ void scan_item_one(const GroupParams& g, const MixedR
 #pragma unroll
   for (int j = 0; j < ZCAP; j++)
     zi0[j] = -1;
+  const float pen = PEN ? (float)g.idw : 0.f;
+  const int ppan = PEN && a0 ? g.panel[prow0] : 0;
   for (int t0 = 0; t0 < T.n_lib; t0 += TR) {
     const int cnt = min(TR, T.n_lib - t0);
     const int npairs = (cnt + 1) >> 1;
@@ -54,14 +62,19 @@ __device__ __forceinline__ void scan_item_one(const GroupParams& g, const MixedR
     for (int i = tid; i < 2 * npairs; i += NT) {
       float* dst = reinterpret_cast<float*>(tile + (i >> 1) * EA) + (i & 1);
       if (i < cnt) {
-        const float* src = m.F32 + (size_t)g.lib_rows[T.lib_off + t0 + i] * RS;
+        const int row = g.lib_rows[T.lib_off + t0 + i];
+        const float* src = m.F32 + (size_t)row * RS;
 #pragma unroll
         for (int j = 0; j < EA; j++)
           dst[2 * j] = src[j];
+        if constexpr (PEN)
+          tpan[i] = g.panel[row];
       } else {
 #pragma unroll
         for (int j = 0; j < EA; j++)
           dst[2 * j] = 1e30f;  // padding row: never a candidate
+        if constexpr (PEN)
+          tpan[i] = 0;  // any panel: the padding row's value is +inf
       }
     }
     __syncthreads();
@@ -74,6 +87,10 @@ __device__ __forceinline__ void scan_item_one(const GroupParams& g, const MixedR
       for (int j = 1; j < EA; j++) {
         d = __fadd2_rn(xr[j], na[j]);
         sa = __ffma2_rn(d, d, sa);
+      }
+      if constexpr (PEN) {
+        const int2 pp = reinterpret_cast<const int2*>(tpan)[ip];
+        sa = __fadd2_rn(sa, make_float2(pp.x != ppan ? pen : 0.f, pp.y != ppan ? pen : 0.f));
       }
       if (fminf(sa.x, sa.y) < D0[C - 1]) {
         const int li = t0 + 2 * ip;
@@ -93,10 +110,11 @@ __device__ __forceinline__ void scan_item_one(const GroupParams& g, const MixedR
     c0.zi[j] = zi0[j];
 }
 
-template<int EA, int C, int RS, int TR, int ALG, int OCC, int NT = TPB>
+template<int EA, int C, int RS, int TR, int ALG, int OCC, int NT = TPB, bool PEN = false>
 __global__ void __launch_bounds__(NT, OCC) knn_one_kernel(GroupParams g, MixedRun m)
 {
   __shared__ __align__(16) float2 tile[(TR / 2) * EA];
+  __shared__ __align__(8) int tpan[PEN ? TR : 2];
   __shared__ int s_item;
   const int tid = threadIdx.x;
   unsigned long long ops = 0;
@@ -115,7 +133,7 @@ __global__ void __launch_bounds__(NT, OCC) knn_one_kernel(GroupParams g, MixedRu
     Cand<C> c0;
     int prow0, pi0;
     bool a0;
-    scan_item_one<EA, C, RS, TR, NT>(g, m, T, it.y, tid, tile, c0, prow0, a0, pi0);
+    scan_item_one<EA, C, RS, TR, NT, PEN>(g, m, T, it.y, tid, tile, tpan, c0, prow0, a0, pi0);
     if constexpr (ALG == 2) {
       // S-map lists for smap_list_kernel: settle the neighbours, write them
       const long long slot = (long long)(item - m.item_begin) * NT + tid;
@@ -142,11 +160,11 @@ __global__ void __launch_bounds__(NT, OCC) knn_one_kernel(GroupParams g, MixedRu
   }
 }
 
-template<int EA, int C, int RS, int TR, int ALG, int OCC, int NT = TPB>
+template<int EA, int C, int RS, int TR, int ALG, int OCC, int NT = TPB, bool PEN = false>
 void launch_one(const GroupParams& g, const MixedRun& m, int num_sms, cudaStream_t s)
 {
   int per_sm = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, knn_one_kernel<EA, C, RS, TR, ALG, OCC, NT>, NT, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, knn_one_kernel<EA, C, RS, TR, ALG, OCC, NT, PEN>, NT, 0);
   if (m.ctas_per_sm > 0 && per_sm > m.ctas_per_sm)
     per_sm = m.ctas_per_sm;
   if (per_sm < 1)
@@ -156,7 +174,64 @@ void launch_one(const GroupParams& g, const MixedRun& m, int num_sms, cudaStream
     blocks = m.item_end - m.item_begin;
   if (blocks < 1)
     blocks = 1;
-  knn_one_kernel<EA, C, RS, TR, ALG, OCC, NT><<<(int)blocks, NT, 0, s>>>(g, m);
+  knn_one_kernel<EA, C, RS, TR, ALG, OCC, NT, PEN><<<(int)blocks, NT, 0, s>>>(g, m);
+}
+
+// The one-point forms by E_a: MIXED_ONE6 (eight candidate slots, six CTAs
+// per SM), MIXED_ONE16 (sixteen slots, four CTAs per SM) and the wide form
+// (E_a 9..16, 32 slots, 512-row tiles, two CTAs per SM).
+constexpr int WTILE = 512;  // wide form: library rows per tile, 32 KB of shared memory at E_a = 16
+constexpr int WC = 32;      // wide form: candidate slots per point
+constexpr int WS = 16;      // wide form: row stride of the float manifold
+
+template<int ALG, bool PEN>
+void launch_one6_t(const GroupParams& g, const MixedRun& m, int num_sms, cudaStream_t s)
+{
+  constexpr int OCC = 6;
+  switch (g.Ea) {
+    case 1: launch_one<1, 8, 4, 1024, ALG, OCC, TPB, PEN>(g, m, num_sms, s); break;
+    case 2: launch_one<2, 8, 4, 1024, ALG, OCC, TPB, PEN>(g, m, num_sms, s); break;
+    case 3: launch_one<3, 8, 4, 1024, ALG, OCC, TPB, PEN>(g, m, num_sms, s); break;
+    case 4: launch_one<4, 8, 4, 1024, ALG, OCC, TPB, PEN>(g, m, num_sms, s); break;
+    case 5: launch_one<5, 8, 8, 1024, ALG, OCC, TPB, PEN>(g, m, num_sms, s); break;
+    case 6: launch_one<6, 8, 8, 1024, ALG, OCC, TPB, PEN>(g, m, num_sms, s); break;
+    case 7: launch_one<7, 8, 8, 1024, ALG, OCC, TPB, PEN>(g, m, num_sms, s); break;
+    case 8: launch_one<8, 8, 8, 1024, ALG, OCC, TPB, PEN>(g, m, num_sms, s); break;
+    default: break;
+  }
+}
+
+template<int ALG, bool PEN>
+void launch_one16_t(const GroupParams& g, const MixedRun& m, int num_sms, cudaStream_t s)
+{
+  constexpr int OCC = 4;
+  switch (g.Ea) {
+    case 1: launch_one<1, 16, 4, 1024, ALG, OCC, TPB, PEN>(g, m, num_sms, s); break;
+    case 2: launch_one<2, 16, 4, 1024, ALG, OCC, TPB, PEN>(g, m, num_sms, s); break;
+    case 3: launch_one<3, 16, 4, 1024, ALG, OCC, TPB, PEN>(g, m, num_sms, s); break;
+    case 4: launch_one<4, 16, 4, 1024, ALG, OCC, TPB, PEN>(g, m, num_sms, s); break;
+    case 5: launch_one<5, 16, 8, 1024, ALG, OCC, TPB, PEN>(g, m, num_sms, s); break;
+    case 6: launch_one<6, 16, 8, 1024, ALG, OCC, TPB, PEN>(g, m, num_sms, s); break;
+    case 7: launch_one<7, 16, 8, 1024, ALG, OCC, TPB, PEN>(g, m, num_sms, s); break;
+    case 8: launch_one<8, 16, 8, 1024, ALG, OCC, TPB, PEN>(g, m, num_sms, s); break;
+    default: break;
+  }
+}
+
+template<int ALG, bool PEN>
+void launch_wide_t(const GroupParams& g, const MixedRun& m, int num_sms, cudaStream_t s)
+{
+  switch (g.Ea) {
+    case 9: launch_one<9, WC, WS, WTILE, ALG, 2, TPB, PEN>(g, m, num_sms, s); break;
+    case 10: launch_one<10, WC, WS, WTILE, ALG, 2, TPB, PEN>(g, m, num_sms, s); break;
+    case 11: launch_one<11, WC, WS, WTILE, ALG, 2, TPB, PEN>(g, m, num_sms, s); break;
+    case 12: launch_one<12, WC, WS, WTILE, ALG, 2, TPB, PEN>(g, m, num_sms, s); break;
+    case 13: launch_one<13, WC, WS, WTILE, ALG, 2, TPB, PEN>(g, m, num_sms, s); break;
+    case 14: launch_one<14, WC, WS, WTILE, ALG, 2, TPB, PEN>(g, m, num_sms, s); break;
+    case 15: launch_one<15, WC, WS, WTILE, ALG, 2, TPB, PEN>(g, m, num_sms, s); break;
+    case 16: launch_one<16, WC, WS, WTILE, ALG, 2, TPB, PEN>(g, m, num_sms, s); break;
+    default: break;
+  }
 }
 
 } // namespace

@@ -112,7 +112,8 @@ def test_headline_line(bench, monkeypatch):
     assert d["concurrent_calls"]["value"] > 0 and d["concurrent_calls"]["rho_identical_to_sequential"]
 
 
-@pytest.mark.parametrize("workload", ["simplex_explore", "smap_sweep", "panels", "panels_independent", "adjoint",
+@pytest.mark.parametrize("workload", ["simplex_explore", "smap_sweep", "panels", "panels_independent",
+                                      "panels_penalty", "adjoint",
                                       "easy_edm"])
 def test_other_workloads_line(bench, monkeypatch, workload):
     # the oracle's CPU sample runs for real on the quick workloads

@@ -3,7 +3,8 @@
 * S-map theta sweep with k = all (config 2 shape), at an oracle-tractable
   size: through the task seam (bit-exact) and through run_command.
 * Uneven multispatial panels with missing values and dt (config 4 shape),
-  reduced to 48 panels: run_command with mixed and independent panels.
+  reduced to 48 panels: run_command with pooled, penalised and independent
+  panels; penalties outside the FP32 range stay on the FP64 kernels.
 * Config 2 at full size (10 000 / 10 000): with theta = 0 every weight is 1,
   so S-map is ordinary least squares on the library; the forecasts must match
   numpy's lstsq (a check that needs no oracle).
@@ -65,9 +66,13 @@ def test_smap_theta_sweep_all_neighbours_command(ctx):
     assert np.array_equal(g["coeffs"], o["coeffs"], equal_nan=True)
 
 
-@pytest.mark.parametrize("panel_weight", [0.0, float("inf")], ids=["mixed_panels", "independent_panels"])
+@pytest.mark.parametrize("panel_weight", [0.0, 0.02, 0.3, float("inf")],
+                         ids=["mixed_panels", "penalty_0.02", "penalty_0.3", "independent_panels"])
 @pytest.mark.parametrize("algorithm", ["simplex", "smap"])
 def test_uneven_panels_missing_dt(ctx, panel_weight, algorithm):
+    """48 uneven panels, E = 3..8 with dt: panels pooled (panelWeight = 0),
+    pooled with a penalty for a library row of another panel (small enough
+    that other panels' rows are often neighbours), and independent."""
     w = workloads.panel_config(n_panels=48, lo=40, hi=300)
     theta = [0.0, 1.0, 2.0, 4.0] if algorithm == "smap" else [1.0]
     kw = dict(panel=w["panel"], E=[3, 4, 5, 6, 7, 8], dt=True, algorithm=algorithm, theta=theta,
@@ -78,6 +83,22 @@ def test_uneven_panels_missing_dt(ctx, panel_weight, algorithm):
     o = edm_oracle.oracle_edm(w["t"], w["x"], numThreads=16, **kw)
     _stats_close(g, o)
     assert g["kMin"] == o["kMin"] and g["kMax"] == o["kMax"] and g["dtWeight"] == o["dtWeight"]
+
+
+@pytest.mark.parametrize("panel_weight", [1e-35, 1e35])
+def test_panel_penalty_outside_fp32_range_stays_exact(panel_weight):
+    """A penalty below 1e-30 or above 1e30 is no normal FP32 number the scan
+    could add with a bounded error: such calls run on the FP64 kernels."""
+    w = workloads.panel_config(n_panels=12, lo=40, hi=200)
+    kw = dict(panel=w["panel"], E=[3, 5], dt=True, algorithm="simplex", theta=[1.0], panelWeight=panel_weight)
+    c = fedm.Context(0, precision=fedm.PRECISION_MIXED)
+    try:
+        g = fedm.edm(w["t"], w["x"], ctx=c, **kw)
+        assert c.timing()["mixed_form"] < 0
+    finally:
+        c.close()
+    o = edm_oracle.oracle_edm(w["t"], w["x"], numThreads=16, **kw)
+    _stats_close(g, o)
 
 
 def test_ccm_replicates_reduced(ctx):

@@ -14,8 +14,8 @@ be the oracle's bits.
 * S-map theta sweep with k = all (10 000 library x 10 000 prediction rows,
   81 thetas), forecasts and the last theta's coefficients.
 * 512 uneven panels with missing values and dt, E = 3..8, simplex and the
-  4-theta S-map, with mixed (panelWeight = 0) and independent
-  (panelWeight = Inf) panels.
+  4-theta S-map, with mixed (panelWeight = 0), penalised (panelWeight =
+  0.1) and independent (panelWeight = Inf) panels.
 """
 import numpy as np
 import pytest
@@ -140,7 +140,8 @@ def test_smap_sweep_full_size_bit_exact(mixed_ctx):
     assert np.array_equal(g["kused"][sel], o["kused"])
 
 
-@pytest.mark.parametrize("panel_weight", [0.0, float("inf")], ids=["mixed_panels", "independent_panels"])
+@pytest.mark.parametrize("panel_weight", [0.0, 0.1, float("inf")],
+                         ids=["mixed_panels", "penalty_0.1", "independent_panels"])
 @pytest.mark.parametrize("algorithm", ["simplex", "smap"])
 def test_panels_full_size_bit_exact(mixed_ctx, algorithm, panel_weight):
     """Config 4 at full size: 512 panels of 50..2000 rows, 5% missing, dt,
@@ -155,8 +156,8 @@ def test_panels_full_size_bit_exact(mixed_ctx, algorithm, panel_weight):
     for f in range(6):
         E, k = int(plan["E"][f]), int(plan["k"][f])
         g = mixed_ctx.run_task(a, plan["lib"][f], plan["pred"][f], E, k)
-        # both panel modes run on the mixed kernels (independent panels as
-        # per-panel sub-tasks)
+        # every panel mode runs on the mixed kernels (independent panels as
+        # per-panel sub-tasks, the penalty inside the one-point scan)
         assert mixed_ctx.timing()["mixed_form"] >= 0
         sub, sel = _strided(plan["pred"][f], 331, offset=f)
         o = _oracle(kw, w["t"], w["x"], None, plan["lib"][f], sub, E, k)
