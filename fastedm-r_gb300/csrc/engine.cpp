@@ -11,6 +11,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <climits>
 #include <cmath>
@@ -122,38 +123,90 @@ uint32_t spread4(uint32_t v)
 // manifold coordinates (F row-major, Ea columns), quantised to 10 bits over
 // the rows' range -- or, with dims = 4, of their first four at 8 bits (at
 // E_a = 4 that keys every coordinate; CCM's S-map step is 1.2% shorter than
-// with three).  Ties keep list order.
+// with three).  Ties keep list order: the sort key is (Morton key, list
+// position).  Long lists are split over host threads: ranges and keys per
+// thread, a stable split on the key's top byte, then each of the 256
+// buckets sorted alone -- the order of one global sort.
 std::vector<int> morton_lane_order(const std::vector<double>& F, int Ea, const int* rows, int n, int dims = 3)
 {
   const int D = std::min(Ea, dims);
   const int bits = dims == 4 ? 8 : 10;
-  double lo[4] = { 0, 0, 0, 0 }, hi[4] = { 0, 0, 0, 0 };
+  const int hw = std::max(1, std::min(16, (int)std::thread::hardware_concurrency()));
+  const int nt = std::max(1, std::min(hw, n / 16384));
+  auto par = [nt](auto&& fn) {
+    std::vector<std::thread> pool;
+    for (int w = 1; w < nt; w++)
+      pool.emplace_back(fn, w);
+    fn(0);
+    for (auto& t : pool)
+      t.join();
+  };
+  auto first = [&](int w) { return (long long)n * w / nt; };
+  std::vector<double> tlo((size_t)nt * 4, INFINITY), thi((size_t)nt * 4, -INFINITY);
+  par([&](int w) {
+    double l[4] = { INFINITY, INFINITY, INFINITY, INFINITY }, h[4] = { -INFINITY, -INFINITY, -INFINITY, -INFINITY };
+    for (long long i = first(w); i < first(w + 1); i++)
+      for (int j = 0; j < D; j++) {
+        const double v = F[(size_t)rows[i] * Ea + j];
+        l[j] = std::min(l[j], v);
+        h[j] = std::max(h[j], v);
+      }
+    for (int j = 0; j < 4; j++) {
+      tlo[(size_t)w * 4 + j] = l[j];
+      thi[(size_t)w * 4 + j] = h[j];
+    }
+  });
+  const double top = (double)((1 << bits) - 1);
+  double lo[4] = { 0, 0, 0, 0 }, scale[4] = { 0, 0, 0, 0 };
   for (int j = 0; j < D; j++) {
-    lo[j] = INFINITY;
-    hi[j] = -INFINITY;
-  }
-  for (int i = 0; i < n; i++)
-    for (int j = 0; j < D; j++) {
-      const double v = F[(size_t)rows[i] * Ea + j];
-      lo[j] = std::min(lo[j], v);
-      hi[j] = std::max(hi[j], v);
+    double l = INFINITY, h = -INFINITY;
+    for (int w = 0; w < nt; w++) {
+      l = std::min(l, tlo[(size_t)w * 4 + j]);
+      h = std::max(h, thi[(size_t)w * 4 + j]);
     }
-  std::vector<std::pair<uint32_t, int>> key(n);
-  for (int i = 0; i < n; i++) {
-    uint32_t k = 0;
-    for (int j = 0; j < D; j++) {
-      const double span = hi[j] - lo[j];
-      const double v = F[(size_t)rows[i] * Ea + j];
-      const double top = (double)((1 << bits) - 1);
-      const uint32_t qv = span > 0 && std::isfinite(v) ? (uint32_t)std::min(top, (v - lo[j]) / span * top) : 0;
-      k |= dims == 4 ? spread4(qv) << (3 - j) : spread3(qv) << (2 - j);
-    }
-    key[i] = { k, i };
+    lo[j] = l;
+    scale[j] = h > l ? top / (h - l) : 0.0;
   }
-  std::sort(key.begin(), key.end());
+  // packed (Morton key, list position), and per thread the count of each top byte
+  std::vector<uint64_t> a(n), b(n);
+  std::vector<int> pos((size_t)nt * 256, 0);
+  par([&](int w) {
+    int* cnt = &pos[(size_t)w * 256];
+    for (long long i = first(w); i < first(w + 1); i++) {
+      uint32_t k = 0;
+      for (int j = 0; j < D; j++) {
+        const double q = (F[(size_t)rows[i] * Ea + j] - lo[j]) * scale[j];
+        const uint32_t qv = q >= 0 ? (uint32_t)std::min(top, q) : 0;  // NaN: 0
+        k |= dims == 4 ? spread4(qv) << (3 - j) : spread3(qv) << (2 - j);
+      }
+      a[i] = ((uint64_t)k << 32) | (uint32_t)i;
+      cnt[k >> 24]++;
+    }
+  });
+  std::vector<int> start(257, 0);
+  int acc = 0;
+  for (int d = 0; d < 256; d++) {
+    start[d] = acc;
+    for (int w = 0; w < nt; w++) {
+      const int c = pos[(size_t)w * 256 + d];
+      pos[(size_t)w * 256 + d] = acc;
+      acc += c;
+    }
+  }
+  start[256] = acc;
+  par([&](int w) {
+    int* p = &pos[(size_t)w * 256];
+    for (long long i = first(w); i < first(w + 1); i++)
+      b[p[a[i] >> 56]++] = a[i];
+  });
+  std::atomic<int> next{ 0 };
+  par([&](int) {
+    for (int d; (d = next++) < 256;)
+      std::sort(b.begin() + start[d], b.begin() + start[d + 1]);
+  });
   std::vector<int> order(n);
   for (int i = 0; i < n; i++)
-    order[i] = key[i].second;
+    order[i] = (int)(uint32_t)b[i];
   return order;
 }
 
