@@ -27,6 +27,7 @@ CU_FLAGS = {
     "kernels_wide.cu": [],
     "kernels_one16.cu": [],
     "kernels_pen.cu": [],
+    "kernels_manifold.cu": ["--fmad=false"],
     "kernels_split.cu": [],
     "kernels_gram_tc.cu": [],
     "static_entry.cu": [],

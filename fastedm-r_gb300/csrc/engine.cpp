@@ -82,6 +82,8 @@ Context::Context(int dev) : device(dev)
     gram_tc = std::strcmp(v, "0") != 0;
   if (const char* v = std::getenv("FEDM_ITEM_ORDER"))
     item_order = std::strcmp(v, "lpt") == 0 ? 0 : 1;
+  if (const char* v = std::getenv("FEDM_HOST_MANIFOLD"))
+    host_manifold = std::strcmp(v, "1") == 0;
   if (const char* v = std::getenv("FEDM_POINT_ORDER"))
     point_order = std::strcmp(v, "list") == 0 ? 0 : (std::strcmp(v, "morton3") == 0 ? 2 : 1);
   reset_timing();
@@ -127,7 +129,7 @@ uint32_t spread4(uint32_t v)
 // position).  Long lists are split over host threads: ranges and keys per
 // thread, a stable split on the key's top byte, then each of the 256
 // buckets sorted alone -- the order of one global sort.
-std::vector<int> morton_lane_order(const std::vector<double>& F, int Ea, const int* rows, int n, int dims = 3)
+std::vector<int> morton_lane_order(const double* F, int Ea, const int* rows, int n, int dims = 3)
 {
   const int D = std::min(Ea, dims);
   const int bits = dims == 4 ? 8 : 10;
@@ -458,8 +460,8 @@ struct GroupJob
   int Ea = 0;
   const double* dF = nullptr;   // library manifold on the device
   const double* dFp = nullptr;  // prediction manifold on the device
-  const std::vector<double>* hF = nullptr;   // host copies (mixed-path margin)
-  const std::vector<double>* hFp = nullptr;
+  const double* hF = nullptr;   // host copies, row-major [n x Ea] (mixed-path margin, lane order)
+  const double* hFp = nullptr;
   bool copredict = false;
   std::vector<int> task_ids;    // indices into the run's task list
   std::vector<const std::vector<int>*> lib_lists, pred_lists;
@@ -503,7 +505,7 @@ bool mixed_eligible(const Context& ctx, const Options& o, const GroupJob& job, b
   // bounding box of the listed rows, split over host threads for long lists
   // (minimum and maximum do not depend on the split)
   const int hw = std::max(1, std::min(16, (int)std::thread::hardware_concurrency()));
-  auto scan = [&](const std::vector<double>& F, const std::vector<int>& rows) {
+  auto scan = [&](const double* F, const std::vector<int>& rows) {
     const long long n = (long long)rows.size();
     const int nt = (int)std::max<long long>(1, std::min<long long>(hw, n / 16384));
     std::vector<std::vector<double>> tlo(nt, lo), thi(nt, hi);
@@ -539,17 +541,17 @@ bool mixed_eligible(const Context& ctx, const Options& o, const GroupJob& job, b
     return true;
   };
   std::vector<const std::vector<int>*> seen_l, seen_p;
-  if (job.lib_superset && !scan(*job.hF, *job.lib_superset))
+  if (job.lib_superset && !scan(job.hF, *job.lib_superset))
     return false;
   for (size_t i = 0; i < job.lib_lists.size(); i++) {
     if (!job.lib_superset && std::find(seen_l.begin(), seen_l.end(), job.lib_lists[i]) == seen_l.end()) {
       seen_l.push_back(job.lib_lists[i]);
-      if (!scan(*job.hF, *job.lib_lists[i]))
+      if (!scan(job.hF, *job.lib_lists[i]))
         return false;
     }
     if (std::find(seen_p.begin(), seen_p.end(), job.pred_lists[i]) == seen_p.end()) {
       seen_p.push_back(job.pred_lists[i]);
-      if (!scan(*job.hFp, *job.pred_lists[i]))
+      if (!scan(job.hFp, *job.pred_lists[i]))
         return false;
     }
   }
@@ -729,7 +731,7 @@ void run_group(Context& ctx, const Options& o, const std::vector<Task>& tasks, c
         auto c = ctx.lane_orders.find(key);
         if (c == ctx.lane_orders.end())
           c = ctx.lane_orders
-                  .emplace(key, morton_lane_order(*job.hFp, Ea, Pl->data() + kt[j].pstart, kt[j].plen,
+                  .emplace(key, morton_lane_order(job.hFp, Ea, Pl->data() + kt[j].pstart, kt[j].plen,
                                                   ctx.point_order == 1 && Ea >= 4 ? 4 : 3))
                   .first;
         it = offs.emplace(key, (int)perm_pool.size()).first;
@@ -1547,24 +1549,85 @@ std::vector<int> lib_rows_of(const std::vector<uint8_t>& mask, const RowTables& 
   return r;
 }
 
+// The manifolds of one call, per (E, coprediction): on the device, and
+// their host copies (row-major [n x Ea]).
 struct Manifolds
 {
-  std::map<std::pair<int, bool>, std::vector<double>> host;
+  std::map<std::pair<int, bool>, const double*> host;
+  std::map<std::pair<int, bool>, std::vector<double>> host_store;  // host-built copies
   std::map<std::pair<int, bool>, double*> dev;
+  // the series on the device for manifold_kernel, uploaded at the first build
+  bool series = false;
+  double *x = nullptr, *co_x = nullptr, *extras = nullptr;
+  int *obs = nullptr, *target_row = nullptr;
 };
 
-double* device_manifold(Context& ctx, Manifolds& M, const Generator& g, const RowTables& rt, int E, bool co,
-                        int threads)
+// The manifold for E (co: of co_x) on the device, built once per call.  By
+// default manifold_kernel builds it from the series and the host copy comes
+// back into a pinned buffer of the context; FEDM_HOST_MANIFOLD=1 builds it
+// on host threads and uploads it.  Both give the same bits.
+double* device_manifold(Context& ctx, Manifolds& M, const Generator& g, const RowTables& rt, const DevRows& rows, int E,
+                        bool co, int threads)
 {
   auto key = std::make_pair(E, co);
   auto it = M.dev.find(key);
   if (it != M.dev.end())
     return it->second;
   const double t0 = now_ms();
-  auto& h = M.host[key];
-  h = build_manifold(g, rt, E, co, threads);
-  double* d = (double*)ctx.buf("F_" + std::to_string(E) + (co ? "_co" : ""), std::max<size_t>(h.size(), 1) * 8);
-  ctx.upload(d, h.data(), h.size() * 8);
+  const int Ea = g.E_actual(E);
+  const size_t count = (size_t)g.n * Ea;
+  const std::string name = "F_" + std::to_string(E) + (co ? "_co" : "");
+  double* d = (double*)ctx.buf(name, std::max<size_t>(count, 1) * 8);
+  if (ctx.host_manifold) {
+    auto& h = M.host_store[key];
+    h = build_manifold(g, rt, E, co, threads);
+    ctx.upload(d, h.data(), h.size() * 8);
+    M.host[key] = h.data();
+  } else {
+    const size_t n = (size_t)g.n;
+    if (!M.series) {
+      M.x = (double*)ctx.buf("series_x", n * 8);
+      ctx.upload(M.x, g.x.data(), n * 8);
+      if (!g.co_x.empty()) {
+        M.co_x = (double*)ctx.buf("series_co_x", n * 8);
+        ctx.upload(M.co_x, g.co_x.data(), n * 8);
+      }
+      if (g.num_extras > 0) {
+        M.extras = (double*)ctx.buf("series_extras", (size_t)g.num_extras * n * 8);
+        for (int e = 0; e < g.num_extras; e++)
+          ctx.upload(M.extras + (size_t)e * n, g.extras[e].data(), n * 8);
+      }
+      M.obs = (int*)ctx.buf("series_obs", n * 4);
+      ctx.upload(M.obs, g.obs.data(), n * 4);
+      M.target_row = (int*)ctx.buf("series_target_row", n * 4);
+      ctx.upload(M.target_row, rt.target_row.data(), n * 4);
+      M.series = true;
+    }
+    ManifoldParams p{};
+    p.t = rows.point_time;
+    p.x = co ? M.co_x : M.x;
+    p.extras = M.extras;
+    p.panel = g.panel_mode ? rows.panel : nullptr;
+    p.obs = M.obs;
+    p.target_row = M.target_row;
+    p.n = g.n;
+    p.E = E;
+    p.Edt = g.E_dt(E);
+    p.Ea = Ea;
+    p.tau = g.tau;
+    p.num_extras = g.num_extras;
+    p.num_extras_lagged = g.num_extras_lagged;
+    p.with_dt = (g.dt || g.reldt) ? 1 : 0;
+    p.reldt = g.reldt ? 1 : 0;
+    p.w = g.dt_weight;
+    launch_manifold(p, d, ctx.num_sms, ctx.stream);
+    ctx.check("manifold_kernel");
+    ctx.timing.kernel_launches += 1;
+    double* h = (double*)ctx.host_buf("host_" + name, std::max<size_t>(count, 1) * 8);
+    ctx.download(h, d, count * 8);
+    ck(cudaStreamSynchronize(ctx.stream), "manifold download");
+    M.host[key] = h;
+  }
   M.dev[key] = d;
   ctx.timing.manifold_ms += now_ms() - t0;
   return d;
@@ -1650,10 +1713,10 @@ CommandResult run_command(Context& ctx, const fedm_args& a)
     GroupJob job;
     job.Ea = gen.E_actual(key.first);
     job.copredict = key.second;
-    job.dF = device_manifold(ctx, M, gen, rt, key.first, false, threads);
-    job.dFp = key.second ? device_manifold(ctx, M, gen, rt, key.first, true, threads) : job.dF;
-    job.hF = &M.host[std::make_pair(key.first, false)];
-    job.hFp = key.second ? &M.host[std::make_pair(key.first, true)] : job.hF;
+    job.dF = device_manifold(ctx, M, gen, rt, drows, key.first, false, threads);
+    job.dFp = key.second ? device_manifold(ctx, M, gen, rt, drows, key.first, true, threads) : job.dF;
+    job.hF = M.host[std::make_pair(key.first, false)];
+    job.hFp = key.second ? M.host[std::make_pair(key.first, true)] : job.hF;
     std::vector<int> ids;
     for (int i = 0; i < (int)plan.tasks.size(); i++)
       if (plan.tasks[i].E == key.first && plan.tasks[i].copredict == key.second)
@@ -1737,7 +1800,7 @@ CommandResult run_command(Context& ctx, const fedm_args& a)
       // src/edm.cpp:473-475, src/r.cpp:406-409: the task's library manifold
       // (library rows whose target is observed) and prediction manifold
       // (co_x lags for coprediction), row-major, MISSING as NA
-      auto append = [&](const std::vector<double>& F, const std::vector<int>& rows, std::vector<double>& out) {
+      auto append = [&](const double* F, const std::vector<int>& rows, std::vector<double>& out) {
         for (int r : rows)
           for (int j = 0; j < Ea; j++)
             out.push_back(na(F[(size_t)r * Ea + j]));
@@ -1991,10 +2054,10 @@ int run_task(Context& ctx, const fedm_args& a, fedm_task_io& io)
     GroupJob job;
     job.Ea = Ea;
     job.copredict = t.copredict;
-    job.dF = device_manifold(ctx, M, gen, rt, io.E, false, threads);
-    job.dFp = t.copredict ? device_manifold(ctx, M, gen, rt, io.E, true, threads) : job.dF;
-    job.hF = &M.host[std::make_pair(io.E, false)];
-    job.hFp = t.copredict ? &M.host[std::make_pair(io.E, true)] : job.hF;
+    job.dF = device_manifold(ctx, M, gen, rt, drows, io.E, false, threads);
+    job.dFp = t.copredict ? device_manifold(ctx, M, gen, rt, drows, io.E, true, threads) : job.dF;
+    job.hF = M.host[std::make_pair(io.E, false)];
+    job.hFp = t.copredict ? M.host[std::make_pair(io.E, true)] : job.hF;
     job.task_ids = { 0 };
     job.lib_lists = { &L };
     job.pred_lists = { &Pl };

@@ -44,6 +44,9 @@ public:
   // smallest library alternately, so that scan-heavy and solve-heavy items
   // share the SMs; 0 largest first (FEDM_ITEM_ORDER=interleave|lpt).
   int item_order = 1;
+  // Manifolds built on host threads and uploaded (FEDM_HOST_MANIFOLD=1)
+  // instead of on the device; the same bits.
+  bool host_manifold = false;
   // Lane order of the one-point mixed kernels: 1 (default) points of a work
   // item in Morton order of their first four manifold coordinates (three
   // when E_a < 4), 2 of their first three, 0 list order

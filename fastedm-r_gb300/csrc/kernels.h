@@ -264,6 +264,23 @@ void launch_mixed_one(const GroupParams& g, const MixedRun& m, int num_sms, cuda
 // The same for 7 <= k <= 14 (MIXED_ONE16, kernels_one16.cu).
 void launch_mixed_one16(const GroupParams& g, const MixedRun& m, int num_sms, cudaStream_t s);
 
+// The lagged manifold of every observation for one E, built on the device
+// from the series (kernels_manifold.cu): row-major [n x Ea], the host
+// generator's bits.
+struct ManifoldParams
+{
+  const double* t;           // observation times
+  const double* x;           // x, or co_x for a coprediction manifold
+  const double* extras;      // [num_extras x n]
+  const int* panel;          // panel ids, null without panels
+  const int* obs;            // observation numbers (INT_MIN: missing)
+  const int* target_row;     // row of each row's forecast target, -1 if none
+  int n, E, Edt, Ea, tau, num_extras, num_extras_lagged;
+  int with_dt, reldt;
+  double w;                  // dt weight
+};
+void launch_manifold(const ManifoldParams& p, double* F, int num_sms, cudaStream_t s);
+
 // Panels with a finite penalty (panel_mode, idw > 0): the one-point form for
 // E_a and C (8 or 16 slots; the wide form at E_a > 8) with the penalty in
 // the scan (kernels_pen.cu).

@@ -450,6 +450,52 @@ def test_save_manifolds(ctx, case):
         assert any(plan["copredict"]) and not all(plan["copredict"])
 
 
+@pytest.mark.parametrize("case", ["panels_dt_missing_extras", "reldt_p2_tau3", "xmap_copredict_p_minus1"])
+def test_device_manifold_is_host_manifold(case, monkeypatch):
+    """The manifolds are built on the device (manifold_kernel: lag search
+    with panel boundaries and missing observations, dt columns, extras);
+    FEDM_HOST_MANIFOLD=1 builds them on host threads.  The saved manifolds
+    and the forecasts of the two must be the same bits."""
+    rng = np.random.default_rng(11)
+    if case == "panels_dt_missing_extras":
+        w = workloads.panel_config(n_panels=12, lo=40, hi=200)
+        t, x, y = w["t"], w["x"].copy(), None
+        x[rng.uniform(size=len(x)) < 0.03] = np.nan
+        kw = dict(panel=w["panel"], E=[2, 4], tau=2, dt=True, allowMissing=True, missingDistance=0.5,
+                  extras=[rng.normal(size=len(t)), rng.normal(size=len(t))], algorithm="smap", theta=[0.5, 2.0])
+    elif case == "reldt_p2_tau3":
+        t, x, _ = workloads.coupled_logistic(900, seed=6)
+        t = t.astype(float).copy()
+        t[7::40] += 0.5
+        y = None
+        kw = dict(E=3, tau=3, p=2, reldt=True, extras=[rng.normal(size=len(t))])
+    else:
+        t, x, y = workloads.coupled_logistic(900, seed=7)
+        kw = dict(E=3, p=-1, library=[100, 400], numReps=2, seed=3, copredict=np.roll(x, 5), savePredictions=True,
+                  saveCoPredictions=True)
+    kw["saveManifolds"] = True
+    out = {}
+    for mode in ("device", "host"):
+        if mode == "host":
+            monkeypatch.setenv("FEDM_HOST_MANIFOLD", "1")
+        else:
+            monkeypatch.delenv("FEDM_HOST_MANIFOLD", raising=False)
+        c = fedm.Context(0, precision=fedm.PRECISION_MIXED)
+        try:
+            out[mode] = fedm.edm(t, x, y, ctx=c, **kw)
+        finally:
+            c.close()
+    d, h = out["device"], out["host"]
+    assert d["rc"] == h["rc"] == 0 and len(d["Ms"]) == len(h["Ms"]) > 0
+    for f in range(len(d["Ms"])):
+        for a, b in ((d["Ms"][f], h["Ms"][f]), (d["Mps"][f], h["Mps"][f])):
+            assert a.shape == b.shape and np.array_equal(a, b, equal_nan=True), (case, f)
+    assert np.array_equal(np.asarray(d["stats"]["rho"]), np.asarray(h["stats"]["rho"]), equal_nan=True)
+    for key in ("predictions", "copredictions"):
+        if d.get(key) is not None:
+            assert np.array_equal(np.asarray(d[key], float), np.asarray(h[key], float), equal_nan=True)
+
+
 def test_easy_edm_call_sequence(ctx):
     """The edm() calls easy_edm() makes (R/easy_edm.R:160-410), in order, on a
     coupled logistic pair: explore E = 3..10; an S-map theta sweep with
