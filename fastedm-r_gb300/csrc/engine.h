@@ -43,6 +43,7 @@ public:
   // Order of the mixed kernels' work items: 1 (default) largest and
   // smallest library alternately, so that scan-heavy and solve-heavy items
   // share the SMs; 0 largest first (FEDM_ITEM_ORDER=interleave|lpt).
+  // Per-panel sub-tasks (independent panels) always go largest first.
   int item_order = 1;
   // Manifolds built on host threads and uploaded (FEDM_HOST_MANIFOLD=1)
   // instead of on the device; the same bits.
@@ -50,7 +51,8 @@ public:
   // Lane order of the one-point mixed kernels: 1 (default) points of a work
   // item in Morton order of their first four manifold coordinates (three
   // when E_a < 4), 2 of their first three, 0 list order
-  // (FEDM_POINT_ORDER=morton|morton3|list).  Results do not depend on it.
+  // (FEDM_POINT_ORDER=morton|morton3|list); per-panel sub-tasks keep list
+  // order.  Results do not depend on it.
   int point_order = 1;
   // the lane orders computed during the current call, by (list, first row,
   // rows, manifold): a CCM call's batches share its prediction list
