@@ -71,6 +71,124 @@ struct Rot
   double c, s;
 };
 
+// True for 2^27 <= |a| < 2^511.  There, evaluated in double,
+// sqrt(1 + a*a) is |a| exactly: a*a >= 2^54 has an ulp of at least 4, so
+// adding 1 rounds back to a*a; and the square root of a correctly rounded
+// square rounds to |a|, because the square's relative rounding error (at
+// most 2^-53) moves its square root by less than half an ulp of |a|.  The
+// upper bound keeps a*a finite.  Checked against the plain evaluation on
+// 10^8 random values over the whole range.
+__device__ __forceinline__ bool hypot_is_abs(double a)
+{
+  const unsigned e = ((unsigned)__double2hiint(a) >> 20) & 0x7ffu;
+  return e - (1023u + 27u) <= 483u;
+}
+
+// True when every lane of the warp that runs this call together (its
+// coalesced threads, as cooperative_groups::coalesced_threads() forms them)
+// passes c.  The FP64 pipe takes a warp instruction in the same time however
+// many of its lanes are active, so a shortcut pays only when the whole
+// group takes it; lanes that could take it run the full sequence, whose
+// results are the same.
+__device__ __forceinline__ bool all_lanes(bool c)
+{
+  return __all_sync(__activemask(), c) != 0;
+}
+
+// Eigen's real_2x2_jacobi_svd on the block [m00 m01; m10 m11]: the left
+// rotation jl and the right rotation jr (as Eigen's JacobiRotation c, s).
+// ops counts the FP64 operations of the reference's sequence.
+//
+// Shortcuts that return the reference's values:
+//  - a symmetric block (|m10 - m01| < DBL_MIN) takes the identity as its
+//    first rotation, whose products return m00, m01, m11 and make
+//    jl = jr^T;
+//  - for 2^27 <= |u| < 2^511, tmp = sqrt(1 + u^2) is |u| (hypot_is_abs),
+//    so the first rotation is c = u/|u| = +-1, s = 1/|u|;
+//  - for 2^27 <= |tau| < 2^511, w = sqrt(tau^2 + 1) is |tau|, tau +- w is
+//    2 tau (exact), t = 1/(2 tau), and t^2 <= 2^-56 makes 1 + t^2 round
+//    to 1, so n = 1/sqrt(1 + t^2) = 1 and the rotation is c = 1, s = +-|t|.
+// Both large cases are the rule in later sweeps, where the block is nearly
+// symmetric (|u| ~ 1/epsilon) and nearly diagonal (large |tau|); a warp
+// takes them when all of its lanes at the call qualify (all_lanes).  Where the
+// shortcut's result is a zero, only its sign can differ from the
+// reference's; the signs of zeros in the work matrix and the accumulators
+// reach no output of the solve (every sum there starts from +0).
+__device__ __forceinline__ void jacobi_2x2_vals(double m00, double m01, double m10, double m11, double& jlc,
+                                                double& jls, double& jrc, double& jrs, int& ops)
+{
+  const double tiny = DBL_MIN;
+  ops += 18;
+  double r1c, r1s, n00, n01, n11;
+  bool r1_id = false, r1_unit = false;
+  const double d = sub(m10, m01);
+  if (fabs(d) < tiny) {
+    r1c = 1;
+    r1s = 0;
+    r1_id = true;
+    n00 = m00;
+    n01 = m01;
+    n11 = m11;
+  } else {
+    const double t = add(m00, m11);
+    const double u = dvd(t, d);
+    ops += 6;
+    if (all_lanes(hypot_is_abs(u))) {
+      // c = u / |u| = +-1: its products are exact sign changes
+      r1s = rcp(fabs(u));
+      r1c = u < 0 ? -1.0 : 1.0;
+      r1_unit = true;
+      const bool cn = u < 0;
+      n00 = add(cn ? -m00 : m00, mul(r1s, m10));
+      n01 = add(cn ? -m01 : m01, mul(r1s, m11));
+      n11 = add(mul(-r1s, m01), cn ? -m11 : m11);
+    } else {
+      const double tmp = __dsqrt_rn(add(1.0, mul(u, u)));
+      r1s = rcp(tmp);
+      r1c = dvd_r(u, tmp, r1s);
+      n00 = add(mul(r1c, m00), mul(r1s, m10));
+      n01 = add(mul(r1c, m01), mul(r1s, m11));
+      n11 = add(mul(-r1s, m01), mul(r1c, m11));
+    }
+  }
+  const double deno = mul(2.0, fabs(n01));
+  if (deno < tiny) {
+    jrc = 1;
+    jrs = 0;
+  } else {
+    const double tau = dvd(sub(n00, n11), deno);
+    ops += 12;
+    // Eigen forms -sign_t * (n01 / |n01|) * |tt| * nn left to right; the
+    // first two products are exact sign changes (n01 is finite and nonzero
+    // here), so only the last multiply rounds.
+    if (all_lanes(hypot_is_abs(tau))) {
+      const double tt = rcp(mul(2.0, tau));
+      const bool neg = (tt > 0) == (n01 > 0);
+      jrs = neg ? -fabs(tt) : fabs(tt);
+      jrc = 1.0;
+    } else {
+      const double w = __dsqrt_rn(add(mul(tau, tau), 1.0));
+      const double tt = rcp(tau > 0 ? add(tau, w) : sub(tau, w));
+      const double nn = rcp(__dsqrt_rn(add(mul(tt, tt), 1.0)));
+      const bool neg = (tt > 0) == (n01 > 0);
+      jrs = mul(neg ? -fabs(tt) : fabs(tt), nn);
+      jrc = nn;
+    }
+  }
+  const double jtc = jrc, jts = -jrs;
+  if (r1_id) {
+    jlc = jtc;
+    jls = jts;
+  } else if (r1_unit) {
+    const bool cn = r1c < 0;
+    jlc = sub(cn ? -jtc : jtc, mul(r1s, jts));
+    jls = add(cn ? -jts : jts, mul(r1s, jtc));
+  } else {
+    jlc = sub(mul(r1c, jtc), mul(r1s, jts));
+    jls = add(mul(r1c, jts), mul(r1s, jtc));
+  }
+}
+
 // rows p, q <- J [row p; row q], J = [c s; -s c]
 __device__ __forceinline__ void rot_rows(double* A, int n, int p, int q, Rot j)
 {
@@ -92,70 +210,74 @@ __device__ __forceinline__ void rot_cols(double* A, int n, int p, int q, Rot j)
   }
 }
 
-// ops counts the FP64 add/sub/mul/div/sqrt operations performed.
-__device__ inline void jacobi_2x2(const double* W, int n, int p, int q, Rot& jl, Rot& jr, int& ops)
+// ops counts the FP64 add/sub/mul/div/sqrt operations of the reference's
+// sequence.
+__device__ __forceinline__ void jacobi_2x2(const double* W, int n, int p, int q, Rot& jl, Rot& jr, int& ops)
 {
-  ops += 18;
-  const double tiny = DBL_MIN;
-  const double m00 = W[p * n + p], m01 = W[p * n + q], m10 = W[q * n + p], m11 = W[q * n + q];
-  Rot r1;
-  const double t = add(m00, m11), d = sub(m10, m01);
-  if (fabs(d) < tiny) {
-    r1.s = 0;
-    r1.c = 1;
+  jacobi_2x2_vals(W[p * n + p], W[p * n + q], W[q * n + p], W[q * n + q], jl.c, jl.s, jr.c, jr.s, ops);
+}
+
+// Columns p, q of a rotation accumulator (U or V, started as the identity)
+// <- [col p, col q] [c -s; s c], in the first sweep.  Before the first
+// sweep's rotation (p, q) column q can be nonzero only in rows < p, and
+// column p only in row p (q = 0) or rows <= p (q > 0): rotations come in
+// the order (1,0), (2,0), (2,1), (3,0), ... and each leaves both of its
+// columns nonzero in the union of their rows.  A lane that skipped an
+// earlier rotation has fewer nonzero rows, never more.  Products by those
+// zeros are left out: c*x + s*0 is c*x for nonzero c*x, and a zero's sign
+// reaches no output of the solve.
+__device__ __forceinline__ void rot_cols_first(double* A, int n, int p, int q, double c, double s)
+{
+  if (q > 0) {
+    for (int i = 0; i < p; i++) {
+      const double x = A[i * n + p], y = A[i * n + q];
+      A[i * n + p] = add(mul(c, x), mul(s, y));
+      A[i * n + q] = add(mul(-s, x), mul(c, y));
+    }
   } else {
-    const double u = dvd(t, d);
-    const double tmp = __dsqrt_rn(add(1.0, mul(u, u)));
-    r1.s = rcp(tmp);
-    r1.c = dvd_r(u, tmp, r1.s);
-    ops += 6;
+    for (int i = 0; i < p; i++) {
+      const double y = A[i * n + q];
+      A[i * n + p] = mul(s, y);
+      A[i * n + q] = mul(c, y);
+    }
   }
-  const double n00 = add(mul(r1.c, m00), mul(r1.s, m10));
-  const double n01 = add(mul(r1.c, m01), mul(r1.s, m11));
-  const double n11 = add(mul(-r1.s, m01), mul(r1.c, m11));
-  const double deno = mul(2.0, fabs(n01));
-  if (deno < tiny) {
-    jr.c = 1;
-    jr.s = 0;
-  } else {
-    const double tau = dvd(sub(n00, n11), deno);
-    const double w = __dsqrt_rn(add(mul(tau, tau), 1.0));
-    const double tt = rcp(tau > 0 ? add(tau, w) : sub(tau, w));
-    const double sign_t = tt > 0 ? 1.0 : -1.0;
-    const double nn = rcp(__dsqrt_rn(add(mul(tt, tt), 1.0)));
-    // Eigen forms -sign_t * (n01 / |n01|) * |tt| * nn left to right; the
-    // first two products are exact sign changes (n01 is finite and nonzero
-    // here), so only the last multiply rounds.
-    const bool neg = (sign_t > 0) == (n01 > 0);
-    jr.s = mul(neg ? -fabs(tt) : fabs(tt), nn);
-    jr.c = nn;
-    ops += 12;
-  }
-  const double jtc = jr.c, jts = -jr.s;
-  jl.c = sub(mul(r1.c, jtc), mul(r1.s, jts));
-  jl.s = add(mul(r1.c, jts), mul(r1.s, jtc));
+  const double x = A[p * n + p];
+  A[p * n + p] = mul(c, x);
+  A[p * n + q] = mul(-s, x);
 }
 
 // Solves A x = b in the pseudo-inverse sense.  W holds A (n x n, destroyed);
 // U, V: n*n scratch; sv, tmp: n scratch.  ops accumulates the number of FP64
-// add/sub/mul/div/sqrt operations performed (the solve's algorithmic work).
+// add/sub/mul/div/sqrt operations of the reference's sequence (the solve's
+// algorithmic work); the exact shortcuts of jacobi_2x2_vals and
+// rot_cols_first leave some of them out without changing a result.
 __device__ inline void svd_solve(double* W, double* U, double* V, double* sv, double* tmp, const double* b, double* x,
                                  int n, int& ops)
 {
   const double tiny = DBL_MIN, eps = DBL_EPSILON;
-  double scale = 0;
+  // scale = max |W_ij| (fmax over the entries from 0, so a NaN never wins),
+  // taken on the magnitudes' bit patterns
+  long long smax = 0;
   for (int i = 0; i < n * n; i++)
-    scale = fmax(scale, fabs(W[i]));
-  if (!isfinite(scale)) {
+    smax = max(smax, mag_bits(W[i]));
+  if (smax >= 0x7ff0000000000000LL) {
     for (int i = 0; i < n; i++)
       x[i] = 0;
     return;
   }
-  if (scale == 0)
-    scale = 1;
+  const double scale = smax == 0 ? 1.0 : __longlong_as_double(smax);
   const double yscale = rcp(scale);
+  // W / scale; the two entries of a symmetric pair have the same quotient
+  for (int i = 0; i < n; i++) {
+    W[i * n + i] = dvd_r(W[i * n + i], scale, yscale);
+    for (int j = i + 1; j < n; j++) {
+      const double a = W[i * n + j], b = W[j * n + i];
+      const double qa = dvd_r(a, scale, yscale);
+      W[i * n + j] = qa;
+      W[j * n + i] = __double_as_longlong(a) == __double_as_longlong(b) ? qa : dvd_r(b, scale, yscale);
+    }
+  }
   for (int i = 0; i < n * n; i++) {
-    W[i] = dvd_r(W[i], scale, yscale);
     U[i] = 0;
     V[i] = 0;
   }
@@ -180,9 +302,14 @@ __device__ inline void svd_solve(double* W, double* U, double* V, double* sv, do
           jacobi_2x2(W, n, p, q, jl, jr, ops);
           ops += 24 * n;
           rot_rows(W, n, p, q, jl);
-          rot_cols(U, n, p, q, Rot{ jl.c, -jl.s });
           rot_cols(W, n, p, q, jr);
-          rot_cols(V, n, p, q, jr);
+          if (sweeps == 1) {
+            rot_cols_first(U, n, p, q, jl.c, jl.s);
+            rot_cols_first(V, n, p, q, jr.c, -jr.s);
+          } else {
+            rot_cols(U, n, p, q, Rot{ jl.c, -jl.s });
+            rot_cols(V, n, p, q, jr);
+          }
           maxDiag = max(maxDiag, max(mag_bits(W[p * n + p]), mag_bits(W[q * n + q])));
         }
       }

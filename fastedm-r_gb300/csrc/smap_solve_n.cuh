@@ -23,33 +23,80 @@ struct StridedMat
   __device__ __forceinline__ double& operator()(int i, int j) const { return base[(i * N + j) * stride]; }
 };
 
-// ops accumulates the FP64 add/sub/mul/div/sqrt operations performed, with
-// the same rules as svd_solve.
+// Columns p, q of the accumulator M <- [col p, col q] [c -s; s c].
+template<int N, class M>
+__device__ __forceinline__ void rot_cols_m(const M& A, int p, int q, double c, double s)
+{
+#pragma unroll
+  for (int i = 0; i < N; i++) {
+    const double xv = A(i, p), yv = A(i, q);
+    A(i, p) = add(mul(c, xv), mul(s, yv));
+    A(i, q) = add(mul(-s, xv), mul(c, yv));
+  }
+}
+
+// The same rotation in the first sweep, skipping the rows that are still
+// zero (the rule of rot_cols_first in smap_solve.cuh).
+template<int N, class M>
+__device__ __forceinline__ void rot_cols_first_m(const M& A, int p, int q, double c, double s)
+{
+#pragma unroll
+  for (int i = 0; i < N; i++) {
+    if (i < p) {
+      if (q > 0) {
+        const double xv = A(i, p), yv = A(i, q);
+        A(i, p) = add(mul(c, xv), mul(s, yv));
+        A(i, q) = add(mul(-s, xv), mul(c, yv));
+      } else {
+        const double yv = A(i, q);
+        A(i, p) = mul(s, yv);
+        A(i, q) = mul(c, yv);
+      }
+    } else if (i == p) {
+      const double xv = A(p, p);
+      A(p, p) = mul(c, xv);
+      A(p, q) = mul(-s, xv);
+    }
+  }
+}
+
+// ops accumulates the FP64 add/sub/mul/div/sqrt operations of the
+// reference's sequence, with the same rules as svd_solve.
 template<int N, class M, class MV>
 __device__ __forceinline__ void svd_solve_nm(double (&W)[N][N], const double (&b)[N], double (&x)[N], const M& U,
                                              const MV& V, int& ops)
 {
   const double tiny = DBL_MIN, eps = DBL_EPSILON;
-  double scale = 0;
+  // scale = max |W_ij|, on the magnitudes' bit patterns (as svd_solve)
+  long long smax = 0;
 #pragma unroll
   for (int i = 0; i < N; i++)
 #pragma unroll
     for (int j = 0; j < N; j++)
-      scale = fmax(scale, fabs(W[i][j]));
-  if (!isfinite(scale)) {
+      smax = max(smax, mag_bits(W[i][j]));
+  if (smax >= 0x7ff0000000000000LL) {
 #pragma unroll
     for (int i = 0; i < N; i++)
       x[i] = 0;
     return;
   }
-  if (scale == 0)
-    scale = 1;
+  const double scale = smax == 0 ? 1.0 : __longlong_as_double(smax);
   const double yscale = rcp(scale);
+#pragma unroll
+  for (int i = 0; i < N; i++) {
+    W[i][i] = dvd_r(W[i][i], scale, yscale);
+#pragma unroll
+    for (int j = i + 1; j < N; j++) {
+      const double a = W[i][j], b = W[j][i];
+      const double qa = dvd_r(a, scale, yscale);
+      W[i][j] = qa;
+      W[j][i] = __double_as_longlong(a) == __double_as_longlong(b) ? qa : dvd_r(b, scale, yscale);
+    }
+  }
 #pragma unroll
   for (int i = 0; i < N; i++)
 #pragma unroll
     for (int j = 0; j < N; j++) {
-      W[i][j] = dvd_r(W[i][j], scale, yscale);
       U(i, j) = i == j ? 1.0 : 0.0;
       V(i, j) = i == j ? 1.0 : 0.0;
     }
@@ -71,44 +118,10 @@ __device__ __forceinline__ void svd_solve_nm(double (&W)[N][N], const double (&b
         const long long threshold = jacobi_threshold_bits(maxDiag);
         if (mag_bits(W[p][q]) > threshold || mag_bits(W[q][p]) > threshold) {
           finished = false;
-          ops += 18 + 24 * N;
+          ops += 24 * N;
           // real_2x2_jacobi_svd on rows/cols p, q
-          const double m00 = W[p][p], m01 = W[p][q], m10 = W[q][p], m11 = W[q][q];
-          double r1c, r1s;
-          const double t = add(m00, m11), d = sub(m10, m01);
-          if (fabs(d) < tiny) {
-            r1s = 0;
-            r1c = 1;
-          } else {
-            const double u = dvd(t, d);
-            const double tmp = __dsqrt_rn(add(1.0, mul(u, u)));
-            r1s = rcp(tmp);
-            r1c = dvd_r(u, tmp, r1s);
-            ops += 6;
-          }
-          const double n00 = add(mul(r1c, m00), mul(r1s, m10));
-          const double n01 = add(mul(r1c, m01), mul(r1s, m11));
-          const double n11 = add(mul(-r1s, m01), mul(r1c, m11));
-          const double deno = mul(2.0, fabs(n01));
-          double jrc, jrs;
-          if (deno < tiny) {
-            jrc = 1;
-            jrs = 0;
-          } else {
-            const double tau = dvd(sub(n00, n11), deno);
-            const double w = __dsqrt_rn(add(mul(tau, tau), 1.0));
-            const double tt = rcp(tau > 0 ? add(tau, w) : sub(tau, w));
-            const double sign_t = tt > 0 ? 1.0 : -1.0;
-            const double nn = rcp(__dsqrt_rn(add(mul(tt, tt), 1.0)));
-            // -sign_t * (n01 / |n01|) * |tt| is an exact sign change
-            const bool neg = (sign_t > 0) == (n01 > 0);
-            jrs = mul(neg ? -fabs(tt) : fabs(tt), nn);
-            jrc = nn;
-            ops += 12;
-          }
-          const double jtc = jrc, jts = -jrs;
-          const double jlc = sub(mul(r1c, jtc), mul(r1s, jts));
-          const double jls = add(mul(r1c, jts), mul(r1s, jtc));
+          double jlc, jls, jrc, jrs;
+          jacobi_2x2_vals(W[p][p], W[p][q], W[q][p], W[q][q], jlc, jls, jrc, jrs, ops);
           // W.applyOnTheLeft(p, q, jl)
 #pragma unroll
           for (int i = 0; i < N; i++) {
@@ -116,17 +129,7 @@ __device__ __forceinline__ void svd_solve_nm(double (&W)[N][N], const double (&b
             W[p][i] = add(mul(jlc, xv), mul(jls, yv));
             W[q][i] = add(mul(-jls, xv), mul(jlc, yv));
           }
-          // U.applyOnTheRight(p, q, jl^T): rotation (c, -s) applied transposed
-          {
-            const double c = jlc, s = jls;  // transpose of (jlc, -jls)
-#pragma unroll
-            for (int i = 0; i < N; i++) {
-              const double xv = U(i, p), yv = U(i, q);
-              U(i, p) = add(mul(c, xv), mul(s, yv));
-              U(i, q) = add(mul(-s, xv), mul(c, yv));
-            }
-          }
-          // W.applyOnTheRight(p, q, jr) and V.applyOnTheRight(p, q, jr)
+          // W.applyOnTheRight(p, q, jr)
           {
             const double c = jrc, s = -jrs;
 #pragma unroll
@@ -135,12 +138,16 @@ __device__ __forceinline__ void svd_solve_nm(double (&W)[N][N], const double (&b
               W[i][p] = add(mul(c, xv), mul(s, yv));
               W[i][q] = add(mul(-s, xv), mul(c, yv));
             }
-#pragma unroll
-            for (int i = 0; i < N; i++) {
-              const double xv = V(i, p), yv = V(i, q);
-              V(i, p) = add(mul(c, xv), mul(s, yv));
-              V(i, q) = add(mul(-s, xv), mul(c, yv));
-            }
+          }
+          // U.applyOnTheRight(p, q, jl^T) and V.applyOnTheRight(p, q, jr):
+          // column rotations by (c, s) = (jlc, jls) and (jrc, -jrs); in the
+          // first sweep only the rows that can be nonzero (rot_cols_first)
+          if (sweeps == 1) {
+            rot_cols_first_m<N>(U, p, q, jlc, jls);
+            rot_cols_first_m<N>(V, p, q, jrc, -jrs);
+          } else {
+            rot_cols_m<N>(U, p, q, jlc, jls);
+            rot_cols_m<N>(V, p, q, jrc, -jrs);
           }
           maxDiag = max(maxDiag, max(mag_bits(W[p][p]), mag_bits(W[q][q])));
         }
