@@ -616,7 +616,45 @@ def config_steps(fedm, workloads, ctx, name):
             edm_oracle.smap_grad(lib, lib_t, pred[:n], pred_t[:n], 1.0, np.ones(6))
             return n, time.perf_counter() - t0, f"the first {n} prediction points, forward and backward, 1 thread"
         return {"workload": "lorenz_smap_grad_kall_lib50000_pred20000_E6_tau5", "T": 100000}, step, cpu
+    if name == "wasserstein":
+        # the Wasserstein distance (src/distances.cpp:270-527) through the
+        # task seam: a coupled logistic series, E = 5 (5 x 5 transport
+        # problems), library the first 2 000 rows, predictions the last
+        # 2 000; simplex k = 6 and S-map k = 7
+        t, x, _ = workloads.coupled_logistic(4000, seed=61)
+        E = 5
+        lib = np.zeros(4000, bool)
+        lib[:2000] = True
+        pred = ~lib
+        calls = [(fedm.normalise(t, x, E=E, theta=1.0), E + 1),
+                 (fedm.normalise(t, x, E=E, theta=1.0, algorithm="smap"), E + 2)]
+
+        def step():
+            out = []
+            for a_, k in calls:
+                t0 = time.perf_counter()
+                ctx.run_task(a_, lib, pred, E, k, distance=2)
+                out.append((ctx.timing(), time.perf_counter() - t0))
+            return out
+
+        def cpu(stride=1):
+            sub_pred = np.zeros_like(pred)
+            sub_pred[np.flatnonzero(pred)[::stride]] = True
+            t0 = time.perf_counter()
+            n = 0
+            for alg, k in (("simplex", E + 1), ("smap", E + 2)):
+                o = edm_oracle.oracle_task(edm_oracle.normalise(t, x, E=E, theta=1.0, algorithm=alg,
+                                                                numThreads=cores), lib, sub_pred, E, k, distance=2)
+                n += o["n_pred"]
+            return n, time.perf_counter() - t0, ("every prediction row, both calls" if stride == 1 else
+                                                 f"every {stride}th prediction row, both calls")
+        return {"workload": "wasserstein_T4000_lib2000_pred2000_E5_simplex_k6+smap_k7", "T": 4000}, step, cpu
     raise ValueError(name)
+
+
+# FP64 instructions per (prediction, library) pair of the Wasserstein
+# neighbour kernel at E = 5 (ncu, profiles/knn_exact_kernel_wasserstein_E5.md)
+WASS_FP64_PER_PAIR = None
 
 
 def config_roofline(name, precision, steps_tm, peaks):
@@ -711,6 +749,24 @@ def config_roofline(name, precision, steps_tm, peaks):
                 "per_call_ms": [{"device": tm["device_ms"], "host": tm["host_ms"], "prep": tm["prep_ms"],
                                  "manifold": tm["manifold_ms"], "setup": tm["setup_ms"],
                                  "finish": tm["finish_ms"]} for tm in steps_tm]}
+    if name == "wasserstein":
+        # combinatorial work: the cost matrix (3 operations per entry) and the
+        # transport solver's shortest-path rounds; its FP64 instructions per
+        # (prediction, library) pair were counted once by ncu on this workload
+        # (sm__sass_thread_inst_executed_op_fp64_pred_on over the neighbour
+        # kernel's pairs) and are the work unit here
+        ms = tot("knn_kernel_ms")
+        pairs = tot("distance_pairs")
+        if WASS_FP64_PER_PAIR is None:
+            return None
+        ops = WASS_FP64_PER_PAIR * pairs
+        return {"kernel": "knn_exact_kernel<Wasserstein> (cost matrix + successive-shortest-path transport per pair)",
+                "bound": "fp64_simt", "achieved": ops / (ms * 1e-3) / 1e12, "peak": peaks["fp64_unfused"],
+                "unit": "TFLOP/s", "frac": ops / (ms * 1e-3) / 1e12 / peaks["fp64_unfused"], "traffic": None,
+                "kernel_ms_per_step": ms, "launches_per_step": tot("knn_launches"),
+                "pairs_per_s": pairs / (ms * 1e-3),
+                "work": f"{WASS_FP64_PER_PAIR} FP64 instructions per (prediction, library) pair (ncu count)",
+                "peak_source": "measured unfused FP64 multiply/add rate (fedm_measure_peak kind 3)"}
     if name == "adjoint":
         tm = steps_tm[0]
         ms = tm["knn_kernel_ms"]
@@ -844,7 +900,7 @@ def main():
                          "weights and double-float normal equations for the k = all S-map)")
     ap.add_argument("--workload", default="ccm",
                     choices=["ccm", "simplex_explore", "smap_sweep", "panels", "panels_independent",
-                             "panels_penalty", "adjoint", "easy_edm"],
+                             "panels_penalty", "adjoint", "easy_edm", "wasserstein"],
                     help="ccm (default): the headline CCM benchmark; the others time the other benchmark "
                          "configurations at full size")
     a = ap.parse_args()

@@ -84,6 +84,8 @@ Context::Context(int dev) : device(dev)
     item_order = std::strcmp(v, "lpt") == 0 ? 0 : 1;
   if (const char* v = std::getenv("FEDM_HOST_MANIFOLD"))
     host_manifold = std::strcmp(v, "1") == 0;
+  if (const char* v = std::getenv("FEDM_SERIES_CACHE"))
+    series_cache = std::strcmp(v, "0") != 0;
   if (const char* v = std::getenv("FEDM_POINT_ORDER"))
     point_order = std::strcmp(v, "list") == 0 ? 0 : (std::strcmp(v, "morton3") == 0 ? 2 : 1);
   reset_timing();
@@ -471,7 +473,21 @@ struct GroupJob
   // for lazily produced CCM lists); the mixed path's bounding box is then
   // taken over it once instead of over each list
   const std::vector<int>* lib_superset = nullptr;
+  // Wasserstein distance: the layout of a point (see GroupParams)
+  int w_E = 0, w_rows = 1, w_unlagged = 0;
+  bool w_dt = false;
 };
+
+// A point of E columns for the Wasserstein distance: the rows of the
+// reference's column-major view and the unlagged extras after it
+// (src/distances.cpp:316-320, 364-366).
+void set_wasserstein_shape(GroupJob& job, const Generator& g, int E)
+{
+  job.w_E = E;
+  job.w_dt = g.E_dt(E) > 0;
+  job.w_rows = 1 + (job.w_dt ? 1 : 0) + g.num_extras_lagged;
+  job.w_unlagged = g.num_extras - g.num_extras_lagged;
+}
 
 constexpr int KCAP_MAX = 16384;
 constexpr int MIX_KMAX = 14;        // neighbours the mixed kernel serves (slots C = 16)
@@ -827,6 +843,12 @@ void run_group(Context& ctx, const Options& o, const std::vector<Task>& tasks, c
   g.has_id_weights = o.has_id_weights;
   g.past_only = o.past_only && !o.low_memory;
   g.force_compute = o.force_compute;
+  g.wasserstein = o.distance == 2;
+  g.w_E = job.w_E;
+  g.w_rows = job.w_rows;
+  g.w_unlagged = job.w_unlagged;
+  g.w_dt = job.w_dt ? 1 : 0;
+  g.aspect_ratio = o.aspect_ratio;
   g.total_points = P;
   g.pred = (double*)ctx.buf("pred", (size_t)std::max<long long>(P, 1) * nth * 8);
   fill_f64(g.pred, P * nth, MISSING_D, s);
@@ -858,7 +880,7 @@ void run_group(Context& ctx, const Options& o, const std::vector<Task>& tasks, c
   // double-float arithmetic from a per-row table of products
   const float2* gram_terms = nullptr;
   if (ctx.precision == FEDM_PRECISION_FAST && any_all && o.algorithm == 1 && Ea <= 8 && !o.has_missing &&
-      !o.low_memory) {
+      !o.low_memory && o.distance == 1) {
     const long long pool = lib_total;
     const long long bytes = pool * gram_terms_per_row(Ea) * (long long)sizeof(float2);
     if (pool > 0 && bytes <= (2LL << 30)) {
@@ -1569,6 +1591,47 @@ struct Manifolds
   int *obs = nullptr, *target_row = nullptr;
 };
 
+template<class T>
+bool same_bits(const std::vector<T>& a, const std::vector<T>& b)
+{
+  return a.size() == b.size() && (a.empty() || std::memcmp(a.data(), b.data(), a.size() * sizeof(T)) == 0);
+}
+
+// Checks the context's record of the series behind its manifold buffers
+// against this call's manifold inputs (every array and setting that
+// manifold_kernel and the host build read), bit for bit.  When they differ
+// the record takes this call's inputs and forgets its manifolds.
+void sync_series(Context& ctx, const Generator& g, const RowTables& rt)
+{
+  auto& c = ctx.series;
+  if (!ctx.series_cache || ctx.host_manifold) {
+    c = Context::SeriesCache{};
+    return;
+  }
+  std::vector<double> scalars = { (double)g.n, (double)g.tau, g.dt ? 1.0 : 0.0, g.reldt ? 1.0 : 0.0, g.dt_weight,
+                                  (double)g.num_extras, (double)g.num_extras_lagged, g.panel_mode ? 1.0 : 0.0 };
+  std::vector<double> extras;
+  for (const auto& e : g.extras)
+    extras.insert(extras.end(), e.begin(), e.end());
+  static const std::vector<int> none;
+  const std::vector<int>& panel = g.panel_mode ? g.panel : none;
+  if (c.valid && same_bits(c.scalars, scalars) && same_bits(c.x, g.x) && same_bits(c.co_x, g.co_x) &&
+      same_bits(c.extras, extras) && same_bits(c.point_time, rt.point_time) && same_bits(c.obs, g.obs) &&
+      same_bits(c.target_row, rt.target_row) && same_bits(c.panel, panel))
+    return;
+  c.valid = true;
+  c.scalars = std::move(scalars);
+  c.x = g.x;
+  c.co_x = g.co_x;
+  c.extras = std::move(extras);
+  c.point_time = rt.point_time;
+  c.obs = g.obs;
+  c.target_row = rt.target_row;
+  c.panel = panel;
+  c.uploaded = false;
+  c.built.clear();
+}
+
 // The manifold for E (co: of co_x) on the device, built once per call.  By
 // default manifold_kernel builds it from the series and the host copy comes
 // back into a pinned buffer of the context; FEDM_HOST_MANIFOLD=1 builds it
@@ -1585,6 +1648,17 @@ double* device_manifold(Context& ctx, Manifolds& M, const Generator& g, const Ro
   const size_t count = (size_t)g.n * Ea;
   const std::string name = "F_" + std::to_string(E) + (co ? "_co" : "");
   double* d = (double*)ctx.buf(name, std::max<size_t>(count, 1) * 8);
+  if (ctx.series.valid && ctx.series.built.count(key)) {
+    // built by an earlier call on the same series: the buffers still hold
+    // it (only this function writes them, and the same size never
+    // reallocates)
+    M.host[key] = (const double*)ctx.host_buf("host_" + name, std::max<size_t>(count, 1) * 8);
+    M.dev[key] = d;
+    ctx.timing.manifolds_reused += 1;
+    ctx.timing.manifold_ms += now_ms() - t0;
+    return d;
+  }
+  ctx.timing.manifold_builds += 1;
   if (ctx.host_manifold) {
     auto& h = M.host_store[key];
     h = build_manifold(g, rt, E, co, threads);
@@ -1593,21 +1667,29 @@ double* device_manifold(Context& ctx, Manifolds& M, const Generator& g, const Ro
   } else {
     const size_t n = (size_t)g.n;
     if (!M.series) {
+      // uploaded once per series: a call on the series the buffers hold
+      // (ctx.series) skips the copies
+      const bool have = ctx.series.valid && ctx.series.uploaded;
       M.x = (double*)ctx.buf("series_x", n * 8);
-      ctx.upload(M.x, g.x.data(), n * 8);
+      if (!have)
+        ctx.upload(M.x, g.x.data(), n * 8);
       if (!g.co_x.empty()) {
         M.co_x = (double*)ctx.buf("series_co_x", n * 8);
-        ctx.upload(M.co_x, g.co_x.data(), n * 8);
+        if (!have)
+          ctx.upload(M.co_x, g.co_x.data(), n * 8);
       }
       if (g.num_extras > 0) {
         M.extras = (double*)ctx.buf("series_extras", (size_t)g.num_extras * n * 8);
-        for (int e = 0; e < g.num_extras; e++)
+        for (int e = 0; e < g.num_extras && !have; e++)
           ctx.upload(M.extras + (size_t)e * n, g.extras[e].data(), n * 8);
       }
       M.obs = (int*)ctx.buf("series_obs", n * 4);
-      ctx.upload(M.obs, g.obs.data(), n * 4);
       M.target_row = (int*)ctx.buf("series_target_row", n * 4);
-      ctx.upload(M.target_row, rt.target_row.data(), n * 4);
+      if (!have) {
+        ctx.upload(M.obs, g.obs.data(), n * 4);
+        ctx.upload(M.target_row, rt.target_row.data(), n * 4);
+      }
+      ctx.series.uploaded = ctx.series.valid;
       M.series = true;
     }
     ManifoldParams p{};
@@ -1634,6 +1716,8 @@ double* device_manifold(Context& ctx, Manifolds& M, const Generator& g, const Ro
     ctx.download(h, d, count * 8);
     ck(cudaStreamSynchronize(ctx.stream), "manifold download");
     M.host[key] = h;
+    if (ctx.series.valid)
+      ctx.series.built.insert(key);
   }
   M.dev[key] = d;
   ctx.timing.manifold_ms += now_ms() - t0;
@@ -1669,6 +1753,7 @@ CommandResult run_command(Context& ctx, const fedm_args& a)
   if (copredict_mode)
     cousable = gen.usable(maxE, true, threads);
   RowTables rt = build_row_tables(gen);
+  sync_series(ctx, gen, rt);
   // CCM library splits are left lazy: a SplitProducer computes their row
   // lists on background threads while the GPU runs earlier task batches
   TaskPlan plan = configure_tasks(gen, o, P.Es, libraries, a.k, a.num_reps, a.crossfold, P.explore, a.full,
@@ -2034,11 +2119,15 @@ int run_task(Context& ctx, const fedm_args& a, fedm_task_io& io)
   Prepared P;
   prepare(a, P);
   Options o = P.opts;
-  o.distance = io.distance == 0 ? 0 : 1;
+  o.distance = io.distance == 0 ? 0 : io.distance == 2 ? 2 : 1;
+  o.aspect_ratio = io.aspect_ratio;
   o.force_compute = io.force_compute != 0;
+  if (o.distance == 2 && (io.E < 1 || io.E > WASS_EMAX))
+    throw Error{ RC_NOT_IMPLEMENTED, "the Wasserstein distance takes 1 <= E <= 16" };
   const Generator& gen = P.gen;
   const int threads = host_threads(a);
   RowTables rt = build_row_tables(gen);
+  sync_series(ctx, gen, rt);
   std::vector<uint8_t> lm(io.library_rows, io.library_rows + a.n), pm(io.prediction_rows, io.prediction_rows + a.n);
   for (auto& v : lm)
     v = v ? 1 : 0;
@@ -2070,6 +2159,7 @@ int run_task(Context& ctx, const fedm_args& a, fedm_task_io& io)
     job.pred_lists = { &Pl };
     job.detail = true;
     job.knn_for_all = true;
+    set_wasserstein_shape(job, gen, io.E);
     run_group(ctx, o, tasks, drows, job, outs);
   }
   const TaskOut& to = outs[0];

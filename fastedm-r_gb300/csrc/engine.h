@@ -4,6 +4,7 @@
 
 #include <array>
 #include <map>
+#include <set>
 #include <string>
 #include <tuple>
 #include <vector>
@@ -48,6 +49,21 @@ public:
   // Manifolds built on host threads and uploaded (FEDM_HOST_MANIFOLD=1)
   // instead of on the device; the same bits.
   bool host_manifold = false;
+  // The series behind the manifolds now held in the context's buffers (the
+  // device manifolds F_E, their pinned host copies and the uploaded series).
+  // A later call whose manifold inputs are the same bits -- easy_edm()'s
+  // sequence of edm() calls on one series -- takes those manifolds instead
+  // of uploading the series and building them again; a call on another
+  // series replaces the record.  FEDM_SERIES_CACHE=0 turns it off.
+  struct SeriesCache
+  {
+    bool valid = false;
+    std::vector<double> scalars, x, co_x, extras, point_time;
+    std::vector<int> obs, target_row, panel;
+    bool uploaded = false;                   // the series_* buffers hold it
+    std::set<std::pair<int, bool>> built;    // (E, co_x) manifolds built from it
+  } series;
+  bool series_cache = true;
   // Lane order of the one-point mixed kernels: 1 (default) points of a work
   // item in Morton order of their first four manifold coordinates (three
   // when E_a < 4), 2 of their first three, 0 list order

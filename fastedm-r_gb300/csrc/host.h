@@ -134,7 +134,8 @@ private:
 struct Options
 {
   int algorithm = 0;  // 0 simplex, 1 smap
-  int distance = 1;   // 0 L1 (mean absolute error), 1 L2
+  int distance = 1;   // 0 L1 (mean absolute error), 1 L2, 2 Wasserstein
+  double aspect_ratio = 0;  // Wasserstein with dt: weight of the time axis
   bool force_compute = true;
   double missing_distance = 0;
   bool has_missing = false;

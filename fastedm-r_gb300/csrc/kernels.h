@@ -36,6 +36,9 @@ struct DevTask
                          // (-1: slot order is list order)
 };
 
+// Largest E (columns of a point) the Wasserstein distance takes.
+constexpr int WASS_EMAX = 16;
+
 struct GroupParams
 {
   // inputs
@@ -68,6 +71,12 @@ struct GroupParams
   int has_id_weights;
   int past_only;
   int force_compute;
+  // Wasserstein distance (src/distances.cpp:270-527) instead of L1/L2: a
+  // point is read as a column-major w_rows x w_E matrix (w_rows = 1 + [dt]
+  // + lagged extras) followed by w_unlagged unlagged extras
+  int wasserstein;
+  int w_E, w_rows, w_unlagged, w_dt;
+  double aspect_ratio;
   long long total_points;  // size of the point space of the whole run
   // outputs
   double* pred;            // [n_thetas x total_points]

@@ -12,6 +12,7 @@
 #include "kernels.h"
 #include "exp_rn.cuh"
 #include "smap_solve.cuh"
+#include "wasserstein.cuh"
 
 namespace fedm {
 
@@ -33,13 +34,40 @@ __device__ __forceinline__ int find_task(const GroupParams& g, long long p)
   return lo;
 }
 
-// One reference distance (src/distances.cpp:160-226).  Returns false for
-// skipped or invalid pairs (zero or missing distance).
+// One reference distance (src/distances.cpp:160-226; with WASS the
+// Wasserstein distance, :488-527).  Returns false for skipped or invalid
+// pairs (zero or missing distance).  The Wasserstein form is a template
+// instance of its own, so the L1/L2 kernels keep their registers.
+template<bool WASS>
 __device__ __forceinline__ bool exact_distance(const GroupParams& g, int lrow, int prow, const double* y, int ppanel,
                                                double ptime, double& out)
 {
   if (g.skip_other_panels && g.panel[lrow] != ppanel)
     return false;
+  if constexpr (WASS) {
+    // src/distances.cpp:488-527: no past-only rule on this path; the panel
+    // term joins the unlagged distance
+    bool has_pen = false;
+    double pen = 0.0;
+    if (g.panel_mode && g.idw > 0) {
+      has_pen = true;
+      pen = g.idw * (double)(g.panel[lrow] != ppanel);
+    } else if (g.panel_mode && g.has_id_weights) {
+      float w = g.id_w[(size_t)g.panel_dense[lrow] * g.n_pid + g.panel_dense[prow]];
+      if (isnan(w)) {
+        atomicExch(g.err_flag, 1);  // the reference's map::at throws here
+        w = 0.f;
+      }
+      has_pen = true;
+      pen = (double)w;
+    }
+    int st = 0;
+    const bool ok = wasserstein_pair(g.F + (size_t)lrow * g.Ea, y, g.w_E, g.w_rows, g.w_unlagged, g.w_dt != 0,
+                                     g.aspect_ratio, g.missing_distance, has_pen, pen, out, st);
+    if (st)
+      atomicExch(g.err_flag, 1);
+    return ok;
+  }
   if (g.past_only && g.lib_target_time[lrow] > ptime)
     return false;
   double d = 0.0;
@@ -113,6 +141,7 @@ __device__ __forceinline__ void note_k(const GroupParams& g, int task, long long
 // pairs are kept sorted in shared memory; a library chunk of 32 is scored in
 // parallel and its candidates are inserted in index order, which realises
 // the reference's (distance asc, index asc) order (src/edm.cpp:652-681).
+template<bool WASS>
 __global__ void knn_exact_kernel(GroupParams g, ChunkBuffers c, int warps_per_block, int per_warp_bytes)
 {
   extern __shared__ __align__(16) unsigned char smem[];
@@ -147,7 +176,7 @@ __global__ void knn_exact_kernel(GroupParams g, ChunkBuffers c, int warps_per_bl
       double d = 0;
       bool valid = false;
       if (i < T.n_lib)
-        valid = exact_distance(g, g.lib_rows[T.lib_off + i], prow, sy, ppanel, ptime, d);
+        valid = exact_distance<WASS>(g, g.lib_rows[T.lib_off + i], prow, sy, ppanel, ptime, d);
       const unsigned vm = __ballot_sync(FULL, valid);
       if (valid) {
         const int slot = count + __popc(vm & ((1u << lane) - 1u));
@@ -164,7 +193,7 @@ __global__ void knn_exact_kernel(GroupParams g, ChunkBuffers c, int warps_per_bl
       double d = 0;
       bool valid = false;
       if (i < T.n_lib)
-        valid = exact_distance(g, g.lib_rows[T.lib_off + i], prow, sy, ppanel, ptime, d);
+        valid = exact_distance<WASS>(g, g.lib_rows[T.lib_off + i], prow, sy, ppanel, ptime, d);
       numValid += __popc(__ballot_sync(FULL, valid));
       const double thr = (k <= 0 || count < k) ? DBL_MAX : sD[k - 1];
       unsigned cm = __ballot_sync(FULL, valid && k > 0 && (count < k ? true : d < thr));
@@ -400,7 +429,7 @@ __global__ void __launch_bounds__(32 * REFINE_WARPS) knn_refine_kernel(GroupPara
         int nvalid = 0;
         for (int e = lane; e < count; e += 32) {
           double d = 0;
-          const bool valid = exact_distance(g, g.lib_rows[T.lib_off + sI[e]], prow, y, ppanel, ptime, d);
+          const bool valid = exact_distance<false>(g, g.lib_rows[T.lib_off + sI[e]], prow, y, ppanel, ptime, d);
           sD[e] = valid ? d : -1.0;
           nvalid += valid ? 1 : 0;
         }
@@ -604,6 +633,7 @@ __global__ void smap_nn_kernel(GroupParams g, ChunkBuffers c, long long slab)
 // its row of the chunk's distance buffer (-1 marks an invalid pair); then
 // one thread per (point, theta) reduces them sequentially in library order,
 // the order the reference's loops use, so the results are the same bits.
+template<bool WASS>
 __global__ void all_dist_kernel(GroupParams g, ChunkBuffers c, long long max_nlib, int per_warp_bytes)
 {
   extern __shared__ __align__(16) unsigned char smem[];
@@ -625,7 +655,7 @@ __global__ void all_dist_kernel(GroupParams g, ChunkBuffers c, long long max_nli
     int lcnt = 0;
     for (int i = lane; i < T.n_lib; i += 32) {
       double d;
-      const bool ok = exact_distance(g, g.lib_rows[T.lib_off + i], prow, sy, ppanel, ptime, d);
+      const bool ok = exact_distance<WASS>(g, g.lib_rows[T.lib_off + i], prow, sy, ppanel, ptime, d);
       dq[i] = ok ? d : -1.0;
       lcnt += ok;
     }
@@ -1094,8 +1124,9 @@ void launch_knn_exact(const GroupParams& g, const ChunkBuffers& c, int num_sms, 
   int per_warp;
   const int w = knn_warps_per_block(g.Ea, c.kcap, per_warp);
   const size_t smem = (size_t)w * per_warp;
+  auto kern = g.wasserstein ? knn_exact_kernel<true> : knn_exact_kernel<false>;
   if (smem > 48 * 1024)
-    cudaFuncSetAttribute(knn_exact_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   const long long chunk = c.p_end - c.p_begin;
   long long blocks = (chunk + w - 1) / w;
   const long long cap = (long long)num_sms * 64;
@@ -1103,7 +1134,7 @@ void launch_knn_exact(const GroupParams& g, const ChunkBuffers& c, int num_sms, 
     blocks = cap;
   if (blocks < 1)
     blocks = 1;
-  knn_exact_kernel<<<(int)blocks, 32 * w, smem, s>>>(g, c, w, per_warp);
+  kern<<<(int)blocks, 32 * w, smem, s>>>(g, c, w, per_warp);
 }
 
 template<int EA>
@@ -1277,7 +1308,10 @@ void launch_all_mode(const GroupParams& g, const ChunkBuffers& c, int num_sms, l
     blocks = (long long)num_sms * 64;
   if (blocks < 1)
     blocks = 1;
-  all_dist_kernel<<<(int)blocks, 32 * w, (size_t)w * per_warp, s>>>(g, c, max_nlib, per_warp);
+  if (g.wasserstein)
+    all_dist_kernel<true><<<(int)blocks, 32 * w, (size_t)w * per_warp, s>>>(g, c, max_nlib, per_warp);
+  else
+    all_dist_kernel<false><<<(int)blocks, 32 * w, (size_t)w * per_warp, s>>>(g, c, max_nlib, per_warp);
   if (chunk * g.n_thetas <= 0)
     return;
   if (ev0)

@@ -62,7 +62,7 @@ class TaskIO(C.Structure):
         ("n_pred", C.c_int), ("n_lib", C.c_int), ("e_actual", C.c_int), ("total_nn", C.c_int),
         ("predictions", C.c_void_p), ("coeffs", C.c_void_p), ("rc", C.c_void_p), ("kused", C.c_void_p),
         ("nn_offsets", C.c_void_p), ("nn_idx", C.c_void_p), ("nn_dist", C.c_void_p),
-        ("stats_rho", C.c_void_p), ("stats_mae", C.c_void_p),
+        ("stats_rho", C.c_void_p), ("stats_mae", C.c_void_p), ("aspect_ratio", C.c_double),
     ]
 
 
@@ -75,7 +75,8 @@ class Timing(C.Structure):
         ("setup_ms", C.c_double), ("finish_ms", C.c_double), ("exact_points", C.c_int),
         ("mixed_form", C.c_int), ("autotune_probes", C.c_int), ("prep_ms", C.c_double),
         ("manifold_ms", C.c_double), ("scan_flops", C.c_longlong), ("forecast_kernel_ms", C.c_double),
-        ("forecast_launches", C.c_int), ("tensor_core_tiles", C.c_int),
+        ("forecast_launches", C.c_int), ("tensor_core_tiles", C.c_int), ("manifold_builds", C.c_int),
+        ("manifolds_reused", C.c_int),
     ]
 
 
@@ -237,8 +238,11 @@ class Context:
             d["error"] = self.last_error()
         return d
 
-    def run_task(self, a, library_rows, prediction_rows, E, k, copredict=False, distance=1, force_compute=True):
-        """One task on explicit masks; neighbour lists included."""
+    def run_task(self, a, library_rows, prediction_rows, E, k, copredict=False, distance=1, force_compute=True,
+                 aspect_ratio=0.0):
+        """One task on explicit masks; neighbour lists included.  distance: 0
+        mean absolute error, 1 Euclidean, 2 Wasserstein (aspect_ratio weights
+        its time axis under dt)."""
         keep = []
         s = make_args(a, keep)
         lr = np.ascontiguousarray(np.asarray(library_rows, dtype=np.uint8))
@@ -246,6 +250,7 @@ class Context:
         io = TaskIO()
         io.library_rows, io.prediction_rows = lr.ctypes.data, pr.ctypes.data
         io.E, io.k, io.copredict, io.distance, io.force_compute = E, k, int(copredict), distance, int(force_compute)
+        io.aspect_ratio = float(aspect_ratio)
         rc = self.lib.fedm_run_task(self.h, C.byref(s), C.byref(io))
         if rc not in (0, 503, 8000) or (rc and io.n_pred == 0 and io.n_lib == 0):
             raise RuntimeError(f"fedm_run_task sizes rc={rc}: {self.last_error()}")

@@ -176,7 +176,10 @@ typedef struct fedm_task_io {
   int E;
   int k;
   int copredict;
-  int distance;       /* 0 mean absolute error (L1), 1 Euclidean (L2)      */
+  int distance;       /* 0 mean absolute error (L1), 1 Euclidean (L2),
+                         2 Wasserstein (src/distances.cpp:270-527; the
+                         reference's Distance enum, src/common.h:37-42;
+                         E <= 16)                                           */
   int force_compute;
   int n_pred, n_lib, e_actual, total_nn;
   double* predictions;
@@ -188,6 +191,8 @@ typedef struct fedm_task_io {
   double* nn_dist;
   double* stats_rho;
   double* stats_mae;
+  double aspect_ratio; /* Wasserstein with dt: Options::aspectRatio
+                          (src/distances.cpp:361), 0 as R sets it           */
 } fedm_task_io;
 
 int fedm_run_task(fedm_ctx* ctx, const fedm_args* args, fedm_task_io* io);
@@ -239,6 +244,10 @@ typedef struct fedm_timing {
   int forecast_launches;     /* their launches                               */
   int tensor_core_tiles;     /* FAST k = all S-map: 128-row tiles whose
                                 normal equations ran on the tensor cores     */
+  int manifold_builds;       /* manifolds built (and their series uploaded)
+                                by this call                                 */
+  int manifolds_reused;      /* manifolds taken from the context's buffers,
+                                built by an earlier call on the same series  */
 } fedm_timing;
 
 int fedm_last_timing(const fedm_ctx* ctx, fedm_timing* out);

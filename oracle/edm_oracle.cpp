@@ -50,7 +50,8 @@ enum class Algorithm
 enum class Distance
 {
   MeanAbsoluteError,
-  Euclidean
+  Euclidean,
+  Wasserstein
 };
 
 // Wrapping int addition: the reference adds offsets to MISSING_I observation
@@ -672,6 +673,7 @@ struct Options
   Algorithm algorithm = Algorithm::Simplex;
   int taskNum = 0, numTasks = 0, configNum = 0;
   Distance distance = Distance::Euclidean;
+  double aspectRatio = 0;
   bool lowMemoryMode = false, useOnlyPastToPredictFuture = false, hasMissing = false;
 };
 
@@ -721,6 +723,213 @@ DistanceIndexPairs lp_distances(int Mp_i, const Options& opts, const Manifold& M
     if (d != 0 && d != MISSING_D) {
       out.dists.push_back(l1 ? d : std::sqrt(d));
       out.inds.push_back(i);
+    }
+  }
+  return out;
+}
+
+// ------------------------------------------------ Wasserstein distance
+// src/distances.cpp:270-527.  The cost matrix is restated step by step; the
+// transport cost that the reference takes from EMD_wrap
+// (src/vendor/EMD_wrapper.h:34-117, POT's network simplex, vendored) is
+// computed here by an independent exact method: an optimal assignment by the
+// Hungarian method (Kuhn-Munkres with potentials, O(N^3)), directly for equal
+// lengths n (flows 1/n) and, for unequal lengths, on the problem with every
+// source repeated len_j times and every sink len_i times (flows in units of
+// 1/(len_i len_j)).  EMD_wrap sums flow * cost over the arcs from the last
+// (i = n1-1, j = n2-1) to the first; the same sum is formed here.  For equal
+// lengths and a unique optimal plan that reproduces EMD_wrap's bits (its
+// network simplex carries the flows 1/n exactly).  Where several plans are
+// optimal the two solvers may return different ones, whose sums differ in
+// the last bits; for unequal lengths EMD_wrap's flows carry roundings of
+// their own, a few ulps from the exact fractions.
+
+// Minimum-cost perfect assignment of an N x N cost matrix (row-major);
+// returns the column of each row.
+std::vector<int> hungarian(const std::vector<double>& cost, int N)
+{
+  const long double INF = std::numeric_limits<long double>::infinity();
+  std::vector<long double> u(N + 1, 0), v(N + 1, 0), minv(N + 1);
+  std::vector<int> p(N + 1, 0), way(N + 1, 0);
+  std::vector<char> used(N + 1);
+  for (int i = 1; i <= N; i++) {
+    p[0] = i;
+    int j0 = 0;
+    std::fill(minv.begin(), minv.end(), INF);
+    std::fill(used.begin(), used.end(), 0);
+    do {
+      used[j0] = 1;
+      const int i0 = p[j0];
+      long double delta = INF;
+      int j1 = 0;
+      for (int j = 1; j <= N; j++)
+        if (!used[j]) {
+          const long double cur = (long double)cost[(size_t)(i0 - 1) * N + (j - 1)] - u[i0] - v[j];
+          if (cur < minv[j]) {
+            minv[j] = cur;
+            way[j] = j0;
+          }
+          if (minv[j] < delta) {
+            delta = minv[j];
+            j1 = j;
+          }
+        }
+      for (int j = 0; j <= N; j++)
+        if (used[j]) {
+          u[p[j]] += delta;
+          v[j] -= delta;
+        } else {
+          minv[j] -= delta;
+        }
+      j0 = j1;
+    } while (p[j0] != 0);
+    do {
+      const int j1 = way[j0];
+      p[j0] = p[j1];
+      j0 = j1;
+    } while (j0);
+  }
+  std::vector<int> col(N);
+  for (int j = 1; j <= N; j++)
+    col[p[j] - 1] = j - 1;
+  return col;
+}
+
+// Transport cost of the n1 x n2 row-major cost matrix D with masses 1/n1
+// and 1/n2 (src/distances.cpp:455-470 calling EMD_wrap).
+double emd_uniform(const double* D, int n1, int n2)
+{
+  std::vector<long long> f((size_t)n1 * n2, 0);
+  long long L;
+  if (n1 == n2) {
+    std::vector<double> c(D, D + (size_t)n1 * n2);
+    const std::vector<int> col = hungarian(c, n1);
+    for (int i = 0; i < n1; i++)
+      f[(size_t)i * n2 + col[i]] = 1;
+    L = n1;
+  } else {
+    const int N = n1 * n2;  // source i repeated n2 times, sink j n1 times
+    std::vector<double> c((size_t)N * N);
+    for (int a = 0; a < N; a++)
+      for (int b = 0; b < N; b++)
+        c[(size_t)a * N + b] = D[(size_t)(a / n2) * n2 + (b / n1)];
+    const std::vector<int> col = hungarian(c, N);
+    for (int a = 0; a < N; a++)
+      f[(size_t)(a / n2) * n2 + col[a] / n1] += 1;
+    L = N;
+  }
+  double cost = 0;
+  for (long long a = (long long)n1 * n2 - 1; a >= 0; a--) {
+    const double flow = (double)f[a] / (double)L;
+    cost += flow * D[a];
+  }
+  return cost;
+}
+
+// src/distances.cpp:296-411: the cost matrix between library point i of M
+// and prediction point j of Mp.  The reference maps each point's leading
+// rows * E values as a column-major rows x E matrix (rows = 1 + [dt] +
+// lagged extras), the unlagged extras after it.
+std::vector<double> wasserstein_cost_matrix(const Manifold& M, const Manifold& Mp, int i, int j, const Options& opts,
+                                            int& len_i, int& len_j)
+{
+  const Generator& g = *M.gen;
+  const int E = M.E_x;
+  const bool skipMissing = opts.missingdistance == 0;
+  const int rows = 1 + (g.E_dt(E) > 0 ? 1 : 0) + g.num_extras_lagged;
+  const double* x = &M.flat[(size_t)i * M.E_actual];
+  const double* y = &Mp.flat[(size_t)j * Mp.E_actual];
+  auto at = [&](const double* v, int r, int c) { return v[(size_t)c * rows + r]; };
+  std::vector<bool> xm(E, false), ym(E, false);
+  for (int c = 0; c < E; c++)
+    for (int r = 0; r < rows; r++) {
+      if (at(x, r, c) == MISSING_D)
+        xm[c] = true;
+      if (at(y, r, c) == MISSING_D)
+        ym[c] = true;
+    }
+  if (skipMissing) {
+    len_i = E - (int)std::count(xm.begin(), xm.end(), true);
+    len_j = E - (int)std::count(ym.begin(), ym.end(), true);
+  } else {
+    len_i = E;
+    len_j = E;
+  }
+  double gamma = 1.0;
+  if (g.E_dt(E) > 0) {
+    double minData = std::numeric_limits<double>::max();
+    double maxData = std::numeric_limits<double>::min();
+    double maxTime = 0.0;
+    for (int t = 0; t < E; t++) {
+      if (at(x, 0, t) != MISSING_D) {
+        if (at(x, 0, t) < minData)
+          minData = at(x, 0, t);
+        if (at(x, 0, t) > maxData)
+          maxData = at(x, 0, t);
+      }
+      if (at(x, 1, t) != MISSING_D && at(x, 1, t) > maxTime)
+        maxTime = at(x, 1, t);
+    }
+    const double epsilon = 1e-6;
+    gamma = opts.aspectRatio * (maxData - minData + epsilon) / (maxTime + epsilon);
+  }
+  double unlaggedDist = 0.0;
+  const int numUnlagged = g.num_extras - g.num_extras_lagged;
+  for (int e = 0; e < numUnlagged; e++) {
+    const double xe = x[(size_t)rows * E + e], ye = y[(size_t)rows * E + e];
+    if (xe == MISSING_D || ye == MISSING_D)
+      unlaggedDist += opts.missingdistance;
+    else
+      unlaggedDist += std::abs(xe - ye);
+  }
+  if (opts.panelMode && opts.idw > 0) {
+    unlaggedDist += opts.idw * (M.panel(i) != Mp.panel(j));
+  } else if (opts.panelMode && !opts.idWeights.empty()) {
+    unlaggedDist += opts.idWeights.at(std::pair<int, int>(M.panel(i), Mp.panel(j)));
+  }
+  std::vector<double> C((size_t)std::max(0, len_i * len_j), unlaggedDist);  // column-major len_i x len_j
+  for (int k = 0; k < rows; k++) {
+    int n = 0;
+    for (int nn = 0; nn < E; nn++) {
+      if (skipMissing && xm[nn])
+        continue;
+      int m = 0;
+      for (int mm = 0; mm < E; mm++) {
+        if (skipMissing && ym[mm])
+          continue;
+        double dist;
+        if (xm[nn] || ym[mm])
+          dist = opts.missingdistance;
+        else
+          dist = std::abs(at(x, k, nn) - at(y, k, mm));
+        if (g.E_dt(E) > 0 && k == 1)
+          dist *= gamma;
+        C[(size_t)m * len_i + n] += dist;
+        m++;
+      }
+      n++;
+    }
+  }
+  return C;
+}
+
+// src/distances.cpp:488-527
+DistanceIndexPairs wasserstein_distances(int Mp_i, const Options& opts, const Manifold& M, const Manifold& Mp)
+{
+  DistanceIndexPairs out;
+  const bool skipOtherPanels = opts.panelMode && (opts.idw < 0);
+  for (int i = 0; i < M.numPoints; i++) {
+    if (skipOtherPanels && M.panel(i) != Mp.panel(Mp_i))
+      continue;
+    int len_i, len_j;
+    std::vector<double> C = wasserstein_cost_matrix(M, Mp, i, Mp_i, opts, len_i, len_j);
+    if (len_i > 0 && len_j > 0) {
+      // EMD_wrap reads the buffer as a row-major len_i x len_j matrix
+      const double d = emd_uniform(C.data(), len_i, len_j);
+      if (d != 0 && std::isnormal(d)) {
+        out.dists.push_back(d);
+        out.inds.push_back(i);
+      }
     }
   }
   return out;
@@ -1004,7 +1213,9 @@ void smap_prediction(int Mp_i, int t, const Options& opts, const Manifold& M, co
 // src/edm.cpp:565-639
 void make_prediction(int Mp_i, const Options& opts, const Manifold& M, const Manifold& Mp, TaskOut& o, bool keepNN)
 {
-  DistanceIndexPairs pn = lp_distances(Mp_i, opts, M, Mp);
+  // src/edm.cpp:578-582
+  DistanceIndexPairs pn = opts.distance == Distance::Wasserstein ? wasserstein_distances(Mp_i, opts, M, Mp)
+                                                                  : lp_distances(Mp_i, opts, M, Mp);
   int numValid = (int)pn.inds.size();
   int k = opts.k;
   if (k > numValid) {
@@ -1791,10 +2002,18 @@ static Options task_options(const Prepared& P, const oracle_args* a, const oracl
   opts.k = io->k;
   opts.copredict = io->copredict != 0;
   opts.forceCompute = io->force_compute != 0;
-  opts.distance = io->distance == 0 ? Distance::MeanAbsoluteError : Distance::Euclidean;
+  opts.distance = io->distance == 0   ? Distance::MeanAbsoluteError
+                  : io->distance == 2 ? Distance::Wasserstein
+                                      : Distance::Euclidean;
+  opts.aspectRatio = io->aspect_ratio;
   opts.saveSMAPCoeffs = true;
   opts.library = 0;
   return opts;
+}
+
+double oracle_emd_uniform(const double* D, int n1, int n2)
+{
+  return emd_uniform(D, n1, n2);
 }
 
 int oracle_task_sizes(const oracle_args* a, oracle_task_io* io)

@@ -111,7 +111,7 @@ typedef struct oracle_task_io {
   int E;
   int k;
   int copredict;
-  int distance; /* 0 MAE (L1), 1 Euclidean */
+  int distance; /* 0 MAE (L1), 1 Euclidean, 2 Wasserstein */
   int force_compute;
   int n_pred, n_lib, e_actual, total_nn; /* filled by oracle_task_sizes */
   double* predictions;
@@ -131,7 +131,13 @@ typedef struct oracle_task_io {
   double* pred_targets; /* [n_pred] or NULL                                 */
   double missing_distance_used;
   double dt_weight_used;
+  double aspect_ratio;  /* Wasserstein with dt (Options::aspectRatio)       */
 } oracle_task_io;
+
+/* The Wasserstein distance's transport cost of an n1 x n2 row-major cost
+ * matrix with masses 1/n1 and 1/n2 (what the reference takes from
+ * EMD_wrap, src/distances.cpp:455-470). */
+double oracle_emd_uniform(const double* D, int n1, int n2);
 
 /* First pass: fills n_pred, n_lib, e_actual and total_nn. */
 int oracle_task_sizes(const oracle_args* args, oracle_task_io* io);

@@ -59,7 +59,7 @@ class OracleTaskIO(C.Structure):
         ("stats_rho", C.c_void_p), ("stats_mae", C.c_void_p), ("lib_point_rows", C.c_void_p),
         ("pred_point_rows", C.c_void_p), ("lib_manifold", C.c_void_p), ("pred_manifold", C.c_void_p),
         ("lib_targets", C.c_void_p), ("pred_targets", C.c_void_p),
-        ("missing_distance_used", C.c_double), ("dt_weight_used", C.c_double),
+        ("missing_distance_used", C.c_double), ("dt_weight_used", C.c_double), ("aspect_ratio", C.c_double),
     ]
 
 
@@ -82,6 +82,8 @@ def load():
         _lib.oracle_set_exp_mode.argtypes = [C.c_int]
         _lib.oracle_set_pred_stride.argtypes = [C.c_int]
         _lib.oracle_set_sum_mode.argtypes = [C.c_int]
+        _lib.oracle_emd_uniform.argtypes = [C.c_void_p, C.c_int, C.c_int]
+        _lib.oracle_emd_uniform.restype = C.c_double
         _lib.oracle_smap_grad.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p, C.c_int, C.c_int,
                                           C.c_double, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
         _lib.oracle_plan.argtypes = [C.POINTER(OracleArgs), C.c_int] + [C.c_void_p] * 7
@@ -243,9 +245,11 @@ def oracle_edm(t, x, y=None, **kw):
     return run_command(normalise(t, x, y, **kw))
 
 
-def oracle_task(a, library_rows, prediction_rows, E, k, copredict=False, distance=1, force_compute=True):
+def oracle_task(a, library_rows, prediction_rows, E, k, copredict=False, distance=1, force_compute=True,
+                aspect_ratio=0.0):
     """One edm_task on explicit masks; returns predictions, coeffs, rc,
-    neighbour lists and the manifolds (numpy arrays)."""
+    neighbour lists and the manifolds (numpy arrays).  distance: 0 mean
+    absolute error, 1 Euclidean, 2 Wasserstein."""
     lib = load()
     keep = []
     s = make_args(a, keep)
@@ -255,6 +259,7 @@ def oracle_task(a, library_rows, prediction_rows, E, k, copredict=False, distanc
     io = OracleTaskIO()
     io.library_rows, io.prediction_rows = lr.ctypes.data, pr.ctypes.data
     io.E, io.k, io.copredict, io.distance, io.force_compute = E, k, int(copredict), distance, int(force_compute)
+    io.aspect_ratio = float(aspect_ratio)
     rc = lib.oracle_task_sizes(C.byref(s), C.byref(io))
     if rc:
         raise RuntimeError(f"oracle_task_sizes rc={rc}")
@@ -358,3 +363,11 @@ def smap_grad(lib, lib_t, pred, pred_t, theta, w, backward=True):
                        pred.shape[0], E, float(theta), w.ctypes.data, C.byref(mse),
                        C.byref(dth) if backward else None, dw.ctypes.data if backward else None, yh.ctypes.data)
     return mse.value, (dth.value if backward else None), (dw if backward else None), yh
+
+
+def emd_uniform(D):
+    """Transport cost of the row-major cost matrix D (n1 x n2) with masses
+    1/n1 and 1/n2, as the reference's Wasserstein distance takes it from
+    EMD_wrap."""
+    D = np.ascontiguousarray(np.asarray(D, dtype=np.float64))
+    return load().oracle_emd_uniform(D.ctypes.data, D.shape[0], D.shape[1])

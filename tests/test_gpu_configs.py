@@ -530,6 +530,56 @@ def test_easy_edm_call_sequence(ctx):
     both(y, x, E=E_best, library=lib_max, theta=opt_theta, algorithm="simplex", k=float("inf"), shuffle=True)
 
 
+def test_series_kept_on_the_device_across_calls(ctx):
+    """A call on the series whose manifolds a context already holds takes
+    them instead of uploading and building again (the easy_edm() pattern: many
+    edm() calls on one series).  Its results are the bits of the same call on a
+    fresh context; a call on another series, or on the same values with other
+    times, builds its own; saved manifolds from the kept buffers are the
+    oracle's."""
+    t, x, y = workloads.coupled_logistic(1500, seed=33)
+    fresh_ctx = fedm.Context(0, precision=ctx.precision)
+
+    def run(c, series, times=t, **kw):
+        r = fedm.edm(times, series, ctx=c, **kw)
+        assert r["rc"] == 0
+        return r, c.timing()
+
+    r, tm = run(ctx, x, E=[2, 3, 4, 5])
+    assert tm["manifold_builds"] + tm["manifolds_reused"] == 4
+    r, tm = run(ctx, x, E=3, theta=[0.5, 2.0], algorithm="smap", k=12)
+    assert (tm["manifold_builds"], tm["manifolds_reused"]) == (0, 1)
+    f, tf = run(fresh_ctx, x, E=3, theta=[0.5, 2.0], algorithm="smap", k=12)
+    assert tf["manifold_builds"] == 1
+    for key in ("rho", "mae"):
+        assert np.array_equal(np.asarray(r["stats"][key]), np.asarray(f["stats"][key]), equal_nan=True)
+    # another series replaces the record; going back builds again
+    r, tm = run(ctx, y, E=3)
+    assert (tm["manifold_builds"], tm["manifolds_reused"]) == (1, 0)
+    r, tm = run(ctx, y, E=3, saveManifolds=True, full=True)
+    assert (tm["manifold_builds"], tm["manifolds_reused"]) == (0, 1)
+    a = edm_oracle.normalise(t, y, E=3, saveManifolds=True, full=True)
+    plan = fedm.host_plan(a)
+    o = edm_oracle.oracle_task(a, plan["lib"][0], plan["pred"][0], 3, int(plan["k"][0]))
+    for got, want in ((r["Ms"][0], o["lib_manifold"]), (r["Mps"][0], o["pred_manifold"])):
+        assert np.array_equal(got, np.where(want == 1e100, np.nan, want), equal_nan=True)
+    r, tm = run(ctx, x, E=3)
+    assert tm["manifold_builds"] == 1
+    # the same values at other times: a gap of three steps leaves the rows
+    # after it without some lags
+    t1 = np.asarray(t, dtype=float).copy()
+    t1[700:] += 3.0
+    r, tm = run(ctx, x, times=t1, E=3)
+    assert tm["manifold_builds"] == 1
+    _stats_close(r, edm_oracle.oracle_edm(t1, x, E=3))
+    # dt columns are a setting of their own (with regular times dt switches
+    # itself off: a zero default dt weight, src/manifold.h:53-67)
+    r, tm = run(ctx, x, times=t1, E=3, dt=True)
+    assert tm["manifold_builds"] == 1
+    _stats_close(r, edm_oracle.oracle_edm(t1, x, E=3, dt=True))
+    fresh_ctx.close()
+
+
 def test_concurrent_contexts_share_the_gpu():
     """Two contexts driven from two host threads at once -- a simplex and an
     S-map CCM call, their mixed kernels capped at 1 and 5 resident CTAs per
