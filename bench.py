@@ -654,7 +654,7 @@ def config_steps(fedm, workloads, ctx, name):
 
 # FP64 instructions per (prediction, library) pair of the Wasserstein
 # neighbour kernel at E = 5 (ncu, profiles/knn_exact_kernel_wasserstein_E5.md)
-WASS_FP64_PER_PAIR = None
+WASS_FP64_PER_PAIR = 1006.6
 
 
 def config_roofline(name, precision, steps_tm, peaks):

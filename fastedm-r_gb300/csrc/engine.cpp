@@ -2124,6 +2124,8 @@ int run_task(Context& ctx, const fedm_args& a, fedm_task_io& io)
   o.force_compute = io.force_compute != 0;
   if (o.distance == 2 && (io.E < 1 || io.E > WASS_EMAX))
     throw Error{ RC_NOT_IMPLEMENTED, "the Wasserstein distance takes 1 <= E <= 16" };
+  // (the task seam routes all-neighbour tasks through knn_exact_kernel, the
+  // only kernel with a Wasserstein instance)
   const Generator& gen = P.gen;
   const int threads = host_threads(a);
   RowTables rt = build_row_tables(gen);

@@ -633,7 +633,6 @@ __global__ void smap_nn_kernel(GroupParams g, ChunkBuffers c, long long slab)
 // its row of the chunk's distance buffer (-1 marks an invalid pair); then
 // one thread per (point, theta) reduces them sequentially in library order,
 // the order the reference's loops use, so the results are the same bits.
-template<bool WASS>
 __global__ void all_dist_kernel(GroupParams g, ChunkBuffers c, long long max_nlib, int per_warp_bytes)
 {
   extern __shared__ __align__(16) unsigned char smem[];
@@ -655,7 +654,7 @@ __global__ void all_dist_kernel(GroupParams g, ChunkBuffers c, long long max_nli
     int lcnt = 0;
     for (int i = lane; i < T.n_lib; i += 32) {
       double d;
-      const bool ok = exact_distance<WASS>(g, g.lib_rows[T.lib_off + i], prow, sy, ppanel, ptime, d);
+      const bool ok = exact_distance<false>(g, g.lib_rows[T.lib_off + i], prow, sy, ppanel, ptime, d);
       dq[i] = ok ? d : -1.0;
       lcnt += ok;
     }
@@ -1308,10 +1307,9 @@ void launch_all_mode(const GroupParams& g, const ChunkBuffers& c, int num_sms, l
     blocks = (long long)num_sms * 64;
   if (blocks < 1)
     blocks = 1;
-  if (g.wasserstein)
-    all_dist_kernel<true><<<(int)blocks, 32 * w, (size_t)w * per_warp, s>>>(g, c, max_nlib, per_warp);
-  else
-    all_dist_kernel<false><<<(int)blocks, 32 * w, (size_t)w * per_warp, s>>>(g, c, max_nlib, per_warp);
+  // the Wasserstein distance is reached only through the task seam, which
+  // sends every task through the neighbour-list path (knn_exact_kernel)
+  all_dist_kernel<<<(int)blocks, 32 * w, (size_t)w * per_warp, s>>>(g, c, max_nlib, per_warp);
   if (chunk * g.n_thetas <= 0)
     return;
   if (ev0)
