@@ -2146,7 +2146,9 @@ int run_task(Context& ctx, const fedm_args& a, fedm_task_io& io)
   t.save_coeffs = true;
   std::vector<Task> tasks{ t };
   std::vector<TaskOut> outs(1);
-  if (!sizes_only || true) {
+  {
+    // the sizes pass runs the task too: total_nn is the length of the
+    // neighbour lists make_prediction keeps, known only after the search
     DevRows drows = upload_rows(ctx, gen, rt, o);
     Manifolds M;
     GroupJob job;
