@@ -257,7 +257,8 @@ def run_ours(a):
             tm = ctx.timing()
             for k in base_keys:
                 tot[k] += tm[k]
-            for k in ("knn_kernel_ms", "knn_launches", "fp64_ops", "distance_pairs", "predictions", "mixed_form"):
+            for k in ("knn_kernel_ms", "knn_launches", "fp64_ops", "distance_pairs", "predictions", "mixed_form",
+                      "scanned_pairs"):
                 tot[f"{alg}_{k}"] = tm[k]
             rhos.append(r["stats"]["rho"])
         return tot, rhos
@@ -297,13 +298,20 @@ def run_ours(a):
     sm_ops = mean_of("smap_fp64_ops")
     sm_points = mean_of("smap_predictions")
     sm_fp64 = sm_ops / (sm_ms * 1e-3) / 1e12
-    sm_fp32 = 3.0 * w["E"] * pairs / 2 / (sm_ms * 1e-3) / 1e12
+    # FP32 scan: the reference's work (every pair, 3 E flops) and the pairs
+    # the one-point kernels actually scored (spatially ordered libraries
+    # skip tiles that no point can use)
+    sm_scanned = mean_of("smap_scanned_pairs")
+    sx_scanned = mean_of("simplex_scanned_pairs")
+    sm_fp32_alg = 3.0 * w["E"] * pairs / 2 / (sm_ms * 1e-3) / 1e12
+    sm_fp32 = 3.0 * w["E"] * sm_scanned / (sm_ms * 1e-3) / 1e12
     traffic = None
     if SMAP_DRAM_BYTES_PER_POINT is not None:
         traffic = SMAP_DRAM_BYTES_PER_POINT * sm_points / sm_launches
     # simplex kernel: FP32 scan + re-rank + forecast
     sx_ms = mean_of("simplex_knn_kernel_ms")
-    sx_fp32 = 3.0 * w["E"] * pairs / 2 / (sx_ms * 1e-3) / 1e12
+    sx_fp32_alg = 3.0 * w["E"] * pairs / 2 / (sx_ms * 1e-3) / 1e12
+    sx_fp32 = 3.0 * w["E"] * sx_scanned / (sx_ms * 1e-3) / 1e12
     knn_ms_step = sm_ms + sx_ms
 
     # plain FP64 GPU form and |delta rho| on a 2-replicate sample
@@ -363,10 +371,15 @@ def run_ours(a):
             "kernel_ms_per_step": sm_ms, "share_of_device_time": sm_ms / (dev_s_max / a.steps * 1e3),
             "traffic": traffic,
             "fp32_scan": {"achieved": sm_fp32, "peak": fp32_peak, "frac": sm_fp32 / fp32_peak,
-                          "flops": "3*E per (prediction, library) pair"},
+                          "flops": "3*E per (prediction, library) pair scored",
+                          "scored_fraction_of_pairs": sm_scanned / max(pairs / 2, 1),
+                          "algorithmic_achieved": sm_fp32_alg},
             "simplex_kernel": {"kernel": form_kernel(s0["simplex_mixed_form"], "simplex"), "bound": "fp32_simt",
                                "achieved": sx_fp32, "peak": fp32_peak, "frac": sx_fp32 / fp32_peak,
                                "kernel_ms_per_step": sx_ms,
+                               "flops": "3*E per (prediction, library) pair scored",
+                               "scored_fraction_of_pairs": sx_scanned / max(pairs / 2, 1),
+                               "algorithmic_achieved": sx_fp32_alg,
                                "peak_source": "measured FFMA rate of this GPU (fedm_measure_peak kind 0)"},
             "hbm": {"achieved_gbs": alg_bytes / (knn_ms_step * 1e-3) / 1e9, "peak_gbs": hbm_gbs,
                     "frac": alg_bytes / (knn_ms_step * 1e-3) / 1e9 / hbm_gbs, "peak_source": hbm_src},

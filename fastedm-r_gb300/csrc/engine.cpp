@@ -86,6 +86,8 @@ Context::Context(int dev) : device(dev)
     host_manifold = std::strcmp(v, "1") == 0;
   if (const char* v = std::getenv("FEDM_SERIES_CACHE"))
     series_cache = std::strcmp(v, "0") != 0;
+  if (const char* v = std::getenv("FEDM_PRUNE"))
+    prune = std::strcmp(v, "0") != 0;
   if (const char* v = std::getenv("FEDM_POINT_ORDER"))
     point_order = std::strcmp(v, "list") == 0 ? 0 : (std::strcmp(v, "morton3") == 0 ? 2 : 1);
   reset_timing();
@@ -96,6 +98,7 @@ void Context::reset_timing()
   timing = fedm_timing{};
   timing.mixed_form = -1;
   lane_orders.clear();  // list and manifold addresses are reused by later calls
+  spatial_ranks.clear();
 }
 
 namespace {
@@ -212,6 +215,45 @@ std::vector<int> morton_lane_order(const double* F, int Ea, const int* rows, int
   for (int i = 0; i < n; i++)
     order[i] = (int)(uint32_t)b[i];
   return order;
+}
+
+} // namespace
+
+namespace {
+
+// Every manifold row's rank in the Morton order of its first four
+// coordinates (8 bits each over the range of the rows that have them all);
+// rows with a missing or non-finite one come last.  Computed once per
+// manifold and call.
+const std::vector<int>& spatial_rank(Context& ctx, const double* F, int n, int Ea)
+{
+  auto it = ctx.spatial_ranks.find(F);
+  if (it != ctx.spatial_ranks.end())
+    return it->second;
+  const int D = std::min(Ea, 4);
+  std::vector<int> rows;
+  rows.reserve(n);
+  for (int i = 0; i < n; i++) {
+    bool ok = true;
+    for (int j = 0; j < D && ok; j++) {
+      const double v = F[(size_t)i * Ea + j];
+      ok = v != MISSING_D && std::isfinite(v);
+    }
+    if (ok)
+      rows.push_back(i);
+  }
+  std::vector<int> rank(n, 0);
+  const std::vector<int> order = morton_lane_order(F, Ea, rows.data(), (int)rows.size(), 4);
+  std::vector<uint8_t> seen(n, 0);
+  int r = 0;
+  for (int s = 0; s < (int)order.size(); s++) {
+    rank[rows[order[s]]] = r++;
+    seen[rows[order[s]]] = 1;
+  }
+  for (int i = 0; i < n; i++)
+    if (!seen[i])
+      rank[i] = r++;
+  return ctx.spatial_ranks.emplace(F, std::move(rank)).first->second;
 }
 
 } // namespace
@@ -736,8 +778,10 @@ void run_group(Context& ctx, const Options& o, const std::vector<Task>& tasks, c
   // gained no device time while their host cost lowered the end-to-end rate
   // by 5%.
   std::vector<int> perm_pool;
-  for (int j = 0; j < nK; j++)
+  for (int j = 0; j < nK; j++) {
     dk[j].perm_off = -1;
+    dk[j].box_off = -1;
+  }
   if (mixed_group && !split && ctx.point_order >= 1 && Ea <= 16) {
     std::map<std::tuple<const void*, int, int, const void*>, int> offs;
     for (int j = 0; j < nK; j++) {
@@ -757,6 +801,32 @@ void run_group(Context& ctx, const Options& o, const std::vector<Task>& tasks, c
         perm_pool.insert(perm_pool.end(), c->second.begin(), c->second.end());
       }
       dk[j].perm_off = it->second;
+    }
+  }
+  // spatially ordered scans of the one-point mixed kernels (one_point.cuh):
+  // each library list of PRUNE_MIN..PRUNE_MAX rows that a mixed kernel task
+  // scans gets an order of its positions by the spatial rank of their rows
+  // (a counting sort on the rank's top 12 bits: tiles of 1 024 rows then
+  // hold rows of a compact region) and BOX_ROWS-row sub-tiles whose boxes a
+  // kernel computes once the float manifold exists
+  constexpr int PRUNE_MIN = 2048, PRUNE_MAX = 1 << 18;
+  std::vector<int4> subtiles;
+  std::vector<const std::vector<int>*> scan_src;
+  std::unordered_map<const std::vector<int>*, int> box_of;
+  if (mixed_group && !split && ctx.prune && job.hF) {
+    for (int q = 0; q < nK; q++) {
+      const std::vector<int>* L = kt[q].L;
+      if (!dk[q].mixed || (int)L->size() < PRUNE_MIN || (int)L->size() > PRUNE_MAX)
+        continue;
+      auto it = box_of.find(L);
+      if (it == box_of.end()) {
+        it = box_of.emplace(L, (int)subtiles.size()).first;
+        scan_src.push_back(L);
+        const int off = lib_off[L];
+        for (int st = 0; st < (int)L->size(); st += BOX_ROWS)
+          subtiles.push_back(make_int4(off, st, std::min<int>(BOX_ROWS, (int)L->size() - st), 0));
+      }
+      dk[q].box_off = it->second;
     }
   }
   // library position of slot v of point p in its task's list (detail mode)
@@ -800,6 +870,39 @@ void run_group(Context& ctx, const Options& o, const std::vector<Task>& tasks, c
   };
   const int* h_lib = fill_pool(lib_src, lib_total, "lib_pool");
   const int* h_pred = fill_pool(pred_src, pred_total, "pred_pool");
+  // the spatial scan orders, at the lists' offsets in the library pool
+  int* d_scan = nullptr;
+  if (!scan_src.empty()) {
+    const std::vector<int>& rank = spatial_rank(ctx, job.hF, rows.n_rows, Ea);
+    int sh = 0;
+    while ((rows.n_rows >> sh) > 4096)
+      sh++;
+    const int nb = (rows.n_rows >> sh) + 1;
+    int* h = (int*)ctx.host_buf("scan_pool", (size_t)std::max<long long>(lib_total, 1) * 4);
+    const int nth_sort = (int)std::min<size_t>(8, scan_src.size());
+    auto sort_range = [&](int w) {
+      std::vector<int> cnt(nb + 1);
+      for (size_t l = w; l < scan_src.size(); l += nth_sort) {
+        const std::vector<int>& L = *scan_src[l];
+        int* out = h + lib_off[scan_src[l]];
+        std::fill(cnt.begin(), cnt.end(), 0);
+        for (int v : L)
+          cnt[(rank[v] >> sh) + 1]++;
+        for (int b = 0; b < nb; b++)
+          cnt[b + 1] += cnt[b];
+        for (int q = 0; q < (int)L.size(); q++)
+          out[cnt[rank[L[q]] >> sh]++] = q;
+      }
+    };
+    std::vector<std::thread> pool;
+    for (int w = 1; w < nth_sort; w++)
+      pool.emplace_back(sort_range, w);
+    sort_range(0);
+    for (auto& th : pool)
+      th.join();
+    d_scan = (int*)ctx.buf("scan_pool", (size_t)std::max<long long>(lib_total, 1) * 4);
+    ctx.upload(d_scan, h, (size_t)lib_total * 4);
+  }
   int* d_lib = (int*)ctx.buf("lib_pool", (size_t)std::max<long long>(lib_total, 1) * 4);
   int* d_pred = (int*)ctx.buf("pred_pool", (size_t)std::max<long long>(pred_total, 1) * 4);
   double* d_thetas = (double*)ctx.buf("thetas", nth * 8);
@@ -1170,6 +1273,7 @@ void run_group(Context& ctx, const Options& o, const std::vector<Task>& tasks, c
     m.fb_count = m.counter + 1;
     m.fp64_ops = (unsigned long long*)(m.counter + 2);
     m.error = m.counter + 4;
+    m.scanned = (unsigned long long*)(m.counter + 6);
     fill_i32(m.counter, 8, 0, s);
     m.form = ctx.mixed_form;
     m.fb_cap = (int)std::min<long long>(std::max<long long>(P, 1), FB_CAP);
@@ -1184,6 +1288,17 @@ void run_group(Context& ctx, const Options& o, const std::vector<Task>& tasks, c
       m.nn_dist = (double*)ctx.buf("mix_nn_dist", (size_t)std::max<long long>(P, 1) * C * 8);
     }
     ctx.timing.kernel_launches += (job.dFp != job.dF ? 2 : 1) + 1;  // centring, counter fill
+    if (d_scan) {
+      // boxes of the spatially ordered lists' sub-tiles, from the float manifold
+      int4* d_sub = (int4*)ctx.buf("subtiles", subtiles.size() * sizeof(int4));
+      float2* d_boxes = (float2*)ctx.buf("boxes", subtiles.size() * Ea * sizeof(float2));
+      ctx.upload(d_sub, subtiles.data(), subtiles.size() * sizeof(int4));
+      launch_tile_boxes(d_lib, d_scan, F32, S, Ea, d_sub, (int)subtiles.size(), d_boxes, s);
+      ctx.check("tile_box_kernel");
+      ctx.timing.kernel_launches += 1;
+      m.scan_pos = d_scan;
+      m.boxes = d_boxes;
+    }
     m.kslots = C;
     m.ctas_per_sm = ctx.ctas_per_sm;
     // The split S-map: the items in chunks; the scan of a chunk writes its
@@ -1343,13 +1458,16 @@ void run_group(Context& ctx, const Options& o, const std::vector<Task>& tasks, c
     int nfb = 0, herr = 0;
     unsigned long long nops = 0;
     ctx.download(&nfb, m.fb_count, 4);
+    unsigned long long nscan = 0;
     ctx.download(&nops, m.fp64_ops, 8);
+    ctx.download(&nscan, m.scanned, 8);
     ctx.download(&herr, m.error, 4);
     ck(cudaStreamSynchronize(s), "sync");
     if (herr)
       throw Error{ RC_UNKNOWN_ERROR, "mixed S-map kernel: scan/solve hand-off timed out" };
     ctx.timing.fallback_points += nfb;
     ctx.timing.fp64_ops += (long long)nops;
+    ctx.timing.scanned_pairs += (long long)nscan;
     if (split_done) {
       for (int b = 0; b < SPLIT_BUFS; b++) {
         cudaEventDestroy(scan_ev[b]);

@@ -73,6 +73,13 @@ public:
   // the lane orders computed during the current call, by (list, first row,
   // rows, manifold): a CCM call's batches share its prediction list
   std::map<std::tuple<const void*, int, int, const void*>, std::vector<int>> lane_orders;
+  // Spatially ordered library scans of the one-point mixed kernels (lists
+  // of 2 048 to 262 144 rows, scanned in a Morton order of their rows with
+  // tiles that no point of a work item can use skipped; the same bits):
+  // on by default, FEDM_PRUNE=0 turns it off.  spatial_ranks: per manifold
+  // of the current call, every row's rank in that order.
+  bool prune = true;
+  std::map<const void*, std::vector<int>> spatial_ranks;
   // The split S-map (MIXED_SPLIT): a second stream for the solves, the
   // scan's and the solver's resident CTAs per SM (FEDM_SPLIT_SCAN_CTAS,
   // FEDM_SPLIT_SOLVE_CTAS) and the points per chunk of the pipeline.

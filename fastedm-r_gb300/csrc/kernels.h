@@ -34,7 +34,15 @@ struct DevTask
   int perm_off;          // one-point mixed kernels: point i of a work item's
                          // slot order is GroupParams::perm[perm_off + slot]
                          // (-1: slot order is list order)
+  int box_off;           // one-point mixed kernels: -1, or the library is
+                         // scanned in the spatial order MixedRun::scan_pos
+                         // [lib_off + i] (positions in the list), whose
+                         // 512-row sub-tiles have bounding boxes at
+                         // MixedRun::boxes[(box_off + s) * E_a + j]
 };
+
+// Rows per sub-tile of the bounding boxes of a spatially ordered library.
+constexpr int BOX_ROWS = 512;
 
 // Largest E (columns of a point) the Wasserstein distance takes.
 constexpr int WASS_EMAX = 16;
@@ -184,7 +192,20 @@ struct MixedRun
   int* l_rows;         // [L x slots] their library manifold rows
   double* l_dist;      // [L x slots] their FP64 distances
   long long l_slots;   // slots of the list buffers (the stride of l_rows / l_dist)
+  // spatially ordered libraries (DevTask::box_off): positions in scan order,
+  // the sub-tiles' (min, max) per coordinate, and a count of the
+  // (prediction, library row) pairs the one-point scan actually scored
+  const int* scan_pos;
+  const float2* boxes;
+  unsigned long long* scanned;
 };
+
+// Bounding boxes of BOX_ROWS-row sub-tiles of spatially ordered libraries:
+// sub-tile s covers positions [t.y, t.y + t.z) of the scan order of the list
+// at pool offset t.x (rows lib_rows[t.x + scan_pos[t.x + i]]); boxes[s * ea
+// + j] = (min, max) of coordinate j of the float manifold (row stride rs).
+void launch_tile_boxes(const int* lib_rows, const int* scan_pos, const float* F32, int rs, int ea, const int4* subtiles,
+                       int n_subtiles, float2* boxes, cudaStream_t s);
 
 void launch_knn_mixed(const GroupParams& g, const MixedRun& m, int C, int num_sms, cudaStream_t s);
 

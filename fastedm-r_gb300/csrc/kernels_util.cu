@@ -1,9 +1,63 @@
-// Small device helpers: fills, and the peak probes of the roofline.
+// Small device helpers: fills, the bounding boxes of spatially ordered
+// library sub-tiles, and the peak probes of the roofline.
 #include <cuda_runtime.h>
+
+#include "kernels.h"
 
 namespace fedm {
 
 namespace {
+
+// One CTA of 256 threads per sub-tile: each thread takes rows i = tid,
+// tid + 256, ... of it and keeps (min, max) per coordinate; a warp-shuffle
+// and a shared-memory reduction give the sub-tile's box.  min and max of
+// float values are exact, so every row of the sub-tile lies in its box.
+__global__ void __launch_bounds__(256) tile_box_kernel(const int* lib_rows, const int* scan_pos, const float* F32,
+                                                       int rs, int ea, const int4* subtiles, float2* boxes)
+{
+  constexpr int EMAX = 16;
+  const int4 t = subtiles[blockIdx.x];
+  __shared__ float s_lo[8][EMAX], s_hi[8][EMAX];
+  const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+  float lo[EMAX], hi[EMAX];
+#pragma unroll
+  for (int j = 0; j < EMAX; j++) {
+    lo[j] = INFINITY;
+    hi[j] = -INFINITY;
+  }
+  for (int i = tid; i < t.z; i += 256) {
+    const float* r = F32 + (size_t)lib_rows[t.x + scan_pos[t.x + t.y + i]] * rs;
+#pragma unroll
+    for (int j = 0; j < EMAX; j++)
+      if (j < ea) {
+        lo[j] = fminf(lo[j], r[j]);
+        hi[j] = fmaxf(hi[j], r[j]);
+      }
+  }
+#pragma unroll
+  for (int j = 0; j < EMAX; j++) {
+    if (j < ea) {
+      float a = lo[j], b = hi[j];
+      for (int o = 16; o > 0; o >>= 1) {
+        a = fminf(a, __shfl_xor_sync(0xffffffffu, a, o));
+        b = fmaxf(b, __shfl_xor_sync(0xffffffffu, b, o));
+      }
+      if (lane == 0) {
+        s_lo[w][j] = a;
+        s_hi[w][j] = b;
+      }
+    }
+  }
+  __syncthreads();
+  if (tid < ea) {
+    float a = s_lo[0][tid], b = s_hi[0][tid];
+    for (int q = 1; q < 8; q++) {
+      a = fminf(a, s_lo[q][tid]);
+      b = fmaxf(b, s_hi[q][tid]);
+    }
+    boxes[(size_t)blockIdx.x * ea + tid] = make_float2(a, b);
+  }
+}
 
 __global__ void fill_f64_kernel(double* p, long long n, double v)
 {
@@ -37,6 +91,13 @@ void fill_i32(int* p, long long n, int v, cudaStream_t s)
 {
   if (n > 0)
     fill_i32_kernel<<<grid_for(n), 256, 0, s>>>(p, n, v);
+}
+
+void launch_tile_boxes(const int* lib_rows, const int* scan_pos, const float* F32, int rs, int ea, const int4* subtiles,
+                       int n_subtiles, float2* boxes, cudaStream_t s)
+{
+  if (n_subtiles > 0 && ea >= 1 && ea <= 16)
+    tile_box_kernel<<<n_subtiles, 256, 0, s>>>(lib_rows, scan_pos, F32, rs, ea, subtiles, boxes);
 }
 
 } // namespace fedm

@@ -357,6 +357,18 @@ __device__ __forceinline__ void add_ops(const MixedRun& m, unsigned long long op
   }
 }
 
+// Adds the warp's count of scored (prediction, library row) pairs to the
+// run's counter; called by whole warps.
+__device__ __forceinline__ void add_scanned(const MixedRun& m, unsigned long long n)
+{
+  if (m.scanned) {
+    for (int o = 16; o > 0; o >>= 1)
+      n += __shfl_xor_sync(0xffffffffu, n, o);
+    if ((threadIdx.x & 31) == 0)
+      atomicAdd(m.scanned, n);
+  }
+}
+
 template<int C>
 struct Job
 {

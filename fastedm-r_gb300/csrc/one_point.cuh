@@ -21,10 +21,26 @@ namespace {
 // the tile's panel ids staged in tpan.  The FP32 value then carries one more
 // rounded addition, within the certification's accumulation bound, and
 // sqrt(idw + x^2) is 1-Lipschitz in x, so the input-rounding term holds too.
+//
+// Spatially ordered libraries (T.box_off >= 0): the rows come in the order
+// m.scan_pos (library positions sorted by a Morton key of their
+// coordinates), in tiles of TR rows whose boxes (the union of their
+// BOX_ROWS-row sub-tiles' boxes) are known.  The CTA visits the tiles that
+// overlap the box of its 256 points first, then the others, and skips a
+// tile for a point when a lower bound on the FP32 value of any of its rows
+// is not below the point's current C-th value: the scan would reject every
+// such row (offer keeps values below D[C-1], which only decreases).  The
+// bound is formed like the scan's value, from the distance to the box per
+// coordinate with the same rounded subtraction, square and fused
+// multiply-add sequence; each step is monotone, so no row of the tile can
+// score below it.  A tile no point needs is not staged.  The kept list is
+// therefore the same C smallest values as a scan of every row (with ties
+// at the C-th value settled by the certification as before), and positions
+// are the list's, so the re-rank and its ties are unchanged.
 template<int EA, int C, int RS, int TR, int NT, bool PEN = false>
 __device__ __forceinline__ void scan_item_one(const GroupParams& g, const MixedRun& m, const DevTask& T, int first,
-                                              int tid, float2* tile, int* tpan, Cand<C>& c0, int& prow0, bool& a0,
-                                              int& pi)
+                                              int tid, float2* tile, int* tpan, int* tpos, float* wbox, Cand<C>& c0,
+                                              int& prow0, bool& a0, int& pi, unsigned long long& scanned)
 {
   // the slot's point: list order, or the task's lane order (points close
   // in the manifold on neighbouring lanes, so that a warp's candidate
@@ -55,6 +71,116 @@ __device__ __forceinline__ void scan_item_one(const GroupParams& g, const MixedR
     zi0[j] = -1;
   const float pen = PEN ? (float)g.idw : 0.f;
   const int ppan = PEN && a0 ? g.panel[prow0] : 0;
+  if (T.box_off >= 0) {
+    // the box of the CTA's points: per warp, then combined into wbox[0..2EA)
+    constexpr int NW = NT / 32;
+    const int lane = tid & 31, w = tid >> 5;
+#pragma unroll
+    for (int j = 0; j < EA; j++) {
+      float lo = a0 ? -na[j].x : INFINITY, hi = a0 ? -na[j].x : -INFINITY;
+      for (int o = 16; o > 0; o >>= 1) {
+        lo = fminf(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+        hi = fmaxf(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+      }
+      if (lane == 0) {
+        wbox[(w + 1) * 2 * EA + j] = lo;
+        wbox[(w + 1) * 2 * EA + EA + j] = hi;
+      }
+    }
+    __syncthreads();
+    if (tid < EA) {
+      float lo = wbox[2 * EA + tid], hi = wbox[2 * EA + EA + tid];
+      for (int q = 2; q <= NW; q++) {
+        lo = fminf(lo, wbox[q * 2 * EA + tid]);
+        hi = fmaxf(hi, wbox[q * 2 * EA + EA + tid]);
+      }
+      wbox[tid] = lo;
+      wbox[EA + tid] = hi;
+    }
+    __syncthreads();
+    constexpr int SPT = TR / BOX_ROWS;
+    const int ntile = (T.n_lib + TR - 1) / TR;
+    const int nsub = (T.n_lib + BOX_ROWS - 1) / BOX_ROWS;
+    for (int pass = 0; pass < 2; pass++) {
+      for (int tt = 0; tt < ntile; tt++) {
+        // the tile's box (the union of its sub-tiles'), whether it overlaps
+        // the points' box, and this thread's lower bound on the scan's value
+        // for any row of it
+        bool overlap = true;
+        float lb = 0.f;
+#pragma unroll
+        for (int j = 0; j < EA; j++) {
+          float tlo = INFINITY, thi = -INFINITY;
+#pragma unroll
+          for (int u = 0; u < SPT; u++) {
+            const int sb = tt * SPT + u;
+            if (sb < nsub) {
+              const float2 b = m.boxes[(size_t)(T.box_off + sb) * EA + j];
+              tlo = fminf(tlo, b.x);
+              thi = fmaxf(thi, b.y);
+            }
+          }
+          overlap = overlap && tlo <= wbox[EA + j] && thi >= wbox[j];
+          const float p = -na[j].x;
+          const float d = p < tlo ? __fadd_rn(tlo, na[j].x) : (p > thi ? __fadd_rn(thi, na[j].x) : 0.f);
+          lb = j == 0 ? __fmul_rn(d, d) : __fmaf_rn(d, d, lb);
+        }
+        if (overlap != (pass == 0))
+          continue;  // the same for every thread of the CTA
+        const bool need = a0 && lb < D0[C - 1];
+        if (!__syncthreads_or(need))
+          continue;
+        const int t0 = tt * TR;
+        const int cnt = min(TR, T.n_lib - t0);
+        const int npairs = (cnt + 1) >> 1;
+        for (int i = tid; i < 2 * npairs; i += NT) {
+          float* dst = reinterpret_cast<float*>(tile + (i >> 1) * EA) + (i & 1);
+          if (i < cnt) {
+            const int pos = m.scan_pos[T.lib_off + t0 + i];
+            const int row = g.lib_rows[T.lib_off + pos];
+            const float* src = m.F32 + (size_t)row * RS;
+#pragma unroll
+            for (int j = 0; j < EA; j++)
+              dst[2 * j] = src[j];
+            tpos[i] = pos;
+            if constexpr (PEN)
+              tpan[i] = g.panel[row];
+          } else {
+#pragma unroll
+            for (int j = 0; j < EA; j++)
+              dst[2 * j] = 1e30f;  // padding row: never a candidate
+            tpos[i] = 0;
+            if constexpr (PEN)
+              tpan[i] = 0;
+          }
+        }
+        __syncthreads();
+        if (need) {
+          scanned += (unsigned long long)cnt;
+#pragma unroll 2
+          for (int ip = 0; ip < npairs; ip++) {
+            const float2* xr = tile + ip * EA;
+            float2 d = __fadd2_rn(xr[0], na[0]);
+            float2 sa = __fmul2_rn(d, d);
+#pragma unroll
+            for (int j = 1; j < EA; j++) {
+              d = __fadd2_rn(xr[j], na[j]);
+              sa = __ffma2_rn(d, d, sa);
+            }
+            if constexpr (PEN) {
+              const int2 pp = reinterpret_cast<const int2*>(tpan)[ip];
+              sa = __fadd2_rn(sa, make_float2(pp.x != ppan ? pen : 0.f, pp.y != ppan ? pen : 0.f));
+            }
+            if (fminf(sa.x, sa.y) < D0[C - 1]) {
+              const int2 lp = reinterpret_cast<const int2*>(tpos)[ip];
+              offer<C>(D0, I0, z0, zi0, sa.x, lp.x);
+              offer<C>(D0, I0, z0, zi0, sa.y, lp.y);
+            }
+          }
+        }
+      }
+    }
+  } else {
   for (int t0 = 0; t0 < T.n_lib; t0 += TR) {
     const int cnt = min(TR, T.n_lib - t0);
     const int npairs = (cnt + 1) >> 1;
@@ -98,6 +224,8 @@ __device__ __forceinline__ void scan_item_one(const GroupParams& g, const MixedR
         offer<C>(D0, I0, z0, zi0, sa.y, li + 1);
       }
     }
+    scanned += a0 ? (unsigned long long)cnt : 0ull;
+  }
   }
 #pragma unroll
   for (int j = 0; j < C; j++) {
@@ -115,9 +243,11 @@ __global__ void __launch_bounds__(NT, OCC) knn_one_kernel(GroupParams g, MixedRu
 {
   __shared__ __align__(16) float2 tile[(TR / 2) * EA];
   __shared__ __align__(8) int tpan[PEN ? TR : 2];
+  __shared__ __align__(8) int tpos[TR];
+  __shared__ float wbox[(NT / 32 + 1) * 2 * EA];
   __shared__ int s_item;
   const int tid = threadIdx.x;
-  unsigned long long ops = 0;
+  unsigned long long ops = 0, scanned = 0;
   for (;;) {
     __syncthreads();
     if (tid == 0)
@@ -126,6 +256,7 @@ __global__ void __launch_bounds__(NT, OCC) knn_one_kernel(GroupParams g, MixedRu
     const int item = s_item;
     if (item >= m.item_end) {
       add_ops(m, ops);  // every thread of the CTA leaves here together
+      add_scanned(m, scanned);
       return;
     }
     const int2 it = m.items[item];
@@ -133,7 +264,7 @@ __global__ void __launch_bounds__(NT, OCC) knn_one_kernel(GroupParams g, MixedRu
     Cand<C> c0;
     int prow0, pi0;
     bool a0;
-    scan_item_one<EA, C, RS, TR, NT, PEN>(g, m, T, it.y, tid, tile, tpan, c0, prow0, a0, pi0);
+    scan_item_one<EA, C, RS, TR, NT, PEN>(g, m, T, it.y, tid, tile, tpan, tpos, wbox, c0, prow0, a0, pi0, scanned);
     if constexpr (ALG == 2) {
       // S-map lists for smap_list_kernel: settle the neighbours, write them
       const long long slot = (long long)(item - m.item_begin) * NT + tid;

@@ -248,6 +248,9 @@ typedef struct fedm_timing {
                                 by this call                                 */
   int manifolds_reused;      /* manifolds taken from the context's buffers,
                                 built by an earlier call on the same series  */
+  long long scanned_pairs;   /* one-point mixed kernels: (prediction, library)
+                                pairs actually scored; spatially ordered
+                                libraries skip tiles no point can use        */
 } fedm_timing;
 
 int fedm_last_timing(const fedm_ctx* ctx, fedm_timing* out);

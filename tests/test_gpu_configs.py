@@ -310,6 +310,48 @@ def test_lane_and_item_orders_keep_bits(point_order, item_order, algorithm, monk
 
 
 @pytest.mark.parametrize("algorithm", ["simplex", "smap"])
+@pytest.mark.parametrize("k", [5, 10])
+def test_spatial_scan_keeps_bits(algorithm, k, monkeypatch):
+    """Libraries of 2 048 rows and more are scanned in a Morton order of
+    their rows, skipping tiles no point of a work item can use.  The kept
+    candidates, and so every forecast and neighbour list, are those of the
+    scan in list order (FEDM_PRUNE=0); fewer pairs are scored."""
+    w = workloads.ccm_config(T=24000, reps=2, n_libs=4, hi=20000)
+    kw = dict(E=4, k=k, library=w["libraries"], numReps=2, seed=w["seed"], algorithm=algorithm,
+              theta=2.0 if algorithm == "smap" else 1.0, savePredictions=True,
+              saveSMAPCoeffs=algorithm == "smap")
+    monkeypatch.setenv("FEDM_PRUNE", "0")
+    plain = fedm.Context(0, precision=fedm.PRECISION_MIXED)
+    monkeypatch.delenv("FEDM_PRUNE")
+    pruned = fedm.Context(0, precision=fedm.PRECISION_MIXED)
+    try:
+        f = fedm.edm(w["t"], w["x"], w["y"], ctx=plain, **kw)
+        tf = plain.timing()
+        g = fedm.edm(w["t"], w["x"], w["y"], ctx=pruned, **kw)
+        tg = pruned.timing()
+        assert g["rc"] == f["rc"] == 0 and tg["mixed_form"] >= 0
+        assert np.array_equal(g["stats"]["rho"], f["stats"]["rho"], equal_nan=True)
+        assert np.array_equal(g["predictions"], f["predictions"], equal_nan=True)
+        if algorithm == "smap":
+            assert np.array_equal(g["coeffs"], f["coeffs"], equal_nan=True)
+        assert tf["scanned_pairs"] == tf["distance_pairs"]
+        assert 0 < tg["scanned_pairs"] < tf["scanned_pairs"]
+        # neighbour lists of one large task through the task seam
+        a = fedm.normalise(w["t"], w["x"], w["y"], E=4, theta=1.0, algorithm=algorithm)
+        lib = np.zeros(len(w["t"]), bool)
+        lib[np.random.default_rng(3).choice(len(w["t"]) - 10, 15000, replace=False) + 5] = True
+        pred = np.ones(len(w["t"]), bool)
+        rg = pruned.run_task(a, lib, pred, 4, k)
+        rf = plain.run_task(a, lib, pred, 4, k)
+        for key in ("nn_idx", "kused", "predictions"):
+            assert np.array_equal(rg[key], rf[key], equal_nan=True), key
+        assert np.array_equal(rg["nn_dist"].view(np.int64), rf["nn_dist"].view(np.int64))
+    finally:
+        plain.close()
+        pruned.close()
+
+
+@pytest.mark.parametrize("algorithm", ["simplex", "smap"])
 @pytest.mark.parametrize("form", ["one16", "fused2"])
 def test_k_up_to_16_forms_agree(form, algorithm, monkeypatch):
     """For 7 <= k <= 14 the mixed path has two forms: one point per thread
