@@ -806,9 +806,9 @@ void run_group(Context& ctx, const Options& o, const std::vector<Task>& tasks, c
   // spatially ordered scans of the one-point mixed kernels (one_point.cuh):
   // each library list of PRUNE_MIN..PRUNE_MAX rows that a mixed kernel task
   // scans gets an order of its positions by the spatial rank of their rows
-  // (a counting sort on the rank's top 12 bits: tiles of 1 024 rows then
-  // hold rows of a compact region) and BOX_ROWS-row sub-tiles whose boxes a
-  // kernel computes once the float manifold exists
+  // (a counting sort on the rank's top 12 bits, on the device: tiles of
+  // 1 024 rows then hold rows of a compact region) and BOX_ROWS-row
+  // sub-tiles whose boxes a kernel computes once the float manifold exists
   constexpr int PRUNE_MIN = 2048, PRUNE_MAX = 1 << 18;
   std::vector<int4> subtiles;
   std::vector<const std::vector<int>*> scan_src;
@@ -870,39 +870,6 @@ void run_group(Context& ctx, const Options& o, const std::vector<Task>& tasks, c
   };
   const int* h_lib = fill_pool(lib_src, lib_total, "lib_pool");
   const int* h_pred = fill_pool(pred_src, pred_total, "pred_pool");
-  // the spatial scan orders, at the lists' offsets in the library pool
-  int* d_scan = nullptr;
-  if (!scan_src.empty()) {
-    const std::vector<int>& rank = spatial_rank(ctx, job.hF, rows.n_rows, Ea);
-    int sh = 0;
-    while ((rows.n_rows >> sh) > 4096)
-      sh++;
-    const int nb = (rows.n_rows >> sh) + 1;
-    int* h = (int*)ctx.host_buf("scan_pool", (size_t)std::max<long long>(lib_total, 1) * 4);
-    const int nth_sort = (int)std::min<size_t>(8, scan_src.size());
-    auto sort_range = [&](int w) {
-      std::vector<int> cnt(nb + 1);
-      for (size_t l = w; l < scan_src.size(); l += nth_sort) {
-        const std::vector<int>& L = *scan_src[l];
-        int* out = h + lib_off[scan_src[l]];
-        std::fill(cnt.begin(), cnt.end(), 0);
-        for (int v : L)
-          cnt[(rank[v] >> sh) + 1]++;
-        for (int b = 0; b < nb; b++)
-          cnt[b + 1] += cnt[b];
-        for (int q = 0; q < (int)L.size(); q++)
-          out[cnt[rank[L[q]] >> sh]++] = q;
-      }
-    };
-    std::vector<std::thread> pool;
-    for (int w = 1; w < nth_sort; w++)
-      pool.emplace_back(sort_range, w);
-    sort_range(0);
-    for (auto& th : pool)
-      th.join();
-    d_scan = (int*)ctx.buf("scan_pool", (size_t)std::max<long long>(lib_total, 1) * 4);
-    ctx.upload(d_scan, h, (size_t)lib_total * 4);
-  }
   int* d_lib = (int*)ctx.buf("lib_pool", (size_t)std::max<long long>(lib_total, 1) * 4);
   int* d_pred = (int*)ctx.buf("pred_pool", (size_t)std::max<long long>(pred_total, 1) * 4);
   double* d_thetas = (double*)ctx.buf("thetas", nth * 8);
@@ -913,6 +880,28 @@ void run_group(Context& ctx, const Options& o, const std::vector<Task>& tasks, c
     ctx.upload(d_perm, perm_pool.data(), perm_pool.size() * 4);
   ctx.upload(d_lib, h_lib, (size_t)lib_total * 4);
   ctx.upload(d_pred, h_pred, (size_t)pred_total * 4);
+  // the spatial scan orders, at the lists' offsets in the library pool: a
+  // counting sort per list on the device, on the top bits of each row's
+  // spatial rank (at most 4 096 buckets)
+  int* d_scan = nullptr;
+  int2* d_lists = nullptr;
+  int* d_rank = nullptr;
+  int scan_sh = 0, scan_nb = 0;
+  if (!scan_src.empty()) {
+    const std::vector<int>& rank = spatial_rank(ctx, job.hF, rows.n_rows, Ea);
+    while ((rows.n_rows >> scan_sh) >= 4096)
+      scan_sh++;
+    scan_nb = (rows.n_rows >> scan_sh) + 1;
+    std::vector<int2> lists;
+    lists.reserve(scan_src.size());
+    for (const std::vector<int>* L : scan_src)
+      lists.push_back(make_int2(lib_off[L], (int)L->size()));
+    d_rank = (int*)ctx.buf("spatial_rank", (size_t)std::max(rows.n_rows, 1) * 4);
+    d_lists = (int2*)ctx.buf("scan_lists", lists.size() * sizeof(int2));
+    ctx.upload(d_rank, rank.data(), (size_t)rows.n_rows * 4);
+    ctx.upload(d_lists, lists.data(), lists.size() * sizeof(int2));
+    d_scan = (int*)ctx.buf("scan_pool", (size_t)std::max<long long>(lib_total, 1) * 4);
+  }
   ctx.upload(d_thetas, o.thetas.data(), nth * 8);
 
   GroupParams g{};
@@ -1289,7 +1278,11 @@ void run_group(Context& ctx, const Options& o, const std::vector<Task>& tasks, c
     }
     ctx.timing.kernel_launches += (job.dFp != job.dF ? 2 : 1) + 1;  // centring, counter fill
     if (d_scan) {
-      // boxes of the spatially ordered lists' sub-tiles, from the float manifold
+      // the lists' spatial orders, then the boxes of their sub-tiles from the
+      // float manifold (inside the timed span)
+      launch_spatial_order(d_lib, d_rank, scan_sh, scan_nb, d_lists, (int)scan_src.size(), d_scan, s);
+      ctx.check("spatial_order_kernel");
+      ctx.timing.kernel_launches += 1;
       int4* d_sub = (int4*)ctx.buf("subtiles", subtiles.size() * sizeof(int4));
       float2* d_boxes = (float2*)ctx.buf("boxes", subtiles.size() * Ea * sizeof(float2));
       ctx.upload(d_sub, subtiles.data(), subtiles.size() * sizeof(int4));

@@ -200,6 +200,12 @@ struct MixedRun
   unsigned long long* scanned;
 };
 
+// Spatial scan orders of library lists (list l at pool offset lists[l].x,
+// lists[l].y entries): its positions sorted by the bucket rank[row] >> sh
+// of their rows (nb buckets, nb <= 8192), into scan_pos at the same offsets.
+void launch_spatial_order(const int* lib_rows, const int* rank, int sh, int nb, const int2* lists, int n_lists,
+                          int* scan_pos, cudaStream_t s);
+
 // Bounding boxes of BOX_ROWS-row sub-tiles of spatially ordered libraries:
 // sub-tile s covers positions [t.y, t.y + t.z) of the scan order of the list
 // at pool offset t.x (rows lib_rows[t.x + scan_pos[t.x + i]]); boxes[s * ea

@@ -79,6 +79,55 @@ int grid_for(long long n)
   return b < 1 ? 1 : (int)b;
 }
 
+// One CTA of 256 threads per library list (pool offset L.x, L.y entries):
+// a counting sort of its positions q by the bucket rank[lib_rows[L.x + q]]
+// >> sh (nb buckets), written to scan_pos[L.x ...].  Shared-memory atomics
+// make the order within a bucket vary from run to run; the scan that reads
+// it gives the same results in any order.
+__global__ void __launch_bounds__(256) spatial_order_kernel(const int* lib_rows, const int* rank, int sh, int nb,
+                                                            const int2* lists, int* scan_pos)
+{
+  extern __shared__ int cnt[];  // nb bucket counters, then 256 partial sums
+  int* part = cnt + nb;
+  const int2 L = lists[blockIdx.x];
+  const int tid = threadIdx.x;
+  for (int b = tid; b < nb; b += 256)
+    cnt[b] = 0;
+  __syncthreads();
+  for (int q = tid; q < L.y; q += 256)
+    atomicAdd(&cnt[rank[lib_rows[L.x + q]] >> sh], 1);
+  __syncthreads();
+  // exclusive prefix sums: each thread a contiguous chunk of buckets, then
+  // the chunks' totals
+  const int per = (nb + 255) / 256;
+  const int b0 = tid * per, b1 = min(nb, b0 + per);
+  int sum = 0;
+  for (int b = b0; b < b1; b++)
+    sum += cnt[b];
+  part[tid] = sum;
+  __syncthreads();
+  if (tid == 0) {
+    int run = 0;
+    for (int w = 0; w < 256; w++) {
+      const int v = part[w];
+      part[w] = run;
+      run += v;
+    }
+  }
+  __syncthreads();
+  int run = part[tid];
+  for (int b = b0; b < b1; b++) {
+    const int v = cnt[b];
+    cnt[b] = run;
+    run += v;
+  }
+  __syncthreads();
+  for (int q = tid; q < L.y; q += 256) {
+    const int b = rank[lib_rows[L.x + q]] >> sh;
+    scan_pos[L.x + atomicAdd(&cnt[b], 1)] = q;
+  }
+}
+
 } // namespace
 
 void fill_f64(double* p, long long n, double v, cudaStream_t s)
@@ -91,6 +140,14 @@ void fill_i32(int* p, long long n, int v, cudaStream_t s)
 {
   if (n > 0)
     fill_i32_kernel<<<grid_for(n), 256, 0, s>>>(p, n, v);
+}
+
+void launch_spatial_order(const int* lib_rows, const int* rank, int sh, int nb, const int2* lists, int n_lists,
+                          int* scan_pos, cudaStream_t s)
+{
+  if (n_lists > 0)
+    spatial_order_kernel<<<n_lists, 256, (size_t)(nb + 256) * sizeof(int), s>>>(lib_rows, rank, sh, nb, lists,
+                                                                                  scan_pos);
 }
 
 void launch_tile_boxes(const int* lib_rows, const int* scan_pos, const float* F32, int rs, int ea, const int4* subtiles,
