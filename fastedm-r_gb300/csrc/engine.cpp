@@ -98,7 +98,6 @@ void Context::reset_timing()
   timing = fedm_timing{};
   timing.mixed_form = -1;
   lane_orders.clear();  // list and manifold addresses are reused by later calls
-  spatial_ranks.clear();
 }
 
 namespace {
@@ -221,39 +220,77 @@ std::vector<int> morton_lane_order(const double* F, int Ea, const int* rows, int
 
 namespace {
 
-// Every manifold row's rank in the Morton order of its first four
-// coordinates (8 bits each over the range of the rows that have them all);
-// rows with a missing or non-finite one come last.  Computed once per
-// manifold and call.
+// Every manifold row's place in a Morton order of its first four
+// coordinates, at the resolution of cells: the coordinates are quantised
+// over the range of the rows that have them all (5 bits each for four, 7
+// for three, 10 for two or one), and a row's rank is the number of rows in
+// cells of smaller Morton index, so the rows of one cell share it.  A cell
+// histogram and its prefix sums give it in O(n), without a sort; rows with a
+// missing or non-finite coordinate come last.  Computed once per manifold
+// and call.
 const std::vector<int>& spatial_rank(Context& ctx, const double* F, int n, int Ea)
 {
   auto it = ctx.spatial_ranks.find(F);
-  if (it != ctx.spatial_ranks.end())
-    return it->second;
+  if (it != ctx.spatial_ranks.end() && it->second.first == ctx.series_gen)
+    return it->second.second;
   const int D = std::min(Ea, 4);
-  std::vector<int> rows;
-  rows.reserve(n);
-  for (int i = 0; i < n; i++) {
-    bool ok = true;
-    for (int j = 0; j < D && ok; j++) {
-      const double v = F[(size_t)i * Ea + j];
-      ok = v != MISSING_D && std::isfinite(v);
-    }
-    if (ok)
-      rows.push_back(i);
-  }
-  std::vector<int> rank(n, 0);
-  const std::vector<int> order = morton_lane_order(F, Ea, rows.data(), (int)rows.size(), 4);
-  std::vector<uint8_t> seen(n, 0);
-  int r = 0;
-  for (int s = 0; s < (int)order.size(); s++) {
-    rank[rows[order[s]]] = r++;
-    seen[rows[order[s]]] = 1;
-  }
+  const int bits = D == 4 ? 5 : (D == 3 ? 7 : 10);
+  double lo[4] = { INFINITY, INFINITY, INFINITY, INFINITY }, hi[4] = { -INFINITY, -INFINITY, -INFINITY, -INFINITY };
+  std::vector<uint8_t> ok(n, 1);
   for (int i = 0; i < n; i++)
-    if (!seen[i])
-      rank[i] = r++;
-  return ctx.spatial_ranks.emplace(F, std::move(rank)).first->second;
+    for (int j = 0; j < D; j++) {
+      const double v = F[(size_t)i * Ea + j];
+      if (v == MISSING_D || !std::isfinite(v)) {
+        ok[i] = 0;
+        break;
+      }
+      lo[j] = std::min(lo[j], v);
+      hi[j] = std::max(hi[j], v);
+    }
+  const double top = (double)((1 << bits) - 1);
+  double scale[4];
+  for (int j = 0; j < D; j++)
+    scale[j] = hi[j] > lo[j] ? top / (hi[j] - lo[j]) : 0.0;
+  auto spread2 = [](uint32_t v) {
+    v &= 0x3ff;
+    v = (v | (v << 8)) & 0x00ff00ff;
+    v = (v | (v << 4)) & 0x0f0f0f0f;
+    v = (v | (v << 2)) & 0x33333333;
+    v = (v | (v << 1)) & 0x55555555;
+    return v;
+  };
+  const size_t ncell = (size_t)1 << (bits * D);
+  std::vector<uint32_t> cell(n);
+  std::vector<int> cnt(ncell + 1, 0);
+  int nok = 0;
+  for (int i = 0; i < n; i++) {
+    if (!ok[i])
+      continue;
+    uint32_t q[4] = { 0, 0, 0, 0 };
+    for (int j = 0; j < D; j++)
+      q[j] = (uint32_t)std::min(top, std::max(0.0, std::floor((F[(size_t)i * Ea + j] - lo[j]) * scale[j])));
+    uint32_t key;
+    if (D == 4)
+      key = spread4(q[0]) | (spread4(q[1]) << 1) | (spread4(q[2]) << 2) | (spread4(q[3]) << 3);
+    else if (D == 3)
+      key = spread3(q[0]) | (spread3(q[1]) << 1) | (spread3(q[2]) << 2);
+    else if (D == 2)
+      key = spread2(q[0]) | (spread2(q[1]) << 1);
+    else
+      key = q[0];
+    cell[i] = key;
+    cnt[key + 1]++;
+    nok++;
+  }
+  for (size_t c = 0; c < ncell; c++)
+    cnt[c + 1] += cnt[c];
+  std::vector<int> rank(n);
+  for (int i = 0; i < n; i++)
+    rank[i] = ok[i] ? cnt[cell[i]] : nok;
+  auto& slot = ctx.spatial_ranks[F];
+  slot.first = ctx.series_gen;
+  slot.second = std::move(rank);
+  return slot.second;
 }
 
 } // namespace
@@ -1717,6 +1754,8 @@ void sync_series(Context& ctx, const Generator& g, const RowTables& rt)
   auto& c = ctx.series;
   if (!ctx.series_cache || ctx.host_manifold) {
     c = Context::SeriesCache{};
+    ctx.series_gen++;
+    ctx.spatial_ranks.clear();
     return;
   }
   std::vector<double> scalars = { (double)g.n, (double)g.tau, g.dt ? 1.0 : 0.0, g.reldt ? 1.0 : 0.0, g.dt_weight,
@@ -1730,6 +1769,8 @@ void sync_series(Context& ctx, const Generator& g, const RowTables& rt)
       same_bits(c.extras, extras) && same_bits(c.point_time, rt.point_time) && same_bits(c.obs, g.obs) &&
       same_bits(c.target_row, rt.target_row) && same_bits(c.panel, panel))
     return;
+  ctx.series_gen++;
+  ctx.spatial_ranks.clear();
   c.valid = true;
   c.scalars = std::move(scalars);
   c.x = g.x;

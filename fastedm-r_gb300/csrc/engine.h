@@ -77,9 +77,13 @@ public:
   // of 2 048 to 262 144 rows, scanned in a Morton order of their rows with
   // tiles that no point of a work item can use skipped; the same bits):
   // on by default, FEDM_PRUNE=0 turns it off.  spatial_ranks: per manifold
-  // of the current call, every row's rank in that order.
+  // buffer, every row's rank in that order, with the series generation it
+  // was computed for (series_gen changes whenever the manifold buffers may
+  // hold another series, so ranks are reused only across calls on the same
+  // series).
   bool prune = true;
-  std::map<const void*, std::vector<int>> spatial_ranks;
+  long long series_gen = 0;
+  std::map<const void*, std::pair<long long, std::vector<int>>> spatial_ranks;
   // The split S-map (MIXED_SPLIT): a second stream for the solves, the
   // scan's and the solver's resident CTAs per SM (FEDM_SPLIT_SCAN_CTAS,
   // FEDM_SPLIT_SOLVE_CTAS) and the points per chunk of the pipeline.

@@ -336,6 +336,22 @@ def test_spatial_scan_keeps_bits(algorithm, k, monkeypatch):
             assert np.array_equal(g["coeffs"], f["coeffs"], equal_nan=True)
         assert tf["scanned_pairs"] == tf["distance_pairs"]
         assert 0 < tg["scanned_pairs"] < tf["scanned_pairs"]
+        # coprediction: the points come from the co_x manifold, the tile
+        # boxes from the library's
+        co = np.roll(w["x"], 11)
+        gc = fedm.edm(w["t"], w["x"], w["y"], ctx=pruned, copredict=co, saveCoPredictions=True, **kw)
+        fc = fedm.edm(w["t"], w["x"], w["y"], ctx=plain, copredict=co, saveCoPredictions=True, **kw)
+        assert np.array_equal(gc["copredStats"]["rho"], fc["copredStats"]["rho"], equal_nan=True)
+        assert np.array_equal(gc["copredictions"], fc["copredictions"], equal_nan=True)
+        # heavy ties: a series quantised to 40 levels repeats rows exactly,
+        # so zero distances and equal FP32 values at the C-th slot abound
+        xq = np.round(w["x"] * 40) / 40
+        yq = np.round(w["y"] * 40) / 40
+        gq = fedm.edm(w["t"], xq, yq, ctx=pruned, **kw)
+        fq = fedm.edm(w["t"], xq, yq, ctx=plain, **kw)
+        assert gq["rc"] == fq["rc"]
+        assert np.array_equal(gq["stats"]["rho"], fq["stats"]["rho"], equal_nan=True)
+        assert np.array_equal(gq["predictions"], fq["predictions"], equal_nan=True)
         # neighbour lists of one large task through the task seam
         a = fedm.normalise(w["t"], w["x"], w["y"], E=4, theta=1.0, algorithm=algorithm)
         lib = np.zeros(len(w["t"]), bool)
