@@ -2263,9 +2263,78 @@ int host_plan(const fedm_args& a, int max_tasks, int* task_E, int* task_k, int* 
 }
 
 // ------------------------------------------------------ single-task seam
+namespace {
+
+// Outputs of the task seam's sizes pass, for the outputs pass that follows.
+struct TaskMemo
+{
+  std::string key;
+  TaskOut out;
+  int n_pred = 0, n_lib = 0, e_actual = 0;
+  bool force_compute = true;
+  int n_thetas = 0;
+  fedm_timing timing{};
+};
+
+// Every input of a task on the seam, as bytes: the arguments' scalars (with
+// their pointers cleared) and the contents of their arrays, the task's masks
+// and settings, and the context's precision.  Equal keys give equal outputs.
+std::string task_key(const Context& ctx, const fedm_args& a, const fedm_task_io& io)
+{
+  std::string k;
+  auto put = [&](const void* p, size_t bytes) {
+    k.append(reinterpret_cast<const char*>(&bytes), sizeof bytes);
+    if (p && bytes)
+      k.append(static_cast<const char*>(p), bytes);
+  };
+  const size_t n = (size_t)std::max(a.n, 0);
+  fedm_args s{};
+  std::memcpy(&s, &a, sizeof s);
+  s.t = s.x = s.y = s.co_x = s.extras = s.thetas = s.panel_weights = nullptr;
+  s.panel = s.Es = s.libs = nullptr;
+  put(&s, sizeof s);
+  put(a.t, n * 8);
+  put(a.x, n * 8);
+  put(a.y, a.y ? n * 8 : 0);
+  put(a.panel, a.panel ? n * 4 : 0);
+  put(a.co_x, a.co_x ? n * 8 : 0);
+  put(a.extras, a.extras ? (size_t)std::max(a.num_extras, 0) * n * 8 : 0);
+  put(a.Es, a.Es ? (size_t)std::max(a.nE, 0) * 4 : 0);
+  put(a.thetas, a.thetas ? (size_t)std::max(a.n_thetas, 0) * 8 : 0);
+  put(a.libs, a.libs ? (size_t)std::max(a.n_libs, 0) * 4 : 0);
+  put(a.panel_weights, a.panel_weights ? (size_t)std::max(a.n_panel_weights, 0) * a.n_panel_weights * 8 : 0);
+  put(io.library_rows, io.library_rows ? n : 0);
+  put(io.prediction_rows, io.prediction_rows ? n : 0);
+  const int sc[6] = { io.E, io.k, io.copredict, io.distance, io.force_compute, ctx.precision };
+  put(sc, sizeof sc);
+  put(&io.aspect_ratio, sizeof io.aspect_ratio);
+  return k;
+}
+
+int write_task_outputs(const TaskOut& to, fedm_task_io& io, int nth, bool force_compute);
+
+} // namespace
+
 int run_task(Context& ctx, const fedm_args& a, fedm_task_io& io)
 {
   const double t0 = now_ms();
+  const bool sizes_only = io.predictions == nullptr;
+  std::string key = task_key(ctx, a, io);
+  if (!sizes_only && ctx.task_memo) {
+    // the outputs pass after a sizes pass on the same inputs
+    std::shared_ptr<TaskMemo> memo = std::static_pointer_cast<TaskMemo>(ctx.task_memo);
+    ctx.task_memo.reset();
+    if (memo->key == key) {
+      ctx.timing = memo->timing;
+      ctx.timing.host_ms += now_ms() - t0;
+      io.n_pred = memo->n_pred;
+      io.n_lib = memo->n_lib;
+      io.e_actual = memo->e_actual;
+      io.total_nn = memo->out.nn_offsets.empty() ? 0 : memo->out.nn_offsets.back();
+      return write_task_outputs(memo->out, io, memo->n_thetas, memo->force_compute);
+    }
+  }
+  ctx.task_memo.reset();
   ctx.reset_timing();
   ck(cudaSetDevice(ctx.device), "cudaSetDevice");
   Prepared P;
@@ -2290,7 +2359,6 @@ int run_task(Context& ctx, const fedm_args& a, fedm_task_io& io)
   std::vector<int> L = lib_rows_of(lm, rt), Pl = rows_of(pm);
   const int Ea = gen.E_actual(io.E);
   const int nth = (int)o.thetas.size();
-  const bool sizes_only = io.predictions == nullptr;
   Task t;
   t.E = io.E;
   t.k = io.k;
@@ -2318,7 +2386,7 @@ int run_task(Context& ctx, const fedm_args& a, fedm_task_io& io)
     set_wasserstein_shape(job, gen, io.E);
     run_group(ctx, o, tasks, drows, job, outs);
   }
-  const TaskOut& to = outs[0];
+  TaskOut& to = outs[0];
   io.n_pred = (int)Pl.size();
   io.n_lib = (int)L.size();
   io.e_actual = Ea;
@@ -2326,8 +2394,28 @@ int run_task(Context& ctx, const fedm_args& a, fedm_task_io& io)
   ctx.timing.host_ms = now_ms() - t0;
   ctx.timing.predictions = (long long)Pl.size() * nth;
   ctx.timing.distance_pairs = (long long)Pl.size() * (long long)L.size();
-  if (sizes_only)
+  if (sizes_only) {
+    auto memo = std::make_shared<TaskMemo>();
+    memo->key = std::move(key);
+    memo->out = std::move(to);
+    memo->n_pred = io.n_pred;
+    memo->n_lib = io.n_lib;
+    memo->e_actual = io.e_actual;
+    memo->force_compute = o.force_compute;
+    memo->n_thetas = nth;
+    memo->timing = ctx.timing;
+    ctx.task_memo = memo;
     return RC_SUCCESS;
+  }
+  return write_task_outputs(to, io, nth, o.force_compute);
+}
+
+namespace {
+
+// The task seam's outputs (src/edm.cpp:598-610 and 730-813 for the return
+// codes), copied into the caller's buffers.
+int write_task_outputs(const TaskOut& to, fedm_task_io& io, int nth, bool force_compute)
+{
   const int np = io.n_pred;
   std::copy(to.pred_all.begin(), to.pred_all.end(), io.predictions);
   if (io.coeffs)
@@ -2338,7 +2426,7 @@ int run_task(Context& ctx, const fedm_args& a, fedm_task_io& io)
     for (int th = 0; th < nth; th++) {
       int code = 0;
       if (!made)
-        code = th == 0 ? (o.force_compute ? 0 : 503) : 8000;
+        code = th == 0 ? (force_compute ? 0 : 503) : 8000;
       if (io.rc)
         io.rc[(size_t)th * np + i] = code;
     }
@@ -2359,5 +2447,7 @@ int run_task(Context& ctx, const fedm_args& a, fedm_task_io& io)
       io.stats_mae[th] = to.mae[th];
   return to.rc;
 }
+
+} // namespace
 
 } // namespace fedm

@@ -4,6 +4,7 @@
 
 #include <array>
 #include <map>
+#include <memory>
 #include <set>
 #include <string>
 #include <tuple>
@@ -64,6 +65,11 @@ public:
     std::set<std::pair<int, bool>> built;    // (E, co_x) manifolds built from it
   } series;
   bool series_cache = true;
+  // The task seam's sizes pass (fedm_run_task with null outputs) keeps its
+  // task's outputs and timing here; the outputs pass that follows with the
+  // same inputs (the same bytes) copies them instead of running the task
+  // again.  Opaque to the header (engine.cpp's TaskMemo).
+  std::shared_ptr<void> task_memo;
   // Lane order of the one-point mixed kernels: 1 (default) points of a work
   // item in Morton order of their first four manifold coordinates (three
   // when E_a < 4), 2 of their first three, 0 list order

@@ -638,6 +638,55 @@ def test_series_kept_on_the_device_across_calls(ctx):
     fresh_ctx.close()
 
 
+def test_task_seam_outputs_pass_reuses_only_its_own_sizes_pass():
+    """fedm_run_task's sizes pass keeps its task's outputs for the outputs
+    pass that follows on the same inputs (one run of the task instead of
+    two).  An outputs pass on other inputs runs its own task: here the sizes
+    pass is for k = 4 and the outputs pass for k = 6, whose results must be
+    those of a plain k = 6 call."""
+    import ctypes as C
+
+    t, x, _ = workloads.coupled_logistic(900, seed=71)
+    ctx = fedm.Context(0)
+    try:
+        a = fedm.normalise(t, x, E=3, theta=[0.5, 2.0])
+        lib = np.zeros(900, bool)
+        lib[:450] = True
+        pred = ~lib
+        want = ctx.run_task(a, lib, pred, 3, 6)
+        keep = []
+        s = fedm.make_args(a, keep)
+        lr = np.ascontiguousarray(lib.astype(np.uint8))
+        pr = np.ascontiguousarray(pred.astype(np.uint8))
+
+        def io_for(k):
+            io = fedm.TaskIO()
+            io.library_rows, io.prediction_rows = lr.ctypes.data, pr.ctypes.data
+            io.E, io.k, io.copredict, io.distance, io.force_compute = 3, k, 0, 1, 1
+            return io
+
+        lib_so = ctx.lib
+        assert lib_so.fedm_run_task(ctx.h, C.byref(s), C.byref(io_for(4))) == 0
+        io6 = io_for(6)
+        assert lib_so.fedm_run_task(ctx.h, C.byref(s), C.byref(io6)) == 0  # sizes of k = 6 (a new task)
+        np_, tot = io6.n_pred, io6.total_nn
+        out = dict(predictions=np.zeros(2 * np_), coeffs=np.zeros(np_ * 4), rc=np.zeros(2 * np_, np.int32),
+                   kused=np.zeros(np_, np.int32), nn_offsets=np.zeros(np_ + 1, np.int32),
+                   nn_idx=np.zeros(tot, np.int32), nn_dist=np.zeros(tot), stats_rho=np.zeros(2), stats_mae=np.zeros(2))
+        for key, arr in out.items():
+            setattr(io6, key, arr.ctypes.data)
+        # a sizes pass of another task in between: the outputs pass below must
+        # not take its outputs
+        assert lib_so.fedm_run_task(ctx.h, C.byref(s), C.byref(io_for(4))) == 0
+        lib_so.fedm_run_task(ctx.h, C.byref(s), C.byref(io6))
+        assert np.array_equal(out["predictions"].reshape(2, np_), want["predictions"])
+        assert np.array_equal(out["nn_idx"], want["nn_idx"])
+        assert np.array_equal(out["kused"], want["kused"])
+        assert np.array_equal(out["stats_rho"], want["stats_rho"])
+    finally:
+        ctx.close()
+
+
 def test_concurrent_contexts_share_the_gpu():
     """Two contexts driven from two host threads at once -- a simplex and an
     S-map CCM call, their mixed kernels capped at 1 and 5 resident CTAs per
