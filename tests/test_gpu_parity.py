@@ -148,6 +148,46 @@ def test_empty_library(ctx):
     assert np.all(g["kused"] == -(2**31))
 
 
+@pytest.mark.parametrize("series", ["all_missing", "one_value", "constant", "shorter_than_E"])
+@pytest.mark.parametrize("algorithm", ["simplex", "smap"])
+def test_degenerate_series(ctx, series, algorithm):
+    """edm() on series that leave nothing or almost nothing to predict: no
+    observed value, a single one, a constant series (every distance is zero
+    and excluded), four points for E = 3.  Return codes, k ranges, NA
+    patterns and statistics as the oracle's run_command gives them."""
+    t = np.arange(1, 41, dtype=float)
+    x = {
+        "all_missing": np.full(40, np.nan),
+        "one_value": np.where(t == 7, 0.3, np.nan),
+        "constant": np.full(40, 0.5),
+        "shorter_than_E": None,
+    }[series]
+    if x is None:
+        t, x = np.arange(1, 5, dtype=float), np.array([0.1, 0.4, 0.2, 0.9])
+    kw = dict(E=3, algorithm=algorithm, savePredictions=True)
+    compare(fedm.edm(t, x, ctx=ctx, **kw), edm_oracle.oracle_edm(t, x, **kw))
+
+
+@pytest.mark.parametrize("algorithm", ["simplex", "smap"])
+def test_degenerate_tasks(ctx, algorithm):
+    """Single tasks on degenerate masks, bit-exact: an empty prediction set;
+    a constant series on raw masks, where the only valid neighbour is the
+    first library row with its lag missing (a coordinate of 1e100); the same
+    series on usable rows, where every distance is zero and no forecast is
+    made."""
+    t = np.arange(1, 41, dtype=float)
+    a = edm_oracle.normalise(t, np.sin(t), E=2, algorithm=algorithm)
+    g, o = _task_pair(ctx, a, np.ones(40, bool), np.zeros(40, bool), 2, 3)
+    assert g["n_pred"] == 0
+    a = edm_oracle.normalise(t, np.full(40, 0.5), E=2, theta=[0.0, 1.0], algorithm=algorithm)
+    first = np.arange(40) < 20
+    g, o = _task_pair(ctx, a, first, ~first, 2, 3)
+    assert np.all(g["kused"] == 1)
+    usable = fedm.host_usable(a, 2)
+    g, o = _task_pair(ctx, a, first & usable, ~first & usable, 2, 3)
+    assert np.all(np.isnan(g["predictions"]) | (g["predictions"] == 1e100))
+
+
 @pytest.mark.parametrize("distance", [0, 1])
 def test_missing_panels_l1(ctx, distance):
     rng = np.random.default_rng(5)

@@ -129,3 +129,36 @@ def test_wasserstein_wider_embeddings_rejected_cleanly(ctx):
     lib, pred = _masks(100, 50)
     with pytest.raises(RuntimeError):
         ctx.run_task(a, lib, pred, 17, 18, distance=2)
+
+
+@pytest.mark.parametrize("algorithm,k", [("simplex", 6), ("smap", 7)])
+def test_wasserstein_full_size(ctx, algorithm, k):
+    """The benchmark's shape: T = 4 000, E = 5, library the first 2 000 rows,
+    every 10th of the last 2 000 rows predicted, against the oracle (200
+    points x 2 000 library rows of 5 x 5 transport problems).  Neighbour
+    lists identical, distances within 1e-14.  Where a point's neighbour
+    distances are the same bits, its forecasts are the same bits too (the
+    forecast stage is the exact path's); elsewhere simplex forecasts are
+    within 1e-12, and S-map forecasts from 7 neighbours (their normal
+    equations are ill-conditioned) are only counted."""
+    t, x, _ = workloads.coupled_logistic(4000, seed=61)
+    lib = np.zeros(4000, bool)
+    lib[:2000] = True
+    pred = np.zeros(4000, bool)
+    pred[2000::10] = True
+    a = _args(t=t, x=x, E=5, theta=[1.0], algorithm=algorithm)
+    g = ctx.run_task(a, lib, pred, 5, k, distance=2)
+    o = edm_oracle.oracle_task(edm_oracle.normalise(**a["_kw"]), lib, pred, 5, k, distance=2)
+    assert g["n_pred"] == o["n_pred"] == 200 and g["n_lib"] == o["n_lib"]
+    assert g["task_rc"] == o["task_rc"]
+    assert np.array_equal(g["kused"], o["kused"])
+    assert np.array_equal(g["nn_offsets"], o["nn_offsets"])
+    assert np.array_equal(g["nn_idx"], o["nn_idx"])
+    assert np.allclose(g["nn_dist"], o["nn_dist"], rtol=1e-14, atol=0)
+    same = np.array([np.array_equal(g["nn_dist"][s:e].view(np.int64), o["nn_dist"][s:e].view(np.int64))
+                     for s, e in zip(o["nn_offsets"][:-1], o["nn_offsets"][1:])])
+    assert same.sum() > 0
+    gp, op = g["predictions"][0], o["predictions"][0]
+    assert np.array_equal(gp[same].view(np.int64), op[same].view(np.int64))
+    if algorithm == "simplex":
+        assert np.allclose(gp, op, rtol=1e-12, atol=1e-13)
