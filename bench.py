@@ -787,10 +787,11 @@ def config_roofline(name, precision, steps_tm, peaks):
         n = E + 1
         per_pair = 2 * (n * (n + 1) / 2 + n) + 2 * (3 * E + 1) + 4 * n
         flops = per_pair * 50000 * tm["predictions"]
-        return {"kernel": "smap_grad_kernel<6> (three passes per point: distances, normal equations, adjoint sums)",
+        return {"kernel": "smap_grad_kernel<6> (three passes per point: distances, normal equations, adjoint sums; "
+                          "distances and weights cached per warp)",
                 "bound": "fp64_simt", "achieved": flops / (ms * 1e-3) / 1e12, "peak": peaks["fp64_fma"],
                 "unit": "TFLOP/s", "frac": flops / (ms * 1e-3) / 1e12 / peaks["fp64_fma"], "traffic": None,
-                "kernel_ms_per_step": ms, "launches_per_step": 1,
+                "kernel_ms_per_step": ms, "launches_per_step": 2,
                 "work": f"{per_pair:.0f} flops per (prediction, library row): the normal equations "
                         "2((E+1)(E+2)/2 + E+1), the adjoint sums 2(3E+1) and the residual and g.u products 4(E+1)",
                 "peak_source": "measured DFMA rate (fedm_measure_peak kind 1): the adjoint passes use FMA"}

@@ -2114,11 +2114,24 @@ int smap_grad(Context& ctx, const double* lib, const double* lib_t, int n_lib, c
   a.e_actual = e_actual;
   a.backward = dtheta != nullptr;
   a.out = d_out;
+  a.z = (double*)ctx.buf("adj_z", (size_t)n_lib * E * 8);
+  // per-warp slices for the distances and weights of passes 1 and 2, within
+  // a budget: a full persistent grid, or at least half of one, else none
+  {
+    constexpr size_t GRAD_CACHE_BUDGET = (size_t)4 << 30;
+    const long long full = grad_cache_warps(e_actual, ctx.num_sms);
+    const long long fit = (long long)(GRAD_CACHE_BUDGET / ((size_t)n_lib * 16));
+    a.cache_warps = std::min(full, fit);
+    if (a.cache_warps * 2 >= full)
+      a.cache = (double*)ctx.buf("adj_cache", (size_t)a.cache_warps * 2 * n_lib * 8);
+    else
+      a.cache_warps = 0;
+  }
   cudaEvent_t e0, e1;
   ck(cudaEventCreate(&e0), "event");
   ck(cudaEventCreate(&e1), "event");
   ck(cudaEventRecord(e0, s), "event");
-  launch_smap_grad(a, s);
+  launch_smap_grad(a, ctx.num_sms, s);
   ctx.check("smap_grad");
   ck(cudaEventRecord(e1, s), "event");
   std::vector<double> out((size_t)n_pred * (E + 3));
@@ -2187,8 +2200,8 @@ int smap_grad(Context& ctx, const double* lib, const double* lib_t, int n_lib, c
   ctx.timing.device_ms = ms;
   ctx.timing.knn_kernel_ms = ms;
   ctx.timing.knn_launches = 1;
-  ctx.timing.kernel_launches = 1;
-  ctx.timing.distance_pairs = (long long)n_pred * n_lib * (dtheta ? 3 : 2);
+  ctx.timing.kernel_launches = 2;  // the scaled library, the passes
+  ctx.timing.distance_pairs = (long long)n_pred * n_lib * (a.cache ? 1 : dtheta ? 3 : 2);
   ctx.timing.predictions = n_pred;
   ctx.timing.host_ms = now_ms() - t0;
   return RC_SUCCESS;

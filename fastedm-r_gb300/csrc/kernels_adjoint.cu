@@ -26,7 +26,18 @@
 // The passes therefore use what the FP64 pipe does cheaply: one reciprocal
 // of d per row instead of a division per lag, a2 = exp(-2 theta d / mu) in
 // one call, and fused multiply-adds for the normal equations and the
-// adjoint sums.  The weights are recomputed in pass 3, not stored.
+// adjoint sums.
+//
+// The FP64 pipe bounds the kernel, and HBM has room: the grid is persistent
+// (one warp per point at a time, points strided over the warps) and each
+// warp owns a slice of 2 n_lib doubles of device memory.  Pass 1 stores d_i
+// there and pass 2 stores a_i^2, so passes 2 and 3 read them instead of
+// recomputing the distance (and, in pass 3, the exponential): about a third
+// of the FP64 instructions per (point, library row).  The scaled library
+// z = w * m is formed once per call.  The cached values are the ones the
+// passes would recompute, so the results are the same bits.  A library too
+// large for the slices' budget runs the same kernel without them.
+#include <algorithm>
 #include <cfloat>
 
 #include "kernels.h"
@@ -37,6 +48,7 @@ namespace fedm {
 namespace {
 
 constexpr unsigned FULL = 0xffffffffu;
+constexpr int GRAD_NT = 128;  // threads per CTA: four warps, one point each at a time
 
 __device__ __forceinline__ double wsum(double v)
 {
@@ -45,16 +57,21 @@ __device__ __forceinline__ double wsum(double v)
   return v;
 }
 
-template<int EA>
-__global__ void __launch_bounds__(128) smap_grad_kernel(AdjointParams a)
+// z = w * m for every library row: the product pass 1 forms for its
+// distance, so the distances keep their bits
+__global__ void scale_rows_kernel(const double* lib, const double* w, long long n, int ea, double* z)
+{
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    z[i] = mul(w[i % ea], lib[i]);
+}
+
+// The three passes for prediction point pnt, by one warp.  cache: this
+// warp's slice (d at [0, n_lib), a^2 at [n_lib, 2 n_lib)) when CACHE.
+template<int EA, bool CACHE>
+__device__ __forceinline__ void grad_point(const AdjointParams& a, long long pnt, int lane, double* cache)
 {
   constexpr int n = EA + 1;
   constexpr int NA = n * (n + 1) / 2;
-  const int lane = threadIdx.x & 31;
-  const int wpb = blockDim.x >> 5;
-  const int pnt = blockIdx.x * wpb + (threadIdx.x >> 5);
-  if (pnt >= a.n_pred)
-    return;
   double w[EA], y[EA], zp[EA];
 #pragma unroll
   for (int j = 0; j < EA; j++) {
@@ -62,6 +79,19 @@ __global__ void __launch_bounds__(128) smap_grad_kernel(AdjointParams a)
     y[j] = a.pred[(size_t)pnt * EA + j];
     zp[j] = mul(w[j], y[j]);
   }
+  // the distance of row i in the reference's operation order (unfused), so
+  // at w = 1 it is the same bits as src/distances.cpp:176-225; 0 for an
+  // excluded (zero) distance
+  auto distance = [&](int i, double* diff) {
+    const double* z = a.z + (size_t)i * EA;
+    double s = 0.0;
+#pragma unroll
+    for (int j = 0; j < EA; j++) {
+      diff[j] = sub(z[j], zp[j]);
+      s = add(s, mul(diff[j], diff[j]));
+    }
+    return s != 0 ? __dsqrt_rn(s) : 0.0;
+  };
   // pass 1: distances, their mean and its derivative
   double sd = 0, dmu[EA];
   int cnt = 0;
@@ -70,16 +100,11 @@ __global__ void __launch_bounds__(128) smap_grad_kernel(AdjointParams a)
     dmu[j] = 0;
   for (int i = lane; i < a.n_lib; i += 32) {
     const double* m = a.lib + (size_t)i * EA;
-    // distance in the reference's operation order (unfused), so at w = 1 it
-    // is the same bits as src/distances.cpp:176-225
-    double diff[EA], s = 0.0;
-#pragma unroll
-    for (int j = 0; j < EA; j++) {
-      diff[j] = sub(mul(w[j], m[j]), zp[j]);
-      s = add(s, mul(diff[j], diff[j]));
-    }
-    if (s != 0) {
-      const double d = __dsqrt_rn(s);
+    double diff[EA];
+    const double d = distance(i, diff);
+    if constexpr (CACHE)
+      cache[i] = d;
+    if (d != 0) {
       const double inv = __drcp_rn(d);
       sd += d;
       cnt++;
@@ -104,18 +129,24 @@ __global__ void __launch_bounds__(128) smap_grad_kernel(AdjointParams a)
   for (int e = 0; e < n; e++)
     b[e] = 0;
   for (int i = lane; i < a.n_lib; i += 32) {
-    const double* m = a.lib + (size_t)i * EA;
-    double u[n], s = 0.0;
+    double d;
+    if constexpr (CACHE) {
+      d = cache[i];
+    } else {
+      double diff[EA];
+      d = distance(i, diff);
+    }
+    if (d == 0)
+      continue;
+    const double a2 = exp(c2 * d);
+    if constexpr (CACHE)
+      cache[a.n_lib + i] = a2;
+    const double* z = a.z + (size_t)i * EA;
+    double u[n];
     u[0] = 1.0;
 #pragma unroll
-    for (int j = 0; j < EA; j++) {
-      u[j + 1] = mul(w[j], m[j]);
-      const double df = sub(u[j + 1], zp[j]);
-      s = add(s, mul(df, df));
-    }
-    if (s == 0)
-      continue;
-    const double a2 = exp(c2 * __dsqrt_rn(s));
+    for (int j = 0; j < EA; j++)
+      u[j + 1] = z[j];
     const double t = a.lib_t[i];
     int e = 0;
 #pragma unroll
@@ -180,18 +211,27 @@ __global__ void __launch_bounds__(128) smap_grad_kernel(AdjointParams a)
     R[j] = S[j] = Tt[j] = 0;
   for (int i = lane; i < a.n_lib; i += 32) {
     const double* m = a.lib + (size_t)i * EA;
-    double u[n], diff[EA], s = 0.0;
+    const double* z = a.z + (size_t)i * EA;
+    double diff[EA], d, a2;
+    if constexpr (CACHE) {
+      d = cache[i];
+      if (d == 0)
+        continue;
+      a2 = cache[a.n_lib + i];
+#pragma unroll
+      for (int j = 0; j < EA; j++)
+        diff[j] = sub(z[j], zp[j]);
+    } else {
+      d = distance(i, diff);
+      if (d == 0)
+        continue;
+      a2 = exp(c2 * d);
+    }
+    double u[n];
     u[0] = 1.0;
 #pragma unroll
-    for (int j = 0; j < EA; j++) {
-      u[j + 1] = mul(w[j], m[j]);
-      diff[j] = sub(u[j + 1], zp[j]);
-      s = add(s, mul(diff[j], diff[j]));
-    }
-    if (s == 0)
-      continue;
-    const double d = __dsqrt_rn(s);
-    const double a2 = exp(c2 * d);
+    for (int j = 0; j < EA; j++)
+      u[j + 1] = z[j];
     double su = 0, uc = 0;
 #pragma unroll
     for (int k = 0; k < n; k++) {
@@ -228,22 +268,69 @@ __global__ void __launch_bounds__(128) smap_grad_kernel(AdjointParams a)
   }
 }
 
+template<int EA, bool CACHE>
+__global__ void __launch_bounds__(GRAD_NT, 3) smap_grad_kernel(AdjointParams a)
+{
+  const int lane = threadIdx.x & 31;
+  const long long warp = (long long)blockIdx.x * (GRAD_NT / 32) + (threadIdx.x >> 5);
+  const long long warps = (long long)gridDim.x * (GRAD_NT / 32);
+  double* cache = CACHE ? a.cache + warp * 2 * a.n_lib : nullptr;
+  for (long long pnt = warp; pnt < a.n_pred; pnt += warps)
+    grad_point<EA, CACHE>(a, pnt, lane, cache);
+}
+
+template<int EA>
+void launch_grad(const AdjointParams& a, int num_sms, cudaStream_t s)
+{
+  int per_sm = 0;
+  if (a.cache)
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, smap_grad_kernel<EA, true>, GRAD_NT, 0);
+  else
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, smap_grad_kernel<EA, false>, GRAD_NT, 0);
+  long long blocks = (long long)num_sms * std::max(per_sm, 1);
+  blocks = std::min(blocks, (long long)(a.n_pred + GRAD_NT / 32 - 1) / (GRAD_NT / 32));
+  if (a.cache)
+    blocks = std::min(blocks, a.cache_warps / (GRAD_NT / 32));
+  if (blocks < 1)
+    return;
+  if (a.cache)
+    smap_grad_kernel<EA, true><<<(int)blocks, GRAD_NT, 0, s>>>(a);
+  else
+    smap_grad_kernel<EA, false><<<(int)blocks, GRAD_NT, 0, s>>>(a);
+}
+
 } // namespace
 
-void launch_smap_grad(const AdjointParams& a, cudaStream_t s)
+int grad_cache_warps(int e_actual, int num_sms)
 {
-  const int blocks = (a.n_pred + 3) / 4;
-  if (blocks <= 0)
+  int per_sm = 0;
+  switch (e_actual) {
+#define FEDM_GRAD_OCC(E)                                                                                     \
+  case E: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, smap_grad_kernel<E, true>, GRAD_NT, 0); break;
+    FEDM_GRAD_OCC(1) FEDM_GRAD_OCC(2) FEDM_GRAD_OCC(3) FEDM_GRAD_OCC(4)
+    FEDM_GRAD_OCC(5) FEDM_GRAD_OCC(6) FEDM_GRAD_OCC(7) FEDM_GRAD_OCC(8)
+#undef FEDM_GRAD_OCC
+    default: break;
+  }
+  return num_sms * std::max(per_sm, 1) * (GRAD_NT / 32);
+}
+
+void launch_smap_grad(const AdjointParams& a, int num_sms, cudaStream_t s)
+{
+  if (a.n_pred <= 0 || a.n_lib <= 0)
     return;
+  const long long n = (long long)a.n_lib * a.e_actual;
+  const int zb = (int)std::min<long long>((n + 255) / 256, (long long)num_sms * 8);
+  scale_rows_kernel<<<zb, 256, 0, s>>>(a.lib, a.w, n, a.e_actual, a.z);
   switch (a.e_actual) {
-    case 1: smap_grad_kernel<1><<<blocks, 128, 0, s>>>(a); break;
-    case 2: smap_grad_kernel<2><<<blocks, 128, 0, s>>>(a); break;
-    case 3: smap_grad_kernel<3><<<blocks, 128, 0, s>>>(a); break;
-    case 4: smap_grad_kernel<4><<<blocks, 128, 0, s>>>(a); break;
-    case 5: smap_grad_kernel<5><<<blocks, 128, 0, s>>>(a); break;
-    case 6: smap_grad_kernel<6><<<blocks, 128, 0, s>>>(a); break;
-    case 7: smap_grad_kernel<7><<<blocks, 128, 0, s>>>(a); break;
-    case 8: smap_grad_kernel<8><<<blocks, 128, 0, s>>>(a); break;
+    case 1: launch_grad<1>(a, num_sms, s); break;
+    case 2: launch_grad<2>(a, num_sms, s); break;
+    case 3: launch_grad<3>(a, num_sms, s); break;
+    case 4: launch_grad<4>(a, num_sms, s); break;
+    case 5: launch_grad<5>(a, num_sms, s); break;
+    case 6: launch_grad<6>(a, num_sms, s); break;
+    case 7: launch_grad<7>(a, num_sms, s); break;
+    case 8: launch_grad<8>(a, num_sms, s); break;
     default: break;
   }
 }
