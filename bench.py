@@ -788,7 +788,7 @@ def config_roofline(name, precision, steps_tm, peaks):
         per_pair = 2 * (n * (n + 1) / 2 + n) + 2 * (3 * E + 1) + 4 * n
         flops = per_pair * 50000 * tm["predictions"]
         return {"kernel": "smap_grad_kernel<6> (three passes per point: distances, normal equations, adjoint sums; "
-                          "distances and weights cached per warp)",
+                          "per-row values cached per warp)",
                 "bound": "fp64_simt", "achieved": flops / (ms * 1e-3) / 1e12, "peak": peaks["fp64_fma"],
                 "unit": "TFLOP/s", "frac": flops / (ms * 1e-3) / 1e12 / peaks["fp64_fma"], "traffic": None,
                 "kernel_ms_per_step": ms, "launches_per_step": 2,

@@ -2115,17 +2115,21 @@ int smap_grad(Context& ctx, const double* lib, const double* lib_t, int n_lib, c
   a.backward = dtheta != nullptr;
   a.out = d_out;
   a.z = (double*)ctx.buf("adj_z", (size_t)n_lib * E * 8);
-  // per-warp slices for the distances and weights of passes 1 and 2, within
-  // a budget: a full persistent grid, or at least half of one, else none
+  // per-warp slices for the per-row values of passes 1 and 2, within a
+  // budget: the highest cache level for which a full persistent grid, or at
+  // least half of one, fits; else none
   {
-    constexpr size_t GRAD_CACHE_BUDGET = (size_t)4 << 30;
+    constexpr size_t GRAD_CACHE_BUDGET = (size_t)8 << 30;
     const long long full = grad_cache_warps(e_actual, ctx.num_sms);
-    const long long fit = (long long)(GRAD_CACHE_BUDGET / ((size_t)n_lib * 16));
-    a.cache_warps = std::min(full, fit);
-    if (a.cache_warps * 2 >= full)
-      a.cache = (double*)ctx.buf("adj_cache", (size_t)a.cache_warps * 2 * n_lib * 8);
-    else
-      a.cache_warps = 0;
+    for (int level = 2; level >= 1 && !a.cache; level--) {
+      const size_t per_row = level == 2 ? 3 + E : 2;
+      const long long fit = (long long)(GRAD_CACHE_BUDGET / ((size_t)n_lib * per_row * 8));
+      if (std::min(full, fit) * 2 >= full) {
+        a.cache_warps = std::min(full, fit);
+        a.cache_level = level;
+        a.cache = (double*)ctx.buf("adj_cache", (size_t)a.cache_warps * per_row * n_lib * 8);
+      }
+    }
   }
   cudaEvent_t e0, e1;
   ck(cudaEventCreate(&e0), "event");

@@ -335,10 +335,12 @@ struct AdjointParams
   int backward;          // 0: r, yhat only; 1: also dyhat/dtheta and dyhat/dw
   double* out;           // [n_pred x (e_actual + 3)]
   double* z;             // [n_lib x e_actual] scratch: the library scaled by w
-  double* cache;         // [cache_warps x 2 n_lib] per-warp distances and weights, or null
+  double* cache;         // [cache_warps x per-row doubles x n_lib] per-warp row values, or null
   long long cache_warps; // warps that own a slice of cache (the grid is capped to them)
+  int cache_level;       // 2: d, a^2, 1/d and e_actual products per row; 1: d and a^2
 };
-// Warps of a full persistent grid of the cached adjoint kernel.
+// Warps of a full persistent grid of the cached adjoint kernel (the levels
+// share one register budget, so one figure serves all of them).
 int grad_cache_warps(int e_actual, int num_sms);
 void launch_smap_grad(const AdjointParams& a, int num_sms, cudaStream_t s);
 void center_to_f32(const double* F, long long n, int Ea, const double* center, float* F32, int stride,

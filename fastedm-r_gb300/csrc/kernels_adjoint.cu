@@ -30,13 +30,14 @@
 //
 // The FP64 pipe bounds the kernel, and HBM has room: the grid is persistent
 // (one warp per point at a time, points strided over the warps) and each
-// warp owns a slice of 2 n_lib doubles of device memory.  Pass 1 stores d_i
-// there and pass 2 stores a_i^2, so passes 2 and 3 read them instead of
-// recomputing the distance (and, in pass 3, the exponential): about a third
-// of the FP64 instructions per (point, library row).  The scaled library
-// z = w * m is formed once per call.  The cached values are the ones the
-// passes would recompute, so the results are the same bits.  A library too
-// large for the slices' budget runs the same kernel without them.
+// warp owns a slice of device memory for its point's per-row values.  At
+// cache level 2 pass 1 stores d_i, 1/d_i and the products
+// (z_ij - z_pj)(m_ij - m_pj), and pass 2 stores a_i^2, so that pass 3 reads
+// them instead of recomputing the distance, the exponential and the products;
+// at level 1 (a library too large for level 2's budget) only d_i and a_i^2
+// are kept; at level 0 (larger still) every pass recomputes.  The scaled
+// library z = w * m is formed once per call.  The cached values are the ones
+// the passes would recompute, so every level gives the same bits.
 #include <algorithm>
 #include <cfloat>
 
@@ -65,11 +66,17 @@ __global__ void scale_rows_kernel(const double* lib, const double* w, long long 
     z[i] = mul(w[i % ea], lib[i]);
 }
 
+// Doubles per library row of a warp's cache slice at each level.
+template<int EA, int CACHE>
+__host__ __device__ constexpr int cache_per_row() { return CACHE == 2 ? 3 + EA : CACHE == 1 ? 2 : 0; }
+
 // The three passes for prediction point pnt, by one warp.  cache: this
-// warp's slice (d at [0, n_lib), a^2 at [n_lib, 2 n_lib)) when CACHE.
-template<int EA, bool CACHE>
+// warp's slice, n_lib rows per array: d, a^2 (level >= 1), then 1/d and the
+// EA products (level 2).
+template<int EA, int CACHE>
 __device__ __forceinline__ void grad_point(const AdjointParams& a, long long pnt, int lane, double* cache)
 {
+  const int nl = a.n_lib;
   constexpr int n = EA + 1;
   constexpr int NA = n * (n + 1) / 2;
   double w[EA], y[EA], zp[EA];
@@ -102,15 +109,21 @@ __device__ __forceinline__ void grad_point(const AdjointParams& a, long long pnt
     const double* m = a.lib + (size_t)i * EA;
     double diff[EA];
     const double d = distance(i, diff);
-    if constexpr (CACHE)
+    if constexpr (CACHE >= 1)
       cache[i] = d;
     if (d != 0) {
       const double inv = __drcp_rn(d);
       sd += d;
       cnt++;
+      if constexpr (CACHE == 2)
+        cache[2 * nl + i] = inv;
 #pragma unroll
-      for (int j = 0; j < EA; j++)
-        dmu[j] = fma(diff[j] * (m[j] - y[j]), inv, dmu[j]);
+      for (int j = 0; j < EA; j++) {
+        const double q = diff[j] * (m[j] - y[j]);
+        if constexpr (CACHE == 2)
+          cache[(3 + j) * nl + i] = q;
+        dmu[j] = fma(q, inv, dmu[j]);
+      }
     }
   }
   const double total = wsum(sd);
@@ -130,7 +143,7 @@ __device__ __forceinline__ void grad_point(const AdjointParams& a, long long pnt
     b[e] = 0;
   for (int i = lane; i < a.n_lib; i += 32) {
     double d;
-    if constexpr (CACHE) {
+    if constexpr (CACHE >= 1) {
       d = cache[i];
     } else {
       double diff[EA];
@@ -139,8 +152,8 @@ __device__ __forceinline__ void grad_point(const AdjointParams& a, long long pnt
     if (d == 0)
       continue;
     const double a2 = exp(c2 * d);
-    if constexpr (CACHE)
-      cache[a.n_lib + i] = a2;
+    if constexpr (CACHE >= 1)
+      cache[nl + i] = a2;
     const double* z = a.z + (size_t)i * EA;
     double u[n];
     u[0] = 1.0;
@@ -212,20 +225,36 @@ __device__ __forceinline__ void grad_point(const AdjointParams& a, long long pnt
   for (int i = lane; i < a.n_lib; i += 32) {
     const double* m = a.lib + (size_t)i * EA;
     const double* z = a.z + (size_t)i * EA;
-    double diff[EA], d, a2;
-    if constexpr (CACHE) {
+    double q[EA], d, a2, inv;
+    if constexpr (CACHE == 2) {
       d = cache[i];
       if (d == 0)
         continue;
-      a2 = cache[a.n_lib + i];
+      a2 = cache[nl + i];
+      inv = cache[2 * nl + i];
 #pragma unroll
       for (int j = 0; j < EA; j++)
-        diff[j] = sub(z[j], zp[j]);
+        q[j] = cache[(3 + j) * nl + i];
     } else {
-      d = distance(i, diff);
-      if (d == 0)
-        continue;
-      a2 = exp(c2 * d);
+      double diff[EA];
+      if constexpr (CACHE == 1) {
+        d = cache[i];
+        if (d == 0)
+          continue;
+        a2 = cache[nl + i];
+#pragma unroll
+        for (int j = 0; j < EA; j++)
+          diff[j] = sub(z[j], zp[j]);
+      } else {
+        d = distance(i, diff);
+        if (d == 0)
+          continue;
+        a2 = exp(c2 * d);
+      }
+      inv = __drcp_rn(d);
+#pragma unroll
+      for (int j = 0; j < EA; j++)
+        q[j] = diff[j] * (m[j] - y[j]);
     }
     double u[n];
     u[0] = 1.0;
@@ -242,10 +271,10 @@ __device__ __forceinline__ void grad_point(const AdjointParams& a, long long pnt
     const double ae = a2 * ei, as = a2 * su;
     const double ase = as * ei;
     Q = fma(ase, d, Q);
-    const double ased = ase * __drcp_rn(d);
+    const double ased = ase * inv;
 #pragma unroll
     for (int j = 0; j < EA; j++) {
-      R[j] = fma(ased, diff[j] * (m[j] - y[j]), R[j]);
+      R[j] = fma(ased, q[j], R[j]);
       S[j] = fma(ae, m[j], S[j]);
       Tt[j] = fma(as, m[j], Tt[j]);
     }
@@ -268,35 +297,40 @@ __device__ __forceinline__ void grad_point(const AdjointParams& a, long long pnt
   }
 }
 
-template<int EA, bool CACHE>
+template<int EA, int CACHE>
 __global__ void __launch_bounds__(GRAD_NT, 3) smap_grad_kernel(AdjointParams a)
 {
   const int lane = threadIdx.x & 31;
   const long long warp = (long long)blockIdx.x * (GRAD_NT / 32) + (threadIdx.x >> 5);
   const long long warps = (long long)gridDim.x * (GRAD_NT / 32);
-  double* cache = CACHE ? a.cache + warp * 2 * a.n_lib : nullptr;
+  double* cache = CACHE ? a.cache + warp * cache_per_row<EA, CACHE>() * (long long)a.n_lib : nullptr;
   for (long long pnt = warp; pnt < a.n_pred; pnt += warps)
     grad_point<EA, CACHE>(a, pnt, lane, cache);
+}
+
+template<int EA, int CACHE>
+void launch_grad_level(const AdjointParams& a, int num_sms, cudaStream_t s)
+{
+  int per_sm = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, smap_grad_kernel<EA, CACHE>, GRAD_NT, 0);
+  long long blocks = (long long)num_sms * std::max(per_sm, 1);
+  blocks = std::min(blocks, (long long)(a.n_pred + GRAD_NT / 32 - 1) / (GRAD_NT / 32));
+  if (CACHE)
+    blocks = std::min(blocks, a.cache_warps / (GRAD_NT / 32));
+  if (blocks < 1)
+    return;
+  smap_grad_kernel<EA, CACHE><<<(int)blocks, GRAD_NT, 0, s>>>(a);
 }
 
 template<int EA>
 void launch_grad(const AdjointParams& a, int num_sms, cudaStream_t s)
 {
-  int per_sm = 0;
-  if (a.cache)
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, smap_grad_kernel<EA, true>, GRAD_NT, 0);
+  if (a.cache && a.cache_level == 2)
+    launch_grad_level<EA, 2>(a, num_sms, s);
+  else if (a.cache && a.cache_level == 1)
+    launch_grad_level<EA, 1>(a, num_sms, s);
   else
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, smap_grad_kernel<EA, false>, GRAD_NT, 0);
-  long long blocks = (long long)num_sms * std::max(per_sm, 1);
-  blocks = std::min(blocks, (long long)(a.n_pred + GRAD_NT / 32 - 1) / (GRAD_NT / 32));
-  if (a.cache)
-    blocks = std::min(blocks, a.cache_warps / (GRAD_NT / 32));
-  if (blocks < 1)
-    return;
-  if (a.cache)
-    smap_grad_kernel<EA, true><<<(int)blocks, GRAD_NT, 0, s>>>(a);
-  else
-    smap_grad_kernel<EA, false><<<(int)blocks, GRAD_NT, 0, s>>>(a);
+    launch_grad_level<EA, 0>(a, num_sms, s);
 }
 
 } // namespace
@@ -306,7 +340,7 @@ int grad_cache_warps(int e_actual, int num_sms)
   int per_sm = 0;
   switch (e_actual) {
 #define FEDM_GRAD_OCC(E)                                                                                     \
-  case E: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, smap_grad_kernel<E, true>, GRAD_NT, 0); break;
+  case E: cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, smap_grad_kernel<E, 2>, GRAD_NT, 0); break;
     FEDM_GRAD_OCC(1) FEDM_GRAD_OCC(2) FEDM_GRAD_OCC(3) FEDM_GRAD_OCC(4)
     FEDM_GRAD_OCC(5) FEDM_GRAD_OCC(6) FEDM_GRAD_OCC(7) FEDM_GRAD_OCC(8)
 #undef FEDM_GRAD_OCC
