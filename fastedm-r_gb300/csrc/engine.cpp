@@ -80,6 +80,8 @@ Context::Context(int dev) : device(dev)
     split_chunk_points = std::max(256LL, std::atoll(v));
   if (const char* v = std::getenv("FEDM_GRAM_TC"))
     gram_tc = std::strcmp(v, "0") != 0;
+  if (const char* v = std::getenv("FEDM_GRAD_CACHE"))
+    grad_cache_max = std::min(2, std::max(0, std::atoi(v)));
   if (const char* v = std::getenv("FEDM_ITEM_ORDER"))
     item_order = std::strcmp(v, "lpt") == 0 ? 0 : 1;
   if (const char* v = std::getenv("FEDM_HOST_MANIFOLD"))
@@ -2121,7 +2123,7 @@ int smap_grad(Context& ctx, const double* lib, const double* lib_t, int n_lib, c
   {
     constexpr size_t GRAD_CACHE_BUDGET = (size_t)8 << 30;
     const long long full = grad_cache_warps(e_actual, ctx.num_sms);
-    for (int level = 2; level >= 1 && !a.cache; level--) {
+    for (int level = ctx.grad_cache_max; level >= 1 && !a.cache; level--) {
       const size_t per_row = level == 2 ? 3 + E : 2;
       const long long fit = (long long)(GRAD_CACHE_BUDGET / ((size_t)n_lib * per_row * 8));
       if (std::min(full, fit) * 2 >= full) {
@@ -2205,6 +2207,7 @@ int smap_grad(Context& ctx, const double* lib, const double* lib_t, int n_lib, c
   ctx.timing.knn_kernel_ms = ms;
   ctx.timing.knn_launches = 1;
   ctx.timing.kernel_launches = 2;  // the scaled library, the passes
+  ctx.timing.grad_cache_level = a.cache ? a.cache_level : 0;
   ctx.timing.distance_pairs = (long long)n_pred * n_lib * (a.cache ? 1 : dtheta ? 3 : 2);
   ctx.timing.predictions = n_pred;
   ctx.timing.host_ms = now_ms() - t0;

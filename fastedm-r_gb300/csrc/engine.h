@@ -100,6 +100,9 @@ public:
   // FAST precision: the k = all S-map's normal equations on the tensor cores
   // (E_a <= 5); FEDM_GRAM_TC=0 keeps the double-float SIMT kernel.
   bool gram_tc = true;
+  // Differentiable S-map: the highest per-warp cache level its kernel may
+  // use (FEDM_GRAD_CACHE=0..2; every level gives the same bits).
+  int grad_cache_max = 2;
   std::map<std::array<int, 3>, int> tuned_forms;
   std::string last_error;
   fedm_timing timing{};

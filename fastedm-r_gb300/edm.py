@@ -76,7 +76,7 @@ class Timing(C.Structure):
         ("mixed_form", C.c_int), ("autotune_probes", C.c_int), ("prep_ms", C.c_double),
         ("manifold_ms", C.c_double), ("scan_flops", C.c_longlong), ("forecast_kernel_ms", C.c_double),
         ("forecast_launches", C.c_int), ("tensor_core_tiles", C.c_int), ("manifold_builds", C.c_int),
-        ("manifolds_reused", C.c_int), ("scanned_pairs", C.c_longlong),
+        ("manifolds_reused", C.c_int), ("scanned_pairs", C.c_longlong), ("grad_cache_level", C.c_int),
     ]
 
 

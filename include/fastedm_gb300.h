@@ -251,6 +251,10 @@ typedef struct fedm_timing {
   long long scanned_pairs;   /* one-point mixed kernels: (prediction, library)
                                 pairs actually scored; spatially ordered
                                 libraries skip tiles no point can use        */
+  int grad_cache_level;      /* differentiable S-map: per-warp cache level of
+                                its kernel (2: distances, weights, 1/d and
+                                per-lag products; 1: distances and weights;
+                                0: none)                                     */
 } fedm_timing;
 
 int fedm_last_timing(const fedm_ctx* ctx, fedm_timing* out);

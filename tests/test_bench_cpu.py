@@ -45,7 +45,7 @@ class FakeContext:
                     fp64_ops=10**10, list_wait_ms=1.0, setup_ms=2.0, finish_ms=0.5, exact_points=1, mixed_form=1,
                     autotune_probes=0, prep_ms=0.3, manifold_ms=0.2, scan_flops=12 * 10**9,
                     forecast_kernel_ms=80.0, forecast_launches=1, tensor_core_tiles=0, manifold_builds=1,
-                    manifolds_reused=0, scanned_pairs=4 * 10**8)
+                    manifolds_reused=0, scanned_pairs=4 * 10**8, grad_cache_level=0)
 
     def close(self):
         pass

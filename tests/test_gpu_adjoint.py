@@ -165,3 +165,33 @@ def test_full_size_gradient(ctx):
     fd = (f(theta + h) - f(theta - h)) / (2 * h)
     assert np.isclose(gt, fd, rtol=1e-4, atol=1e-13), (gt, fd)
     print(f"full-size differentiable S-map: {tm['device_ms']:.1f} ms forward+backward")
+
+
+@pytest.mark.parametrize("e_actual", [2, 6, 8])
+def test_cache_levels_give_the_same_bits(e_actual, monkeypatch):
+    """The kernel keeps each point's per-row values in a per-warp cache
+    (level 2: distances, weights, reciprocals and per-lag products; level 1:
+    distances and weights; level 0: none, every pass recomputes).  The cached
+    values are the ones the passes recompute: every level gives the same
+    bits for the forecasts, the MSE and its gradient."""
+    w = workloads.lorenz_config(seed=8, T=8000)
+    a = fedm.normalise(w["t"], w["x"], E=e_actual, tau=3)
+    F = fedm.host_manifold(a, e_actual)
+    first = (e_actual - 1) * 3
+    lib_rows = np.arange(first, first + 3000)
+    pred_rows = np.arange(first + 3000, first + 3700)
+    lib, lib_t = F[lib_rows], w["x"][lib_rows + 1]
+    pred, pred_t = F[pred_rows], w["x"][pred_rows + 1]
+    wv = np.linspace(0.7, 1.4, e_actual)
+    out = {}
+    for level in (2, 1, 0):
+        monkeypatch.setenv("FEDM_GRAD_CACHE", str(level))
+        c = fedm.Context(0, precision=fedm.PRECISION_FP64)
+        try:
+            mse, gt, gw, _ = c.smap_grad(lib, lib_t, pred, pred_t, 1.5, wv)
+            assert c.timing()["grad_cache_level"] == level
+            _, _, _, yh = c.smap_grad(lib, lib_t, pred, pred_t, 1.5, wv, backward=False)
+        finally:
+            c.close()
+        out[level] = np.concatenate([[mse, gt], gw, yh]).view(np.int64)
+    assert np.array_equal(out[2], out[1]) and np.array_equal(out[2], out[0])
