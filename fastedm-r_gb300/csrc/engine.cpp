@@ -354,6 +354,24 @@ void* Context::buf(const std::string& name, size_t bytes)
   return b.p;
 }
 
+void* Context::try_buf(const std::string& name, size_t bytes)
+{
+  auto it = bufs_.find(name);
+  if (it != bufs_.end() && it->second.cap >= bytes)
+    return it->second.p;
+  void* p = nullptr;
+  if (cudaMalloc(&p, bytes) != cudaSuccess) {
+    cudaGetLastError();  // an allocation failure leaves the context usable
+    return nullptr;
+  }
+  if (it != bufs_.end() && it->second.p) {
+    ck(cudaStreamSynchronize(stream), "sync before realloc");
+    ck(cudaFree(it->second.p), "cudaFree");
+  }
+  bufs_[name] = DevBuf{ p, bytes };
+  return p;
+}
+
 void Context::upload(void* dst, const void* src, size_t bytes)
 {
   if (bytes) {
@@ -2127,9 +2145,11 @@ int smap_grad(Context& ctx, const double* lib, const double* lib_t, int n_lib, c
       const size_t per_row = level == 2 ? 3 + E : 2;
       const long long fit = (long long)(GRAD_CACHE_BUDGET / ((size_t)n_lib * per_row * 8));
       if (std::min(full, fit) * 2 >= full) {
-        a.cache_warps = std::min(full, fit);
-        a.cache_level = level;
-        a.cache = (double*)ctx.buf("adj_cache", (size_t)a.cache_warps * per_row * n_lib * 8);
+        a.cache = (double*)ctx.try_buf("adj_cache", (size_t)std::min(full, fit) * per_row * n_lib * 8);
+        if (a.cache) {
+          a.cache_warps = std::min(full, fit);
+          a.cache_level = level;
+        }
       }
     }
   }

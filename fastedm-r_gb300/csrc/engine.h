@@ -112,6 +112,9 @@ public:
   void reset_timing();
   // Grow-only named device buffers (the context's memory pool).
   void* buf(const std::string& name, size_t bytes);
+  // The same for an optional buffer: null (and the pool unchanged) when the
+  // device cannot provide it.
+  void* try_buf(const std::string& name, size_t bytes);
   // Grow-only named pinned host buffers, for uploads that need no staging;
   // the caller must not refill one while a copy from it is in flight.
   void* host_buf(const std::string& name, size_t bytes);

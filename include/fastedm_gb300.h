@@ -287,9 +287,13 @@ int fedm_host_plan(const fedm_args* args, int max_tasks, int* n_tasks, int* task
  *  fedm_smap_fwd: mse = mean (yhat - target)^2 over prediction points;
  *                 predictions [n_pred] (may be NULL).
  *  fedm_smap_bwd: mse and its gradient dmse_dtheta, dmse_dw [e_actual],
- *                 from the adjoint of the weighted normal equations (the
- *                 weights are recomputed in the backward pass, nothing of
- *                 size n_pred x n_lib is stored). */
+ *                 from the adjoint of the weighted normal equations.
+ *                 Nothing of size n_pred x n_lib is stored: each resident
+ *                 warp keeps its current point's per-row values (distance,
+ *                 weight, 1/d, per-lag products) in a slice of device
+ *                 memory that the context holds for later calls, up to
+ *                 8 GB; where that cannot be had, a smaller cache or none
+ *                 is used, with the same results. */
 int fedm_smap_fwd(fedm_ctx* ctx, const double* lib_manifold, const double* lib_targets, int n_lib,
                   const double* pred_manifold, const double* pred_targets, int n_pred, int e_actual, double theta,
                   const double* w, double* mse, double* predictions);
