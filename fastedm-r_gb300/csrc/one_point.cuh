@@ -156,25 +156,48 @@ __device__ __forceinline__ void scan_item_one(const GroupParams& g, const MixedR
         }
         __syncthreads();
         if (need) {
-          scanned += (unsigned long long)cnt;
-#pragma unroll 2
-          for (int ip = 0; ip < npairs; ip++) {
-            const float2* xr = tile + ip * EA;
-            float2 d = __fadd2_rn(xr[0], na[0]);
-            float2 sa = __fmul2_rn(d, d);
+          // the tile's sub-tiles in turn, each skipped when the bound from
+          // its own box is not below the point's current C-th value (which
+          // only decreases as the scan goes on)
+          const float2* sbox = m.boxes + (size_t)(T.box_off + tt * SPT) * EA;
+#pragma unroll 1
+          for (int u = 0; u < SPT; u++) {
+            const int r0 = u * BOX_ROWS;
+            if (r0 >= cnt)
+              break;
+            const int rn = min(BOX_ROWS, cnt - r0);
+            if constexpr (SPT > 1) {
+              float lbu = 0.f;
 #pragma unroll
-            for (int j = 1; j < EA; j++) {
-              d = __fadd2_rn(xr[j], na[j]);
-              sa = __ffma2_rn(d, d, sa);
+              for (int j = 0; j < EA; j++) {
+                const float2 b = sbox[u * EA + j];
+                const float p = -na[j].x;
+                const float d = p < b.x ? __fadd_rn(b.x, na[j].x) : (p > b.y ? __fadd_rn(b.y, na[j].x) : 0.f);
+                lbu = j == 0 ? __fmul_rn(d, d) : __fmaf_rn(d, d, lbu);
+              }
+              if (!(lbu < D0[C - 1]))
+                continue;
             }
-            if constexpr (PEN) {
-              const int2 pp = reinterpret_cast<const int2*>(tpan)[ip];
-              sa = __fadd2_rn(sa, make_float2(pp.x != ppan ? pen : 0.f, pp.y != ppan ? pen : 0.f));
-            }
-            if (fminf(sa.x, sa.y) < D0[C - 1]) {
-              const int2 lp = reinterpret_cast<const int2*>(tpos)[ip];
-              offer<C>(D0, I0, z0, zi0, sa.x, lp.x);
-              offer<C>(D0, I0, z0, zi0, sa.y, lp.y);
+            scanned += (unsigned long long)rn;
+#pragma unroll 2
+            for (int ip = r0 >> 1; ip < (r0 + rn + 1) >> 1; ip++) {
+              const float2* xr = tile + ip * EA;
+              float2 d = __fadd2_rn(xr[0], na[0]);
+              float2 sa = __fmul2_rn(d, d);
+#pragma unroll
+              for (int j = 1; j < EA; j++) {
+                d = __fadd2_rn(xr[j], na[j]);
+                sa = __ffma2_rn(d, d, sa);
+              }
+              if constexpr (PEN) {
+                const int2 pp = reinterpret_cast<const int2*>(tpan)[ip];
+                sa = __fadd2_rn(sa, make_float2(pp.x != ppan ? pen : 0.f, pp.y != ppan ? pen : 0.f));
+              }
+              if (fminf(sa.x, sa.y) < D0[C - 1]) {
+                const int2 lp = reinterpret_cast<const int2*>(tpos)[ip];
+                offer<C>(D0, I0, z0, zi0, sa.x, lp.x);
+                offer<C>(D0, I0, z0, zi0, sa.y, lp.y);
+              }
             }
           }
         }
