@@ -1233,7 +1233,7 @@ void run_group(Context& ctx, const Options& o, const std::vector<Task>& tasks, c
       cudaEventElapsedTime(&ms, f0, f1);
       ctx.timing.forecast_kernel_ms += ms;
       ctx.timing.forecast_launches += 1;
-      ctx.timing.kernel_launches += o.algorithm == 1 ? (gram_terms ? (tiles ? 4 : 3) : 2) : 1;
+      ctx.timing.kernel_launches += o.algorithm == 1 ? (gram_terms ? (tiles ? 4 : 3) : (Ea <= 8 ? 3 : 2)) : 1;
     }
   };
 

@@ -769,9 +769,38 @@ __global__ void all_forecast_kernel(GroupParams g, ChunkBuffers c, long long max
   smap_finish(g, T, p, prow, t, xs, n);
 }
 
+// The S-map's weights over every valid neighbour depend on theta only
+// through w = exp(-theta * (d / mean)) (src/edm.cpp:744-745).  One thread per
+// point forms mean (in library order, as the forecast kernels do) and the
+// ratios d / mean in place of the distances, once for every theta; invalid
+// rows keep their -1 mark.  Runs only before all_smap_kernel, the last
+// reader of the distance rows.
+__global__ void all_ratio_kernel(GroupParams g, ChunkBuffers c, long long max_nlib)
+{
+  const long long chunk = c.p_end - c.p_begin;
+  const long long q = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= chunk)
+    return;
+  const long long p = point_of(c, q);
+  const DevTask T = g.tasks[find_task(g, p)];
+  if (!T.all_mode || c.status[q] != PT_OK)
+    return;
+  double* dq = c.scratch + q * max_nlib;
+  double mean = 0;
+  for (int i = 0; i < T.n_lib; i++)
+    if (dq[i] >= 0)
+      mean += dq[i];
+  mean /= (double)c.nn_count[q];
+  const double ymean = rcp(mean);
+  for (int i = 0; i < T.n_lib; i++)
+    if (dq[i] >= 0)
+      dq[i] = dvd_r(dq[i], mean, ymean);
+}
+
 // S-map over every valid neighbour for E_a <= 8 (src/edm.cpp:737-814): the
 // all_forecast_kernel computation with the normal equations accumulated in
-// registers (the same operations in the same order, so the same bits).
+// registers (the same operations in the same order, so the same bits), on
+// the ratios d / mean that all_ratio_kernel left in the distance rows.
 template<int EA>
 __global__ void __launch_bounds__(128) all_smap_kernel(GroupParams g, ChunkBuffers c, long long max_nlib)
 {
@@ -791,15 +820,8 @@ __global__ void __launch_bounds__(128) all_smap_kernel(GroupParams g, ChunkBuffe
     early_rc(g, T.task, st, t);
     return;
   }
-  const double* dq = c.scratch + q * max_nlib;
+  const double* rq = c.scratch + q * max_nlib;  // d / mean per valid row
   const double theta = g.thetas[t];
-  const int ke = c.nn_count[q];
-  double mean = 0;
-  for (int i = 0; i < T.n_lib; i++)
-    if (dq[i] >= 0)
-      mean += dq[i];
-  mean /= (double)ke;
-  const double ymean = rcp(mean);
   double W[n][n], bv[n];
 #pragma unroll
   for (int a = 0; a < n; a++) {
@@ -809,10 +831,10 @@ __global__ void __launch_bounds__(128) all_smap_kernel(GroupParams g, ChunkBuffe
       W[a][b] = 0;
   }
   for (int i = 0; i < T.n_lib; i++) {
-    const double d = dq[i];
-    if (d < 0)
+    const double r = rq[i];
+    if (r < 0)
       continue;
-    const double w = exp_rn(-theta * dvd_r(d, mean, ymean));
+    const double w = exp_rn(-theta * r);
     const int row = g.lib_rows[T.lib_off + i];
     const double* fr = g.F + (size_t)row * EA;
     const double yl = w * g.lib_target[row];
@@ -1278,6 +1300,7 @@ void launch_forecast(const GroupParams& g, const ChunkBuffers& c, long long max_
     }
   }
   if (g.algorithm == 1 && g.Ea <= 8) {
+    all_ratio_kernel<<<(int)((chunk + 127) / 128), 128, 0, s>>>(g, c, max_nlib);
     switch (g.Ea) {
       case 1: all_smap_kernel<1><<<fb, 128, 0, s>>>(g, c, max_nlib); return;
       case 2: all_smap_kernel<2><<<fb, 128, 0, s>>>(g, c, max_nlib); return;
