@@ -36,10 +36,10 @@ METRIC = "CCM S-map predictions/s: batched FP32+FP64-fix vs plain FP64 GPU @|Î”Ï
 # DRAM bytes per S-map prediction point of the S-map kernel
 # (knn_one_kernel<4,8,4,1024,1,6>): ncu dram__bytes_read.sum +
 # dram__bytes_write.sum of one launch over the 2-replicate x 20-library
-# workload (4156.5 MB + 11224.8 MB) divided by its 1 999 880 points.  The
+# workload (4231.5 MB + 11340.9 MB) divided by its 1 999 880 points.  The
 # traffic is the solver's per-thread scratch and spills leaving L1, so it
 # scales with the points of a launch.
-SMAP_DRAM_BYTES_PER_POINT = 7691.0
+SMAP_DRAM_BYTES_PER_POINT = 7786.6
 
 
 def concurrent_calls(fedm, w, a, local, rhos, steps=2):
