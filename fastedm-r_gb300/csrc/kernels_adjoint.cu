@@ -32,8 +32,9 @@
 // (one warp per point at a time, points strided over the warps) and each
 // warp owns a slice of device memory for its point's per-row values.  At
 // cache level 2 pass 1 stores d_i, 1/d_i and the products
-// (z_ij - z_pj)(m_ij - m_pj), and pass 2 stores a_i^2, so that pass 3 reads
-// them instead of recomputing the distance, the exponential and the products;
+// (z_ij - z_pj)(m_ij - m_pj), and pass 2 (reading d_i) stores a_i^2, so that
+// pass 3 reads them instead of recomputing the distance, the exponential and
+// the products;
 // at level 1 (a library too large for level 2's budget) only d_i and a_i^2
 // are kept; at level 0 (larger still) every pass recomputes.  The scaled
 // library z = w * m is formed once per call.  The cached values are the ones
