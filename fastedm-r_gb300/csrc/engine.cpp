@@ -849,11 +849,32 @@ void run_group(Context& ctx, const Options& o, const std::vector<Task>& tasks, c
       auto it = offs.find(key);
       if (it == offs.end()) {
         auto c = ctx.lane_orders.find(key);
-        if (c == ctx.lane_orders.end())
-          c = ctx.lane_orders
-                  .emplace(key, morton_lane_order(job.hFp, Ea, Pl->data() + kt[j].pstart, kt[j].plen,
-                                                  ctx.point_order == 1 && Ea >= 4 ? 4 : 3))
-                  .first;
+        if (c == ctx.lane_orders.end()) {
+          const int dims = ctx.point_order == 1 && Ea >= 4 ? 4 : 3;
+          const int* rows = Pl->data() + kt[j].pstart;
+          const int len = kt[j].plen;
+          const std::vector<int>* kept = nullptr;
+          for (const auto& e : ctx.kept_lane_orders)
+            if (e.gen == ctx.series_gen && e.F == (const void*)job.hFp && e.dims == dims && (int)e.rows.size() == len &&
+                std::memcmp(e.rows.data(), rows, (size_t)len * sizeof(int)) == 0) {
+              kept = &e.order;
+              break;
+            }
+          if (kept) {
+            c = ctx.lane_orders.emplace(key, *kept).first;
+          } else {
+            c = ctx.lane_orders.emplace(key, morton_lane_order(job.hFp, Ea, rows, len, dims)).first;
+            // keep it for later calls on this series (at most 32 lists)
+            auto& kl = ctx.kept_lane_orders;
+            kl.erase(std::remove_if(kl.begin(), kl.end(),
+                                    [&](const Context::KeptLaneOrder& e) { return e.gen != ctx.series_gen; }),
+                     kl.end());
+            if (kl.size() >= 32)
+              kl.erase(kl.begin());
+            kl.push_back(Context::KeptLaneOrder{ ctx.series_gen, (const void*)job.hFp, dims,
+                                                 std::vector<int>(rows, rows + len), c->second });
+          }
+        }
         it = offs.emplace(key, (int)perm_pool.size()).first;
         perm_pool.insert(perm_pool.end(), c->second.begin(), c->second.end());
       }

@@ -79,6 +79,17 @@ public:
   // the lane orders computed during the current call, by (list, first row,
   // rows, manifold): a CCM call's batches share its prediction list
   std::map<std::tuple<const void*, int, int, const void*>, std::vector<int>> lane_orders;
+  // lane orders kept across calls on the same series (the simplex and the
+  // S-map call of one workflow order the same prediction lists alike), by
+  // series generation, host manifold, key dimensions and the list's rows
+  struct KeptLaneOrder
+  {
+    long long gen;
+    const void* F;
+    int dims;
+    std::vector<int> rows, order;
+  };
+  std::vector<KeptLaneOrder> kept_lane_orders;
   // Spatially ordered library scans of the one-point mixed kernels (lists
   // of 2 048 to 262 144 rows, scanned in a Morton order of their rows with
   // tiles that no point of a work item can use skipped; the same bits):
