@@ -830,7 +830,7 @@ void run_group(Context& ctx, const Options& o, const std::vector<Task>& tasks, c
     ctx.timing.scan_flops += 3LL * Ea * d.n_pred * (long long)d.n_lib;
   // lane orders of the one-point mixed kernels: per kernel task, its
   // prediction rows in Morton order of their coordinates (computed once per
-  // list and call).  Not for per-panel sub-tasks: their small libraries make
+  // list and call, or taken from an earlier call on the same series).  Not for per-panel sub-tasks: their small libraries make
   // every item solve-bound alike, and on 512 independent panels the orders
   // gained no device time while their host cost lowered the end-to-end rate
   // by 5%.
